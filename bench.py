@@ -1,0 +1,388 @@
+#!/usr/bin/env python3
+"""LLG spin-steps/s on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+                    [--precision fp32c|fp64] [--impl ours|reference]
+
+A step is one stochastic-LLG time step (Heun: predictor + corrector, RK4:
+four stages) over every spin of the workload.  Default workload: bcc,
+2-site conventional basis, 64^3 cells (524,288 spins), isotropic exchange
+to the third shell, cubic anisotropy, T = 300 K thermal field, Heun,
+FP32 spins with compensated neighbour sums (the benchmark's FP32 form).
+
+Timing: W untimed steps, then K timed steps, each bracketed by CUDA events
+on the solver's stream with an L2 flush (a 256 MiB write) between steps, a
+barrier + synchronize on both sides, max over ranks.  value = spins x K /
+sum of step times.  e2e: the same steps through the C ABI with the FP64
+spin state copied from pinned host memory before and back after every step.
+roofline: the dominant stage kernel's algorithmic bytes per launch / its
+mean CUDA-event duration, against the measured HBM copy bandwidth.
+cpu_baseline / --impl reference: the oracle's restatement of the
+reference's CPU Heun path (CSR SpMV, per-term field arrays, serial noise
+draw as the reference does) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from jams_gb300 import workloads as W  # noqa: E402
+
+# algorithmic bytes per spin per stage launch (state vectors that must cross
+# HBM between grid-wide dependency points; stencil and noise cost 0 bytes)
+STAGE_BYTES = {
+    ("heun", "fp32c"): [24, 36],    # predictor: r s0, w sp; corrector: r s0, r sp, w s1
+    ("heun", "fp64"): [72, 96],     # + ds written / read (the FP64 form stores it)
+    ("rk4", "fp32c"): [36, 60, 60, 48],
+    ("rk4", "fp64"): [72, 120, 120, 96],
+}
+STAGE_NAMES = {"heun": ["heun_predict", "heun_correct"], "rk4": ["rk4_stage1", "rk4_stage2", "rk4_stage3",
+                                                                 "rk4_stage4"]}
+
+WORKLOADS = {
+    # bcc 64^3 x 2, J1..J3, cubic K, 300 K, Heun dt 0.5 fs (the benchmark's headline configuration)
+    "bcc64_3shell": lambda: W.bcc_three_shell(L=64, T=300.0, start="+z"),
+    # simple-cubic 32^3, T = 0, Heun dt 1 fs (the reference's CPU-runnable case)
+    "sc32": lambda: W.sc_ferromagnet(L=32, T=0.0),
+    # bcc 256^3 x 2 (33.5 M spins), 500 K, both readings of its Hamiltonian
+    "bcc256_nn": lambda: W.bcc_nearest_neighbour(L=256, T=500.0),
+    "bcc256_3shell": lambda: W.bcc_three_shell(L=256, T=500.0),
+    # 256 simple-cubic replicas, L in {16..64}, T in 0..1200 K
+    "sc_sweep256": lambda: W.sc_temperature_sweep(),
+    # triangular 2048^2 x 16 fields, tensor exchange + DMI, RK4, 5 K
+    "tri2048_dmi_x16": lambda: W.triangular_dmi_field_sweep(),
+}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2000)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--workload", default="bcc64_3shell", choices=sorted(WORKLOADS))
+    p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--profile-steps", type=int, default=50)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ clocks --
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- CPU port --
+
+def cpu_port_rate(w: W.Workload, seconds: float = 15.0, max_steps: int = 200, warm: int = 1):
+    """Spin-steps/s of the oracle (the reference's CPU Heun/RK4 path restated
+    in C, OpenMP over all host cores, serial noise draw as the reference)
+    on replica 0 of the workload (replicas are independent)."""
+    from oracle import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    sim = O.OracleSim(w, 0, serial_noise=True, threads=threads)
+    s = W.initial_state(w, 0)
+    s = sim.run(s, warm, first_step=0)
+    t0 = time.perf_counter()
+    s = sim.run(s, 1, first_step=warm)
+    one = time.perf_counter() - t0
+    n = int(max(1, min(max_steps, seconds / max(one, 1e-9))))
+    t0 = time.perf_counter()
+    sim.run(s, n, first_step=warm + 1)
+    dt = time.perf_counter() - t0
+    return sim.n * n / dt, threads, n, sim.n
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU path of the reference (restated in the
+    oracle) on the host cores, K timed steps after W warm-up steps."""
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+
+    w = WORKLOADS[args.workload]()
+    O.build()
+    threads = os.cpu_count() or 1
+    sim = O.OracleSim(w, 0, serial_noise=True, threads=threads)
+    s = W.initial_state(w, 0)
+    s = sim.run(s, args.warmup, first_step=0)
+    # bound the run to a few minutes: time one step, cap K accordingly
+    t0 = time.perf_counter()
+    s = sim.run(s, 1, first_step=args.warmup)
+    one = time.perf_counter() - t0
+    k = max(1, min(args.steps, int(120.0 / max(one, 1e-9))))
+    t0 = time.perf_counter()
+    sim.run(s, k, first_step=args.warmup + 1)
+    dt = time.perf_counter() - t0
+    value = sim.n * k / dt
+    line = {
+        "metric": "LLG spin-steps/s", "value": value, "unit": "spin-steps/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": k, "warmup": args.warmup, "ms_per_step": 1e3 * dt / k,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": args.workload, "spins": sim.n, "description": w.description,
+                                         "replicas_timed": 1},
+        "cpu_baseline": {"value": value, "unit": "spin-steps/s", "cores": threads, "kind": "port",
+                         "sample": "%d Heun steps of replica 0 (%d spins), full lattice" % (k, sim.n)},
+        "e2e": {"value": value, "unit": "spin-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# -------------------------------------------------------------------- GPU --
+
+def traffic_from_profiles(workload: str, kernel: str, precision: str):
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if not os.path.exists(path):
+        return None
+    try:
+        d = json.load(open(path))
+        return d.get(workload, {}).get(precision, {}).get(kernel)
+    except (ValueError, OSError):
+        return None
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from jams_gb300 import build as B
+    from jams_gb300 import llg
+
+    B.build()
+    w = WORKLOADS[args.workload]()
+    prec = llg.FP32C if args.precision == "fp32c" else llg.FP64
+    integ = "heun" if w.model.integrator == W.HEUN else "rk4"
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)  # torch work (L2 flush, events) and the solver share one stream
+    sol = llg.Solver(w, precision=prec, device=local)
+    sol.set_stream(stream.cuda_stream)
+    for r in range(len(w.replicas)):
+        sol.set_state(W.initial_state(w, r), r)
+    n_spins = sol.num_spins(-1)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    # warm-up (also builds nothing lazily: single steps use direct launches)
+    for _ in range(args.warmup):
+        sol.step(1)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, L2 flushed between steps
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches = 0
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        evs[k][0].record(stream)
+        sol.step(1)
+        evs[k][1].record(stream)
+        launches += sol.last_launch_count
+    torch.cuda.synchronize()
+    barrier(world)
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = max_over_ranks(sum(step_ms), world, torch.device("cuda", local))
+    ms_per_step = total_ms / args.steps
+    value = world * n_spins * args.steps / (total_ms * 1e-3)
+    sol.synchronize()
+
+    # ---- per-stage kernel durations (same flush between steps)
+    ns = len(STAGE_BYTES[(integ, args.precision)])
+    stage_ms = np.zeros(ns)
+    for _ in range(args.profile_steps):
+        flush.fill_(1.0)
+        stage_ms += sol.profile_stages(1)[:ns]
+    stage_ms /= args.profile_steps
+    dom = int(np.argmax(stage_ms))
+    bytes_per_launch = STAGE_BYTES[(integ, args.precision)][dom] * n_spins
+    achieved = bytes_per_launch / (stage_ms[dom] * 1e-3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    kernel_name = STAGE_NAMES[integ][dom] + ("_f32" if args.precision == "fp32c" else "_f64")
+    traffic = traffic_from_profiles(args.workload, kernel_name, args.precision)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": kernel_name, "peak_source": peak_src,
+                "stage_ms": [float(x) for x in stage_ms],
+                "algorithmic_bytes_per_spin_step": int(sum(STAGE_BYTES[(integ, args.precision)])),
+                "step_frac": (sum(STAGE_BYTES[(integ, args.precision)]) * n_spins / (ms_per_step * 1e-3) / 1e9)
+                / peak}
+
+    # ---- steady state without flush: blocks of 100 steps as CUDA graphs
+    blk = 100
+    sol.step(blk)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nblk = max(1, min(10, args.steps // blk))
+    e0.record(stream)
+    for _ in range(nblk):
+        sol.step(blk)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    graph_ms = e0.elapsed_time(e1) / (nblk * blk)
+    steady = {"value": n_spins / (graph_ms * 1e-3), "ms_per_step": graph_ms,
+              "note": "100-step CUDA-graph blocks, no L2 flush (the state stays L2-resident when it fits)"}
+
+    # ---- e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((n_spins, 3), dtype=torch.float64, pin_memory=True)
+        host_np = host.numpy()
+        host_np[:] = sol.get_state(-1)
+        ke = max(10, min(200, args.steps // 10))
+        for _ in range(3):
+            sol.set_state(host_np, -1)
+            sol.step(1)
+            sol.get_state(-1, out=host_np)
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            sol.set_state(host_np, -1)
+            sol.step(1)
+            sol.get_state(-1, out=host_np)
+        dt = time.perf_counter() - t0
+        dt = max_over_ranks(dt, world, torch.device("cuda", local))
+        e2e = {"value": world * n_spins * ke / dt, "unit": "spin-steps/s", "h2d_bytes_per_step": n_spins * 24,
+               "d2h_bytes_per_step": n_spins * 24, "steps": ke}
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, cores, n_steps, n_rep = cpu_port_rate(w)
+        cpu = {"value": rate, "unit": "spin-steps/s", "cores": cores, "kind": "port",
+               "sample": "%d Heun/RK4 steps of replica 0 (%d spins), oracle restatement of the reference CPU path"
+                         % (n_steps, n_rep)}
+
+    line = {
+        "metric": "LLG spin-steps/s", "value": value, "unit": "spin-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32c" else "f64",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "description": w.description, "spins": n_spins,
+                   "replicas": len(w.replicas), "precision": args.precision, "integrator": integ,
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas" if world > 1
+                   else "single GPU"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+        "steady_state_graph": steady, "wall_s_timed_region": t_wall,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    sol.close()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,191 @@
+/*
+ * jams_llg.h - C ABI of the GB300 (sm_103a) stochastic Landau-Lifshitz-Gilbert
+ * step library (libjams_llg.so).
+ *
+ * The library replaces the GPU LLG hot path of JAMS (stonerlab/jams):
+ *   CUDAHeunLLGSolver::run        src/jams/solvers/cuda_llg_heun.cu:64-122
+ *   CudaRK4BaseSolver::run        src/jams/solvers/cuda_rk4_base.cu:50-108
+ *   CudaSolver::compute_fields    src/jams/cuda/cuda_solver.cc:11-26
+ *   SparseInteractionHamiltonian::calculate_fields
+ *                                 src/jams/hamiltonian/sparse_interaction.cc:36-45
+ *   CudaUniaxialAnisotropyHamiltonian / CubicAnisotropyHamiltonian /
+ *   CudaAppliedFieldHamiltonian::calculate_fields
+ *                                 src/jams/hamiltonian/cuda_uniaxial_anisotropy.cu:28-32,
+ *                                 src/jams/hamiltonian/cubic_anisotropy.cc:197-226,
+ *                                 src/jams/hamiltonian/cuda_applied_field.cu:10-23
+ *   CudaThermostatClassical::update
+ *                                 src/jams/thermostats/cuda_thermostat_classical.cc:47-56
+ * with one fused pass per integrator stage (field of every term + thermal
+ * noise + LLG update) and a batched form over independent replicas.
+ *
+ * Conventions (those of the reference):
+ *   spins   N x 3 row-major doubles, site index ((i*L2 + j)*L3 + k)*nb + m
+ *           (src/jams/core/lattice.cc:617-651)
+ *   energy  meV; fields of the terms in meV (-dE/dS, not divided by mu_s)
+ *   mu_s    meV/T, gamma rad/ps/T, dt ps, temperature K, B tesla
+ *
+ * Every function returns 0 on success or a negative LLG_ERR_* code; the
+ * message is available from llg_last_error(handle) (or with a NULL handle for
+ * failures before a handle exists).  Nothing here throws across the ABI.
+ */
+#ifndef JAMS_LLG_H
+#define JAMS_LLG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LLG_ABI_VERSION 1
+
+/* status codes */
+enum {
+  LLG_OK = 0,
+  LLG_ERR_BAD_DESC = -1,     /* invalid descriptor or argument */
+  LLG_ERR_OOM = -2,          /* device or host allocation failed */
+  LLG_ERR_CUDA = -3,         /* CUDA launch or runtime error */
+  LLG_ERR_TIMEOUT = -4,      /* a device-side wait ran out of iterations */
+  LLG_ERR_NONFINITE = -5,    /* a spin became NaN or infinite */
+  LLG_ERR_NO_DEVICE = -6,    /* no usable sm_103 device */
+  LLG_ERR_UNSUPPORTED = -7   /* combination not implemented */
+};
+
+/* arithmetic form */
+enum {
+  LLG_FP64 = 0,   /* plain FP64, same association order as the reference CPU
+                     path: results equal the CPU solver's bit for bit */
+  LLG_FP32C = 1   /* FP32 spins/fields, compensated neighbour sums, FP64
+                     noise prefactors and reductions */
+};
+
+enum { LLG_HEUN = 0, LLG_RK4 = 1 };
+
+/* Hamiltonian term kinds, summed in list order like Solver::compute_fields
+   (src/jams/core/solver.cc:43-57) */
+enum {
+  LLG_TERM_EXCHANGE = 0,      /* module "exchange": bilinear 3x3 tensors */
+  LLG_TERM_UNIAXIAL = 1,      /* module "uniaxial": -K (S.a)^p, p = 2, 4, 6 */
+  LLG_TERM_CUBIC = 2,         /* module "cubic": K1 or K2 cubic anisotropy */
+  LLG_TERM_APPLIED_FIELD = 3  /* module "applied-field"/"zeeman": mu_s B */
+};
+
+typedef struct {
+  int32_t kind;
+  int32_t order;          /* uniaxial power (2, 4, 6); cubic order (1, 2) */
+  /* exchange template: entry e couples basis site bi[e] of cell c to basis
+     site bj[e] of cell c + T[3e..3e+2] with tensor J[9e..9e+8] (meV,
+     row-major) - the post-symmetry interaction list of
+     src/jams/core/interactions.cc:292-348 */
+  int32_t n_int;
+  const int32_t *bi;
+  const int32_t *bj;
+  const int32_t *T;
+  const double *J;
+  /* anisotropy: magnitude per basis site (meV) and unit axes per basis site
+     (uniaxial: 3 doubles; cubic: 9 doubles u, v, w) */
+  const double *K;
+  const double *axis;
+  double B[3];            /* applied field (T) */
+} llg_term;
+
+typedef struct {
+  int32_t L[3];           /* unit cells along a1, a2, a3 */
+  double temperature;     /* K */
+  double B[3];            /* replaces the applied-field term's B if use_B */
+  int32_t use_B;
+} llg_replica;
+
+typedef struct {
+  int32_t abi_version;    /* LLG_ABI_VERSION */
+  int32_t nb;             /* basis sites per cell (one material each) */
+  int32_t periodic[3];
+  const double *mus;      /* nb: mu_s (meV/T) */
+  const double *gyro;     /* nb: gamma (rad/ps/T), gilbert prefactor applied */
+  const double *alpha;    /* nb */
+  int32_t n_terms;
+  const llg_term *terms;
+  double dt;              /* ps (t_step / 1e-12) */
+  int32_t gilbert_prefactor; /* noise amplitude / (1 + alpha^2) */
+  int32_t integrator;     /* LLG_HEUN or LLG_RK4 */
+  int32_t precision;      /* LLG_FP64 or LLG_FP32C */
+  int32_t rk4_normalise_stages; /* FP32C RK4: renormalise every stage */
+  uint64_t seed;          /* Philox key of the thermal noise */
+  int32_t n_replicas;
+  const llg_replica *replicas;
+  int32_t device;         /* CUDA ordinal */
+  int32_t steps_per_graph;/* steps captured per CUDA graph (0: 100) */
+} llg_desc;
+
+typedef struct llg_handle llg_handle;
+
+/* Creates the solver state on the device (Solver::initialize +
+   Hamiltonian::create for the listed terms, src/jams/core/solver.cc:60-77,
+   src/jams/core/hamiltonian.cc:80-115).  Spins start at +z. */
+int llg_create(const llg_desc *desc, llg_handle **out);
+
+void llg_destroy(llg_handle *h);
+
+/* message of the last failure on h (thread-local when h is NULL) */
+const char *llg_last_error(const llg_handle *h);
+
+int64_t llg_num_spins(const llg_handle *h, int32_t replica);
+int32_t llg_num_replicas(const llg_handle *h);
+
+/* Spin state of one replica (replica < 0: all replicas back to back), host
+   buffers of N x 3 doubles.  Set normalises nothing (the reference loads
+   spins as given, src/jams/core/lattice.cc:741-748). */
+int llg_set_state(llg_handle *h, int32_t replica, const double *s_host);
+int llg_get_state(llg_handle *h, int32_t replica, double *s_host);
+
+/* Same with device buffers (the globals::s.device_data() of the reference). */
+int llg_set_state_device(llg_handle *h, int32_t replica, const double *s_dev);
+int llg_get_state_device(llg_handle *h, int32_t replica, double *s_dev);
+
+/* Advances every replica nsteps steps (Solver::run called nsteps times;
+   src/jams/core/jams++.cc:333-347).  Asynchronous on the handle's stream;
+   full blocks of steps_per_graph steps run as one CUDA graph launch. */
+int llg_step(llg_handle *h, int32_t nsteps);
+
+/* Waits for the handle's stream and reports device-side status
+   (LLG_ERR_NONFINITE when a spin became NaN or infinite). */
+int llg_synchronize(llg_handle *h);
+
+int64_t llg_iteration(const llg_handle *h);
+int llg_set_iteration(llg_handle *h, int64_t iteration);
+
+/* Per-replica physics (Physics::temperature, applied-field B). */
+int llg_set_temperature(llg_handle *h, int32_t replica, double temperature);
+int llg_set_field(llg_handle *h, int32_t replica, const double B[3]);
+
+/* Total field (meV) at the current spins, N x 3, summed over the terms in
+   order (CudaSolver::compute_fields, src/jams/cuda/cuda_solver.cc:11-26). */
+int llg_fields(llg_handle *h, int32_t replica, double *h_host);
+
+/* FP64 on-device reductions of one replica: m4 = (Mx, My, Mz, |M|) with
+   M = sum mu_s S / sum mu_s (src/jams/monitors/magnetisation.cc:77-104);
+   e_terms[n_terms] = total energy of each term in meV
+   (Hamiltonian::calculate_total_energy). */
+int llg_observables(llg_handle *h, int32_t replica, double *m4, double *e_terms);
+
+/* Geometric topological charge of a one-basis-site triangular monolayer
+   replica (src/jams/monitors/topological_charge_geometrical_def.cc:159-181). */
+int llg_topological_charge(llg_handle *h, int32_t replica, double *q);
+
+/* Uses a caller-owned cudaStream_t (NULL: the handle's own stream). */
+int llg_set_stream(llg_handle *h, void *cuda_stream);
+
+/* Number of kernel launches issued by the last llg_step or
+   llg_profile_stages call. */
+int64_t llg_last_launch_count(const llg_handle *h);
+
+/* Advances nsteps steps like llg_step, without graphs, with a CUDA event
+   pair around every stage kernel; ms[k] = mean duration (ms) of stage k
+   (Heun: predictor, corrector; RK4: stages 1-4).  Synchronous. */
+int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JAMS_LLG_H */

@@ -1,0 +1,978 @@
+// Host runtime of libjams_llg.so: validates an llg_desc, builds the stencil
+// tables, owns the device buffers and streams, runs blocks of steps as CUDA
+// graphs and exposes the C ABI declared in include/jams_llg.h.
+//
+// Stencil tables.  The reference expands the interaction template into a
+// 3N x 3N CSR matrix (src/jams/core/interactions.cc:350-396,
+// src/jams/containers/sparse_matrix_builder.h:186-248).  On a periodic or
+// open lattice without impurities the neighbour of site (c, b) through
+// template entry e is site (c + T_e wrapped, bj_e), so j - i depends only on
+// which axes wrap at c.  Cells are grouped into boundary classes per axis
+// (c < R, interior, c >= L - R, with R the stencil reach; every coordinate is
+// its own class when L <= 2R + 1) and one table of offsets j - i per (basis
+// site, class) describes the whole matrix.  For the FP64 form the entries of
+// each class are stored in ascending j, the order in which the CSR row sum
+// visits them.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/jams_llg.h"
+#include "llg_internal.h"
+
+#include "llg_kernels.h"
+
+using namespace jams_llg;
+
+namespace {
+
+thread_local std::string g_tls_error;
+
+// src/jams/helpers/consts.h:32
+constexpr double kBoltzmannIU = 0.0861733326;
+
+struct ExchangeHost {
+  int term;
+  int zmax = 0;        // FP64 list length per (b, class)
+  int nslot_max = 0;   // FP32 slots per (b, class)
+  // FP32 slot layout per basis site: entry index of each slot, groups, rest
+  std::vector<int> slot_entry[kMaxBasis];
+  std::vector<int> group_end[kMaxBasis];
+  std::vector<double> group_j[kMaxBasis];
+  std::vector<float> rest_j;  // [nb][kMaxSlots][9]
+  std::vector<double> J64;    // [n_entries][9]
+  std::vector<uint16_t> mask; // [n_entries]
+};
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~DevBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    reset();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void**)&p, count * sizeof(T));
+  }
+};
+
+struct GraphKey {
+  int parity;
+  int nsteps;
+  bool operator<(const GraphKey& o) const { return parity != o.parity ? parity < o.parity : nsteps < o.nsteps; }
+};
+
+}  // namespace
+
+struct llg_handle {
+  std::string err;
+  int device = 0;
+  bool fp64 = false;
+  int integrator = LLG_HEUN;
+  int nb = 1;
+  int nterms = 0;
+  int steps_per_graph = 100;
+  std::vector<llg_term> terms_copy;
+  std::vector<double> term_B;  // applied-field B of the desc (per term, 3)
+  std::vector<ReplicaDev> reps;
+  std::vector<double> rep_T;
+  std::vector<int2> tiles;
+  std::vector<int> rep_first_tile, rep_ntiles;
+  int64_t npad = 0;
+  double mus[kMaxBasis], gyro[kMaxBasis], alpha[kMaxBasis];
+  bool gilbert = false;
+  double dt = 0.0;
+  Params P{};
+  // device
+  DevBuf<unsigned char> state[3];  // spin planes (float or double)
+  DevBuf<unsigned char> aux;       // FP64 Heun ds / RK4 accumulator
+  DevBuf<ReplicaDev> d_rep;
+  DevBuf<int2> d_tiles;
+  DevBuf<int32_t> d_tab32;
+  DevBuf<int2> d_tab64;
+  DevBuf<int32_t> d_cnt64;
+  DevBuf<float> d_rest[kMaxExchange];
+  DevBuf<double> d_J64[kMaxExchange];
+  DevBuf<uint16_t> d_mask[kMaxExchange];
+  DevBuf<unsigned int> d_status;
+  DevBuf<uint64_t> d_step_base;
+  DevBuf<double> d_scratch;        // N x 3 doubles for host transfers
+  DevBuf<double> d_partials;
+  std::vector<double> h_partials;
+  int cur = 0;                     // index of the buffer holding the state
+  int64_t iteration = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::map<GraphKey, cudaGraphExec_t> graphs;
+  int64_t last_launches = 0;
+  bool params_dirty = false;
+
+  ~llg_handle() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    g_tls_error = buf;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? LLG_ERR_OOM : LLG_ERR_CUDA, "%s: %s", what,
+                cudaGetErrorString(e));
+  }
+};
+
+namespace {
+
+int tls_fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_tls_error = buf;
+  return code;
+}
+
+size_t real_size(const llg_handle* h) { return h->fp64 ? sizeof(double) : sizeof(float); }
+
+int axis_classes(int L, int R) { return (L <= 2 * R + 1) ? L : 2 * R + 1; }
+
+int class_rep(int k, int L, int R, int ncls) {
+  if (ncls == L) return k;
+  if (k <= R) return k;
+  return L - R + (k - R - 1);
+}
+
+// builds FP32 slot layout (groups of equal isotropic J, then anisotropic rests)
+int build_slots(llg_handle* h, const llg_term& t, ExchangeHost& X) {
+  const int nb = h->nb;
+  X.rest_j.assign((size_t)nb * kMaxSlots * 9, 0.f);
+  for (int b = 0; b < nb; ++b) {
+    std::vector<double> iso_vals;
+    std::vector<std::vector<int>> iso_members;
+    std::vector<int> rest_members;
+    for (int e = 0; e < t.n_int; ++e) {
+      if (t.bi[e] != b) continue;
+      const double* J = t.J + 9 * e;
+      double mx = 0.0;
+      for (int a = 0; a < 9; ++a) mx = std::max(mx, std::fabs(J[a]));
+      if (!(mx > 0.0)) continue;  // exchange.cc:166: only tensors with max|J| > 0
+      double iso = 0.0;
+      if (J[0] == J[4] && J[4] == J[8]) iso = J[0];
+      bool rest = false;
+      for (int a = 0; a < 9; ++a) {
+        const double r = J[a] - ((a % 4 == 0) ? iso : 0.0);
+        if (r != 0.0) rest = true;
+      }
+      if (iso != 0.0) {
+        size_t g = 0;
+        for (; g < iso_vals.size(); ++g)
+          if (iso_vals[g] == iso) break;
+        if (g == iso_vals.size()) {
+          iso_vals.push_back(iso);
+          iso_members.emplace_back();
+        }
+        iso_members[g].push_back(e);
+      }
+      if (rest) rest_members.push_back(e);
+    }
+    if ((int)iso_vals.size() > kMaxGroups)
+      return h->fail(LLG_ERR_UNSUPPORTED, "more than %d distinct isotropic exchange values on basis site %d",
+                     kMaxGroups, b);
+    size_t iso_slots = 0;
+    for (auto& g : iso_members) iso_slots += g.size();
+    if (iso_slots > (size_t)kMaxSlots)
+      return h->fail(LLG_ERR_UNSUPPORTED, "more than %d neighbour slots on basis site %d", kMaxSlots, b);
+    for (size_t g = 0; g < iso_vals.size(); ++g) {
+      for (int e : iso_members[g]) X.slot_entry[b].push_back(e);
+      X.group_end[b].push_back((int)X.slot_entry[b].size());
+      X.group_j[b].push_back(iso_vals[g]);
+    }
+    for (int e : rest_members) {
+      const int slot = (int)X.slot_entry[b].size();
+      if (slot >= kMaxSlots)
+        return h->fail(LLG_ERR_UNSUPPORTED, "more than %d neighbour slots on basis site %d", kMaxSlots, b);
+      X.slot_entry[b].push_back(e);
+      const double* J = t.J + 9 * e;
+      const double iso = (J[0] == J[4] && J[4] == J[8]) ? J[0] : 0.0;
+      for (int a = 0; a < 9; ++a)
+        X.rest_j[((size_t)b * kMaxSlots + slot) * 9 + a] = (float)(J[a] - ((a % 4 == 0) ? iso : 0.0));
+    }
+    X.nslot_max = std::max<int>(X.nslot_max, (int)X.slot_entry[b].size());
+  }
+  X.J64.assign((size_t)t.n_int * 9, 0.0);
+  X.mask.assign((size_t)t.n_int, 0);
+  for (int e = 0; e < t.n_int; ++e) {
+    uint16_t m = 0;
+    for (int a = 0; a < 9; ++a) {
+      X.J64[(size_t)e * 9 + a] = t.J[9 * e + a];
+      if (t.J[9 * e + a] != 0.0) m |= (uint16_t)(1u << a);
+    }
+    X.mask[e] = m;
+  }
+  for (int b = 0; b < nb; ++b) {
+    int z = 0;
+    for (int e = 0; e < t.n_int; ++e)
+      if (t.bi[e] == b) ++z;
+    X.zmax = std::max(X.zmax, z);
+  }
+  return 0;
+}
+
+int build(llg_handle* h, const llg_desc* d) {
+  if (!d) return h->fail(LLG_ERR_BAD_DESC, "null descriptor");
+  if (d->abi_version != LLG_ABI_VERSION)
+    return h->fail(LLG_ERR_BAD_DESC, "abi_version %d, library has %d", d->abi_version, LLG_ABI_VERSION);
+  if (d->nb < 1 || d->nb > kMaxBasis) return h->fail(LLG_ERR_BAD_DESC, "nb must be in [1, %d]", kMaxBasis);
+  if (d->n_terms < 0 || d->n_terms > kMaxTerms)
+    return h->fail(LLG_ERR_BAD_DESC, "n_terms must be in [0, %d]", kMaxTerms);
+  if (d->n_terms > 0 && !d->terms) return h->fail(LLG_ERR_BAD_DESC, "terms is null");
+  if (d->n_replicas < 1 || !d->replicas) return h->fail(LLG_ERR_BAD_DESC, "need at least one replica");
+  if (!(d->dt > 0.0) || !std::isfinite(d->dt)) return h->fail(LLG_ERR_BAD_DESC, "dt must be positive");
+  if (!d->mus || !d->gyro || !d->alpha) return h->fail(LLG_ERR_BAD_DESC, "material arrays are null");
+  if (d->precision != LLG_FP64 && d->precision != LLG_FP32C)
+    return h->fail(LLG_ERR_BAD_DESC, "unknown precision %d", d->precision);
+  if (d->integrator != LLG_HEUN && d->integrator != LLG_RK4)
+    return h->fail(LLG_ERR_BAD_DESC, "unknown integrator %d", d->integrator);
+  h->fp64 = d->precision == LLG_FP64;
+  h->integrator = d->integrator;
+  h->nb = d->nb;
+  h->nterms = d->n_terms;
+  h->dt = d->dt;
+  h->gilbert = d->gilbert_prefactor != 0;
+  h->steps_per_graph = d->steps_per_graph > 0 ? d->steps_per_graph : 100;
+  for (int b = 0; b < d->nb; ++b) {
+    h->mus[b] = d->mus[b];
+    h->gyro[b] = d->gyro[b];
+    h->alpha[b] = d->alpha[b];
+    if (!(d->mus[b] > 0.0)) return h->fail(LLG_ERR_BAD_DESC, "mu_s of basis site %d must be positive", b);
+  }
+
+  Params& P = h->P;
+  P = Params{};
+  P.nb = d->nb;
+  P.nterms = d->n_terms;
+  P.dt = d->dt;
+  P.dt32 = (float)d->dt;
+  P.seed = d->seed;
+  P.rk4_normalise_stages = d->rk4_normalise_stages;
+  for (int b = 0; b < d->nb; ++b) {
+    P.mus[b] = d->mus[b];
+    P.gyro[b] = d->gyro[b];
+    P.alpha[b] = d->alpha[b];
+    // src/jams/solvers/cpu_llg_heun.cc:36-43
+    double denominator = 1.0;
+    if (h->gilbert) denominator = 1.0 + d->alpha[b] * d->alpha[b];
+    P.sigma[b] = std::sqrt((2.0 * kBoltzmannIU * d->alpha[b]) / (d->mus[b] * d->gyro[b] * d->dt * denominator));
+    P.inv_mus32[b] = (float)(1.0 / d->mus[b]);
+    P.mus32[b] = (float)d->mus[b];
+    P.gyro32[b] = (float)d->gyro[b];
+    P.alpha32[b] = (float)d->alpha[b];
+  }
+
+  // terms
+  std::vector<ExchangeHost> ex;
+  h->term_B.assign((size_t)d->n_terms * 3, 0.0);
+  int field_terms = 0;
+  for (int t = 0; t < d->n_terms; ++t) {
+    const llg_term& T = d->terms[t];
+    TermDev& TD = P.term[t];
+    TD.kind = T.kind;
+    TD.order = T.order;
+    TD.exch = -1;
+    switch (T.kind) {
+      case LLG_TERM_EXCHANGE: {
+        if ((int)ex.size() >= kMaxExchange)
+          return h->fail(LLG_ERR_UNSUPPORTED, "more than %d exchange terms", kMaxExchange);
+        if (T.n_int < 0 || (T.n_int > 0 && (!T.bi || !T.bj || !T.T || !T.J)))
+          return h->fail(LLG_ERR_BAD_DESC, "exchange term %d has null arrays", t);
+        for (int e = 0; e < T.n_int; ++e) {
+          if (T.bi[e] < 0 || T.bi[e] >= d->nb || T.bj[e] < 0 || T.bj[e] >= d->nb)
+            return h->fail(LLG_ERR_BAD_DESC, "exchange term %d entry %d: basis index outside [0, %d)", t, e,
+                           d->nb);
+          for (int a = 0; a < 9; ++a)
+            if (!std::isfinite(T.J[9 * e + a]))
+              return h->fail(LLG_ERR_BAD_DESC, "exchange term %d entry %d: non-finite J", t, e);
+        }
+        ExchangeHost X;
+        X.term = t;
+        int rc = build_slots(h, T, X);
+        if (rc) return rc;
+        TD.exch = (int)ex.size();
+        ex.push_back(std::move(X));
+        break;
+      }
+      case LLG_TERM_UNIAXIAL:
+      case LLG_TERM_CUBIC: {
+        if (!T.K || !T.axis) return h->fail(LLG_ERR_BAD_DESC, "anisotropy term %d has null arrays", t);
+        if (T.kind == LLG_TERM_UNIAXIAL && !(T.order == 2 || T.order == 4 || T.order == 6))
+          return h->fail(LLG_ERR_BAD_DESC, "uniaxial power must be 2, 4 or 6");
+        if (T.kind == LLG_TERM_CUBIC && !(T.order == 1 || T.order == 2))
+          return h->fail(LLG_ERR_BAD_DESC, "cubic order must be 1 or 2");
+        const int na = T.kind == LLG_TERM_UNIAXIAL ? 3 : 9;
+        for (int b = 0; b < d->nb; ++b) {
+          TD.K[b] = T.K[b];
+          TD.Kf[b] = (float)T.K[b];
+          for (int a = 0; a < na; ++a) {
+            TD.axis[b][a] = T.axis[na * b + a];
+            TD.axisf[b][a] = (float)T.axis[na * b + a];
+          }
+        }
+        break;
+      }
+      case LLG_TERM_APPLIED_FIELD:
+        for (int a = 0; a < 3; ++a) h->term_B[3 * t + a] = T.B[a];
+        ++field_terms;
+        break;
+      default:
+        return h->fail(LLG_ERR_BAD_DESC, "unknown term kind %d", T.kind);
+    }
+  }
+  if (field_terms > 1) return h->fail(LLG_ERR_UNSUPPORTED, "at most one applied-field term");
+  P.nexch = (int)ex.size();
+
+  // stencil reach over all exchange terms
+  int reach[3] = {0, 0, 0};
+  for (auto& X : ex) {
+    const llg_term& T = d->terms[X.term];
+    for (int e = 0; e < T.n_int; ++e)
+      for (int l = 0; l < 3; ++l) reach[l] = std::max(reach[l], std::abs(T.T[3 * e + l]));
+  }
+
+  // replicas, tiles and tables
+  std::vector<int32_t> tab32;
+  std::vector<int2> tab64;
+  std::vector<int32_t> cnt64;
+  int64_t offset = 0;
+  h->reps.resize(d->n_replicas);
+  h->rep_T.resize(d->n_replicas);
+  h->rep_first_tile.resize(d->n_replicas);
+  h->rep_ntiles.resize(d->n_replicas);
+  for (int r = 0; r < d->n_replicas; ++r) {
+    const llg_replica& rp = d->replicas[r];
+    ReplicaDev R{};
+    int64_t n = (int64_t)d->nb;
+    for (int l = 0; l < 3; ++l) {
+      if (rp.L[l] < 1) return h->fail(LLG_ERR_BAD_DESC, "replica %d: lattice size must be positive", r);
+      if (reach[l] > rp.L[l] && d->periodic[l])
+        return h->fail(LLG_ERR_BAD_DESC, "replica %d: interaction reach %d exceeds lattice size %d on axis %d",
+                       r, reach[l], rp.L[l], l);
+      R.L[l] = rp.L[l];
+      R.R[l] = reach[l];
+      R.ncls[l] = axis_classes(rp.L[l], reach[l]);
+      n *= rp.L[l];
+    }
+    if (n > (int64_t)INT32_MAX / 2) return h->fail(LLG_ERR_UNSUPPORTED, "replica %d has too many spins", r);
+    if (!(rp.temperature >= 0.0) || !std::isfinite(rp.temperature))
+      return h->fail(LLG_ERR_BAD_DESC, "replica %d: temperature must be >= 0", r);
+    R.n = (int32_t)n;
+    R.offset = offset;
+    offset += (n + 63) / 64 * 64;
+    h->rep_T[r] = rp.temperature;
+    for (int a = 0; a < 3; ++a) {
+      double B = 0.0;
+      for (int t = 0; t < d->n_terms; ++t)
+        if (d->terms[t].kind == LLG_TERM_APPLIED_FIELD) B = d->terms[t].B[a];
+      if (rp.use_B) B = rp.B[a];
+      R.B[a] = B;
+      R.Bf[a] = (float)B;
+    }
+    const int ncl = R.ncls[0] * R.ncls[1] * R.ncls[2];
+    for (size_t x = 0; x < ex.size(); ++x) {
+      ExchangeHost& X = ex[x];
+      const llg_term& T = d->terms[X.term];
+      R.tab32[x] = (int64_t)tab32.size();
+      R.tab64[x] = (int64_t)tab64.size();
+      R.cnt64[x] = (int64_t)cnt64.size();
+      tab32.resize(tab32.size() + (size_t)d->nb * ncl * std::max(X.nslot_max, 1), kMissing);
+      tab64.resize(tab64.size() + (size_t)d->nb * ncl * std::max(X.zmax, 1), make_int2(0, 0));
+      cnt64.resize(cnt64.size() + (size_t)d->nb * ncl, 0);
+      for (int b = 0; b < d->nb; ++b)
+        for (int k1 = 0; k1 < R.ncls[0]; ++k1)
+          for (int k2 = 0; k2 < R.ncls[1]; ++k2)
+            for (int k3 = 0; k3 < R.ncls[2]; ++k3) {
+              const int q = (k1 * R.ncls[1] + k2) * R.ncls[2] + k3;
+              const int c[3] = {class_rep(k1, R.L[0], R.R[0], R.ncls[0]), class_rep(k2, R.L[1], R.R[1], R.ncls[1]),
+                                class_rep(k3, R.L[2], R.R[2], R.ncls[2])};
+              const int64_t i = (((int64_t)c[0] * R.L[1] + c[1]) * R.L[2] + c[2]) * d->nb + b;
+              // neighbour offset of every entry of this basis site (INT64_MIN: outside)
+              std::vector<std::pair<int64_t, int>> nbrs;
+              std::map<int, int64_t> off_of_entry;
+              for (int e = 0; e < T.n_int; ++e) {
+                if (T.bi[e] != b) continue;
+                int64_t w[3];
+                bool outside = false;
+                for (int l = 0; l < 3; ++l) {
+                  int64_t v = (int64_t)c[l] + T.T[3 * e + l];
+                  if (!d->periodic[l] && (v < 0 || v >= R.L[l])) {
+                    outside = true;
+                    break;
+                  }
+                  v = ((v % R.L[l]) + R.L[l]) % R.L[l];
+                  w[l] = v;
+                }
+                if (outside) continue;
+                const int64_t j = ((w[0] * R.L[1] + w[1]) * R.L[2] + w[2]) * d->nb + T.bj[e];
+                nbrs.push_back({j, e});
+                off_of_entry[e] = j - i;
+              }
+              std::sort(nbrs.begin(), nbrs.end());
+              for (size_t k = 1; k < nbrs.size(); ++k)
+                if (nbrs[k].first == nbrs[k - 1].first)
+                  return h->fail(LLG_ERR_BAD_DESC,
+                                 "Multiple interactions for sites %lld and %lld (replica %d, term %d)",
+                                 (long long)i, (long long)nbrs[k].first, r, X.term);
+              // FP64 list in ascending j (zero tensors skipped as the reference does)
+              const size_t base64 = R.tab64[x] + ((size_t)b * ncl + q) * std::max(X.zmax, 1);
+              int cnt = 0;
+              for (auto& nj : nbrs) {
+                if (X.mask[nj.second] == 0) continue;
+                tab64[base64 + cnt] = make_int2((int)(nj.first - i), nj.second);
+                ++cnt;
+              }
+              cnt64[R.cnt64[x] + (size_t)b * ncl + q] = cnt;
+              // FP32 slots
+              const size_t base32 = R.tab32[x] + ((size_t)b * ncl + q) * std::max(X.nslot_max, 1);
+              for (size_t s = 0; s < X.slot_entry[b].size(); ++s) {
+                auto it = off_of_entry.find(X.slot_entry[b][s]);
+                tab32[base32 + s] = it == off_of_entry.end() ? kMissing : (int32_t)it->second;
+              }
+            }
+    }
+    h->rep_first_tile[r] = (int)h->tiles.size();
+    for (int64_t s = 0; s < n; s += kBlock) h->tiles.push_back(make_int2(r, (int)s));
+    h->rep_ntiles[r] = (int)h->tiles.size() - h->rep_first_tile[r];
+    h->reps[r] = R;
+  }
+  h->npad = std::max<int64_t>(offset, 64);
+  P.npad = h->npad;
+  P.ntiles = (int)h->tiles.size();
+  for (size_t x = 0; x < ex.size(); ++x) {
+    ExchangeHost& X = ex[x];
+    P.nslot_max[x] = std::max(X.nslot_max, 1);
+    P.zmax[x] = std::max(X.zmax, 1);
+    ExchangeF32& E = P.ex32[x];
+    for (int b = 0; b < d->nb; ++b) {
+      E.nslot[b] = (int)X.slot_entry[b].size();
+      E.ngroup[b] = (int)X.group_end[b].size();
+      for (size_t g = 0; g < X.group_end[b].size(); ++g) {
+        E.group_end[b][g] = X.group_end[b][g];
+        const float hi = (float)X.group_j[b][g];
+        E.group_j_hi[b][g] = hi;
+        E.group_j_lo[b][g] = (float)(X.group_j[b][g] - (double)hi);
+      }
+      E.nrest[b] = E.nslot[b] - (E.ngroup[b] ? E.group_end[b][E.ngroup[b] - 1] : 0);
+    }
+  }
+
+  // device
+  cudaError_t ce = cudaSetDevice(d->device);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaSetDevice");
+  h->device = d->device;
+  cudaDeviceProp prop;
+  ce = cudaGetDeviceProperties(&prop, d->device);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaGetDeviceProperties");
+  if (prop.major != 10 || prop.minor != 3)
+    return h->fail(LLG_ERR_NO_DEVICE, "device %d is sm_%d%d; this library is built for sm_103a", d->device,
+                   prop.major, prop.minor);
+  ce = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamCreate");
+  h->stream = h->own_stream;
+
+  const size_t rs = real_size(h);
+  for (int k = 0; k < 3; ++k) {
+    ce = h->state[k].alloc((size_t)3 * h->npad * rs);
+    if (ce != cudaSuccess) return h->cuda_fail(ce, "allocating spin planes");
+    cudaMemsetAsync(h->state[k].p, 0, (size_t)3 * h->npad * rs, h->stream);
+  }
+  const bool need_aux = h->integrator == LLG_RK4 || h->fp64;
+  if (need_aux) {
+    ce = h->aux.alloc((size_t)3 * h->npad * rs);
+    if (ce != cudaSuccess) return h->cuda_fail(ce, "allocating integrator scratch");
+    cudaMemsetAsync(h->aux.p, 0, (size_t)3 * h->npad * rs, h->stream);
+  }
+  struct Up {
+    void* dst;
+    const void* src;
+    size_t bytes;
+  };
+  std::vector<Up> ups;
+  if ((ce = h->d_rep.alloc(h->reps.size())) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  if ((ce = h->d_tiles.alloc(h->tiles.size())) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  if ((ce = h->d_tab32.alloc(std::max<size_t>(tab32.size(), 1))) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  if ((ce = h->d_tab64.alloc(std::max<size_t>(tab64.size(), 1))) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  if ((ce = h->d_cnt64.alloc(std::max<size_t>(cnt64.size(), 1))) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  if ((ce = h->d_status.alloc(1)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  if ((ce = h->d_step_base.alloc(1)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  ups.push_back({h->d_tiles.p, h->tiles.data(), h->tiles.size() * sizeof(int2)});
+  if (!tab32.empty()) ups.push_back({h->d_tab32.p, tab32.data(), tab32.size() * sizeof(int32_t)});
+  if (!tab64.empty()) ups.push_back({h->d_tab64.p, tab64.data(), tab64.size() * sizeof(int2)});
+  if (!cnt64.empty()) ups.push_back({h->d_cnt64.p, cnt64.data(), cnt64.size() * sizeof(int32_t)});
+  for (size_t x = 0; x < ex.size(); ++x) {
+    if ((ce = h->d_rest[x].alloc(ex[x].rest_j.size())) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+    if ((ce = h->d_J64[x].alloc(std::max<size_t>(ex[x].J64.size(), 1))) != cudaSuccess)
+      return h->cuda_fail(ce, "alloc");
+    if ((ce = h->d_mask[x].alloc(std::max<size_t>(ex[x].mask.size(), 1))) != cudaSuccess)
+      return h->cuda_fail(ce, "alloc");
+    ups.push_back({h->d_rest[x].p, ex[x].rest_j.data(), ex[x].rest_j.size() * sizeof(float)});
+    if (!ex[x].J64.empty()) ups.push_back({h->d_J64[x].p, ex[x].J64.data(), ex[x].J64.size() * sizeof(double)});
+    if (!ex[x].mask.empty())
+      ups.push_back({h->d_mask[x].p, ex[x].mask.data(), ex[x].mask.size() * sizeof(uint16_t)});
+    P.ex32[x].rest_j = h->d_rest[x].p;
+    P.ex64[x].J = h->d_J64[x].p;
+    P.ex64[x].mask = h->d_mask[x].p;
+  }
+  for (auto& u : ups) {
+    ce = cudaMemcpy(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) return h->cuda_fail(ce, "uploading tables");
+  }
+  cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), h->stream);
+  cudaMemsetAsync(h->d_step_base.p, 0, sizeof(uint64_t), h->stream);
+  P.tab32 = h->d_tab32.p;
+  P.tab64 = h->d_tab64.p;
+  P.cnt64 = h->d_cnt64.p;
+  P.tiles = h->d_tiles.p;
+  P.rep = h->d_rep.p;
+  P.status = h->d_status.p;
+  P.step_base = h->d_step_base.p;
+  size_t maxn = 0;
+  for (auto& R : h->reps) maxn = std::max<size_t>(maxn, (size_t)R.n);
+  if ((ce = h->d_scratch.alloc(3 * maxn)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  size_t max_tiles = 0;
+  for (int r = 0; r < d->n_replicas; ++r) max_tiles = std::max<size_t>(max_tiles, h->rep_ntiles[r]);
+  const size_t nq = 4 + (size_t)kMaxTerms;
+  if ((ce = h->d_partials.alloc(std::max<size_t>(max_tiles, 1) * nq)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  h->h_partials.resize(std::max<size_t>(max_tiles, 1) * nq);
+  h->params_dirty = true;
+  return 0;
+}
+
+// uploads replica records (temperature- and field-dependent parts)
+int sync_replicas(llg_handle* h) {
+  if (!h->params_dirty) return 0;
+  for (size_t r = 0; r < h->reps.size(); ++r) {
+    ReplicaDev& R = h->reps[r];
+    const double T = h->rep_T[r];
+    R.thermal = T > 0.0 ? 1 : 0;
+    R.sqrt_t = std::sqrt(T);
+    for (int b = 0; b < h->nb; ++b) R.amp32[b] = (float)(h->P.sigma[b] * R.sqrt_t);
+  }
+  cudaError_t ce = cudaMemcpyAsync(h->d_rep.p, h->reps.data(), h->reps.size() * sizeof(ReplicaDev),
+                                   cudaMemcpyHostToDevice, h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "uploading replica records");
+  // pageable source: make sure the copy has consumed it before the vector changes
+  ce = cudaStreamSynchronize(h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "uploading replica records");
+  h->params_dirty = false;
+  return 0;
+}
+
+template <typename Real>
+Real* buf(llg_handle* h, int k) {
+  return reinterpret_cast<Real*>(h->state[k].p);
+}
+
+int num_stages(const llg_handle* h) { return h->integrator == LLG_HEUN ? 2 : 4; }
+
+// launches stage `stage` of step `ks` of a block; `cur` is the buffer that
+// holds the state at the start of the step (FP32 Heun alternates 0 and 2)
+void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur) {
+  const Params& P = h->P;
+  const unsigned grid = (unsigned)P.ntiles;
+  cudaStream_t st = h->stream;
+  if (h->integrator == LLG_HEUN) {
+    if (h->fp64) {
+      // state stays in buffer 0; 1 = predictor, aux = ds
+      double* s0 = buf<double>(h, 0);
+      double* sp = buf<double>(h, 1);
+      double* ds = reinterpret_cast<double*>(h->aux.p);
+      if (stage == 0)
+        heun_predict_f64<<<grid, kBlock, 0, st>>>(P, s0, sp, ds, ks);
+      else
+        heun_correct_f64<<<grid, kBlock, 0, st>>>(P, s0, sp, ds, s0, ks);
+    } else {
+      // state alternates between buffers 0 and 2; 1 = predictor
+      float* s0 = buf<float>(h, cur);
+      float* sp = buf<float>(h, 1);
+      float* s1 = buf<float>(h, 2 - cur);
+      if (stage == 0)
+        heun_predict_f32<<<grid, kBlock, 0, st>>>(P, s0, sp, ks);
+      else
+        heun_correct_f32<<<grid, kBlock, 0, st>>>(P, s0, sp, s1, ks);
+    }
+  } else {
+    // state stays in buffer 0; 1 and 2 hold stage states, aux the k sum
+    void* s0 = h->state[0].p;
+    void* a = h->state[1].p;
+    void* b = h->state[2].p;
+    void* in = stage == 0 ? s0 : (stage == 2 ? b : a);
+    void* out = stage == 0 ? a : (stage == 1 ? b : (stage == 2 ? a : s0));
+    if (h->fp64)
+      launch_rk4_f64(stage + 1, grid, st, P, (const double*)s0, (const double*)in, (double*)h->aux.p,
+                     (double*)out, ks);
+    else
+      launch_rk4_f32(stage + 1, grid, st, P, (const float*)s0, (const float*)in, (float*)h->aux.p,
+                     (float*)out, ks);
+  }
+}
+
+int next_buffer(const llg_handle* h, int cur) { return (!h->fp64 && h->integrator == LLG_HEUN) ? 2 - cur : cur; }
+
+// launches `nsteps` steps starting with the state in buffer `cur`; returns
+// the number of kernel launches
+int64_t enqueue_steps(llg_handle* h, int nsteps, int cur) {
+  const int ns = num_stages(h);
+  for (int k = 0; k < nsteps; ++k) {
+    for (int stg = 0; stg < ns; ++stg) launch_stage(h, stg, (uint32_t)k, cur);
+    cur = next_buffer(h, cur);
+  }
+  advance_step_base<<<1, 1, 0, h->stream>>>(h->d_step_base.p, (uint32_t)nsteps);
+  return (int64_t)nsteps * ns + 1;
+}
+
+int state_buffer(const llg_handle* h) { return (h->fp64 || h->integrator == LLG_RK4) ? 0 : h->cur; }
+
+}  // namespace
+
+// =================================================================== ABI ==
+
+extern "C" {
+
+int llg_create(const llg_desc* desc, llg_handle** out) {
+  if (!out) return tls_fail(LLG_ERR_BAD_DESC, "out is null");
+  *out = nullptr;
+  llg_handle* h = new (std::nothrow) llg_handle();
+  if (!h) return tls_fail(LLG_ERR_OOM, "host allocation failed");
+  int rc = build(h, desc);
+  if (rc == 0) rc = sync_replicas(h);
+  if (rc == 0) {
+    // all spins +z
+    for (int r = 0; r < (int)h->reps.size() && rc == 0; ++r) {
+      std::vector<double> s((size_t)h->reps[r].n * 3, 0.0);
+      for (int64_t i = 0; i < h->reps[r].n; ++i) s[3 * i + 2] = 1.0;
+      rc = llg_set_state(h, r, s.data());
+    }
+  }
+  if (rc != 0) {
+    g_tls_error = h->err;
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return 0;
+}
+
+void llg_destroy(llg_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  delete h;
+}
+
+const char* llg_last_error(const llg_handle* h) { return h ? h->err.c_str() : g_tls_error.c_str(); }
+
+int64_t llg_num_spins(const llg_handle* h, int32_t replica) {
+  if (!h) return -1;
+  if (replica < 0) {
+    int64_t n = 0;
+    for (auto& R : h->reps) n += R.n;
+    return n;
+  }
+  if (replica >= (int32_t)h->reps.size()) return -1;
+  return h->reps[replica].n;
+}
+
+int32_t llg_num_replicas(const llg_handle* h) { return h ? (int32_t)h->reps.size() : -1; }
+
+static int transfer_state(llg_handle* h, int32_t replica, const double* src, double* dst, bool device_ptr) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (replica >= (int32_t)h->reps.size()) return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
+  cudaSetDevice(h->device);
+  const int r0 = replica < 0 ? 0 : replica;
+  const int r1 = replica < 0 ? (int)h->reps.size() : replica + 1;
+  int64_t host_off = 0;
+  const int sb = state_buffer(h);
+  for (int r = r0; r < r1; ++r) {
+    const ReplicaDev& R = h->reps[r];
+    const size_t bytes = (size_t)R.n * 3 * sizeof(double);
+    double* dev_aos = h->d_scratch.p;
+    cudaError_t ce = cudaSuccess;
+    if (src) {
+      const double* s = src + 3 * host_off;
+      if (device_ptr) {
+        dev_aos = const_cast<double*>(s);
+      } else {
+        ce = cudaMemcpyAsync(dev_aos, s, bytes, cudaMemcpyHostToDevice, h->stream);
+        if (ce != cudaSuccess) return h->cuda_fail(ce, "copying spins to the device");
+      }
+      launch_unpack(h->fp64, h->stream, dev_aos, h->state[sb].p, R.offset, R.n, h->npad);
+      if (!device_ptr) {
+        ce = cudaStreamSynchronize(h->stream);
+        if (ce != cudaSuccess) return h->cuda_fail(ce, "setting spins");
+      }
+    } else {
+      double* d = dst + 3 * host_off;
+      if (device_ptr) dev_aos = d;
+      launch_pack(h->fp64, h->stream, h->state[sb].p, dev_aos, R.offset, R.n, h->npad);
+      if (!device_ptr) {
+        ce = cudaMemcpyAsync(d, dev_aos, bytes, cudaMemcpyDeviceToHost, h->stream);
+        if (ce != cudaSuccess) return h->cuda_fail(ce, "copying spins to the host");
+        ce = cudaStreamSynchronize(h->stream);
+        if (ce != cudaSuccess) return h->cuda_fail(ce, "getting spins");
+      }
+    }
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) return h->cuda_fail(ce, "state transfer kernel");
+    host_off += R.n;
+  }
+  return 0;
+}
+
+int llg_set_state(llg_handle* h, int32_t replica, const double* s_host) {
+  if (!s_host) return h ? h->fail(LLG_ERR_BAD_DESC, "null buffer") : tls_fail(LLG_ERR_BAD_DESC, "null buffer");
+  return transfer_state(h, replica, s_host, nullptr, false);
+}
+int llg_get_state(llg_handle* h, int32_t replica, double* s_host) {
+  if (!s_host) return h ? h->fail(LLG_ERR_BAD_DESC, "null buffer") : tls_fail(LLG_ERR_BAD_DESC, "null buffer");
+  return transfer_state(h, replica, nullptr, s_host, false);
+}
+int llg_set_state_device(llg_handle* h, int32_t replica, const double* s_dev) {
+  if (!s_dev) return h ? h->fail(LLG_ERR_BAD_DESC, "null buffer") : tls_fail(LLG_ERR_BAD_DESC, "null buffer");
+  return transfer_state(h, replica, s_dev, nullptr, true);
+}
+int llg_get_state_device(llg_handle* h, int32_t replica, double* s_dev) {
+  if (!s_dev) return h ? h->fail(LLG_ERR_BAD_DESC, "null buffer") : tls_fail(LLG_ERR_BAD_DESC, "null buffer");
+  return transfer_state(h, replica, nullptr, s_dev, true);
+}
+
+int llg_step(llg_handle* h, int32_t nsteps) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (nsteps < 0) return h->fail(LLG_ERR_BAD_DESC, "nsteps must be >= 0");
+  cudaSetDevice(h->device);
+  int rc = sync_replicas(h);
+  if (rc) return rc;
+  h->last_launches = 0;
+  const bool alternates = !h->fp64 && h->integrator == LLG_HEUN;
+  int K = h->steps_per_graph;
+  if (alternates && (K & 1)) K += 1;  // graphs must return the state to the buffer they found it in
+  int remaining = nsteps;
+  while (remaining >= K && K > 1) {
+    GraphKey key{h->cur, K};
+    auto it = h->graphs.find(key);
+    if (it == h->graphs.end()) {
+      cudaGraph_t g;
+      cudaError_t ce = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+      if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamBeginCapture");
+      enqueue_steps(h, K, h->cur);
+      ce = cudaStreamEndCapture(h->stream, &g);
+      if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamEndCapture");
+      cudaGraphExec_t ge;
+      ce = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaGraphInstantiate");
+      it = h->graphs.emplace(key, ge).first;
+    }
+    cudaError_t ce = cudaGraphLaunch(it->second, h->stream);
+    if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaGraphLaunch");
+    h->last_launches += (int64_t)K * (h->integrator == LLG_HEUN ? 2 : 4) + 1;
+    remaining -= K;
+    h->iteration += K;
+  }
+  if (remaining > 0) {
+    h->last_launches += enqueue_steps(h, remaining, h->cur);
+    if (remaining & 1) h->cur = next_buffer(h, h->cur);
+    h->iteration += remaining;
+  }
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "launching LLG steps");
+  return 0;
+}
+
+int llg_synchronize(llg_handle* h) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  cudaSetDevice(h->device);
+  cudaError_t ce = cudaStreamSynchronize(h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamSynchronize");
+  unsigned int status = 0;
+  ce = cudaMemcpy(&status, h->d_status.p, sizeof status, cudaMemcpyDeviceToHost);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "reading status");
+  if (status & 1u) return h->fail(LLG_ERR_NONFINITE, "a spin became NaN or infinite");
+  return 0;
+}
+
+int64_t llg_iteration(const llg_handle* h) { return h ? h->iteration : -1; }
+
+int llg_set_iteration(llg_handle* h, int64_t iteration) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (iteration < 0) return h->fail(LLG_ERR_BAD_DESC, "iteration must be >= 0");
+  cudaSetDevice(h->device);
+  uint64_t v = (uint64_t)iteration;
+  cudaError_t ce = cudaMemcpyAsync(h->d_step_base.p, &v, sizeof v, cudaMemcpyHostToDevice, h->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "setting the iteration");
+  h->iteration = iteration;
+  return 0;
+}
+
+int llg_set_temperature(llg_handle* h, int32_t replica, double temperature) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (replica < 0 || replica >= (int32_t)h->reps.size())
+    return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
+  if (!(temperature >= 0.0) || !std::isfinite(temperature))
+    return h->fail(LLG_ERR_BAD_DESC, "temperature must be >= 0");
+  h->rep_T[replica] = temperature;
+  h->params_dirty = true;
+  return 0;
+}
+
+int llg_set_field(llg_handle* h, int32_t replica, const double B[3]) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (replica < 0 || replica >= (int32_t)h->reps.size() || !B)
+    return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
+  for (int a = 0; a < 3; ++a) {
+    h->reps[replica].B[a] = B[a];
+    h->reps[replica].Bf[a] = (float)B[a];
+  }
+  h->params_dirty = true;
+  return 0;
+}
+
+int llg_fields(llg_handle* h, int32_t replica, double* h_host) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (replica < 0 || replica >= (int32_t)h->reps.size() || !h_host)
+    return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
+  cudaSetDevice(h->device);
+  int rc = sync_replicas(h);
+  if (rc) return rc;
+  const ReplicaDev& R = h->reps[replica];
+  const dim3 grid((unsigned)h->P.ntiles);
+  const int sb = state_buffer(h);
+  if (h->fp64)
+    fields_f64<<<grid, kBlock, 0, h->stream>>>(h->P, buf<double>(h, sb), h->d_scratch.p, replica);
+  else
+    fields_f32<<<grid, kBlock, 0, h->stream>>>(h->P, buf<float>(h, sb), h->d_scratch.p, replica);
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "fields kernel");
+  ce = cudaMemcpyAsync(h_host, h->d_scratch.p, (size_t)R.n * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                       h->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "copying fields");
+  return 0;
+}
+
+int llg_observables(llg_handle* h, int32_t replica, double* m4, double* e_terms) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (replica < 0 || replica >= (int32_t)h->reps.size())
+    return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
+  cudaSetDevice(h->device);
+  int rc = sync_replicas(h);
+  if (rc) return rc;
+  const int nq = 4 + h->nterms;
+  const int sb = state_buffer(h);
+  rc = observe(h->P, h->state[sb].p, h->fp64, replica, h->rep_first_tile[replica], h->rep_ntiles[replica],
+               h->d_partials.p, h->h_partials.data(), nq, h->stream);
+  if (rc) return h->cuda_fail(cudaGetLastError(), "observables");
+  // ordered sums over tiles (deterministic), Neumaier compensation
+  std::vector<double> sum(nq, 0.0), comp(nq, 0.0);
+  for (int t = 0; t < h->rep_ntiles[replica]; ++t)
+    for (int q = 0; q < nq; ++q) {
+      const double x = h->h_partials[(size_t)t * nq + q];
+      const double s = sum[q] + x;
+      comp[q] += std::fabs(sum[q]) >= std::fabs(x) ? (sum[q] - s) + x : (x - s) + sum[q];
+      sum[q] = s;
+    }
+  for (int q = 0; q < nq; ++q) sum[q] += comp[q];
+  if (m4) {
+    m4[0] = sum[0] / sum[3];
+    m4[1] = sum[1] / sum[3];
+    m4[2] = sum[2] / sum[3];
+    m4[3] = std::sqrt(sum[0] * sum[0] + sum[1] * sum[1] + sum[2] * sum[2]) / sum[3];
+  }
+  if (e_terms)
+    for (int t = 0; t < h->nterms; ++t) e_terms[t] = sum[4 + t];
+  return 0;
+}
+
+int llg_topological_charge(llg_handle* h, int32_t replica, double* q) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (replica < 0 || replica >= (int32_t)h->reps.size() || !q)
+    return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
+  if (h->nb != 1 || h->reps[replica].L[2] != 1)
+    return h->fail(LLG_ERR_UNSUPPORTED, "topological charge needs a one-site monolayer");
+  cudaSetDevice(h->device);
+  const int sb = state_buffer(h);
+  int rc = topological_charge(h->P, h->state[sb].p, h->fp64, replica, (int)(h->d_partials.n / (4 + kMaxTerms)),
+                              h->d_partials.p, h->h_partials.data(), h->stream, q);
+  if (rc) return h->cuda_fail(cudaGetLastError(), "topological charge");
+  return 0;
+}
+
+int llg_set_stream(llg_handle* h, void* cuda_stream) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own_stream;
+  return 0;
+}
+
+int64_t llg_last_launch_count(const llg_handle* h) { return h ? h->last_launches : -1; }
+
+int llg_profile_stages(llg_handle* h, int32_t nsteps, double* ms) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (nsteps < 1 || !ms) return h->fail(LLG_ERR_BAD_DESC, "nsteps must be >= 1 and ms non-null");
+  cudaSetDevice(h->device);
+  int rc = sync_replicas(h);
+  if (rc) return rc;
+  const int ns = num_stages(h);
+  std::vector<cudaEvent_t> ev((size_t)nsteps * ns * 2);
+  for (auto& e : ev) {
+    cudaError_t ce = cudaEventCreate(&e);
+    if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaEventCreate");
+  }
+  int cur = h->cur;
+  for (int k = 0; k < nsteps; ++k) {
+    for (int stg = 0; stg < ns; ++stg) {
+      cudaEventRecord(ev[((size_t)k * ns + stg) * 2], h->stream);
+      launch_stage(h, stg, (uint32_t)k, cur);
+      cudaEventRecord(ev[((size_t)k * ns + stg) * 2 + 1], h->stream);
+    }
+    cur = next_buffer(h, cur);
+  }
+  advance_step_base<<<1, 1, 0, h->stream>>>(h->d_step_base.p, (uint32_t)nsteps);
+  h->cur = cur;
+  h->iteration += nsteps;
+  h->last_launches = (int64_t)nsteps * ns + 1;
+  cudaError_t ce = cudaStreamSynchronize(h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "profiling stages");
+  for (int stg = 0; stg < ns; ++stg) ms[stg] = 0.0;
+  for (int k = 0; k < nsteps; ++k)
+    for (int stg = 0; stg < ns; ++stg) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[((size_t)k * ns + stg) * 2], ev[((size_t)k * ns + stg) * 2 + 1]);
+      ms[stg] += t / nsteps;
+    }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return 0;
+}
+
+}  // extern "C"

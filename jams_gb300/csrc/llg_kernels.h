@@ -1,0 +1,52 @@
+// Declarations of the kernels in llg_kernels.cu, launched by llg_host.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "llg_internal.h"
+
+namespace jams_llg {
+
+__global__ void heun_predict_f32(const __grid_constant__ Params P, const float* __restrict__ s0,
+                                 float* __restrict__ sp, uint32_t kstep);
+__global__ void heun_correct_f32(const __grid_constant__ Params P, const float* __restrict__ s0,
+                                 const float* __restrict__ sp, float* __restrict__ s1, uint32_t kstep);
+__global__ void heun_predict_f64(const __grid_constant__ Params P, const double* __restrict__ s0,
+                                 double* __restrict__ sp, double* __restrict__ ds, uint32_t kstep);
+__global__ void heun_correct_f64(const __grid_constant__ Params P, const double* s0, const double* sp,
+                                 const double* ds, double* s1, uint32_t kstep);
+template <int STAGE>
+__global__ void rk4_stage_f32(const __grid_constant__ Params P, const float* s0, const float* sin, float* acc,
+                              float* sout, uint32_t kstep);
+template <int STAGE>
+__global__ void rk4_stage_f64(const __grid_constant__ Params P, const double* s0, const double* sin,
+                              double* acc, double* sout, uint32_t kstep);
+__global__ void advance_step_base(uint64_t* base, uint32_t nsteps);
+template <typename Real>
+__global__ void unpack_state(const double* __restrict__ aos, Real* __restrict__ soa, int64_t offset, int64_t n,
+                             int64_t npad);
+template <typename Real>
+__global__ void pack_state(const Real* __restrict__ soa, double* __restrict__ aos, int64_t offset, int64_t n,
+                           int64_t npad);
+__global__ void fields_f32(const __grid_constant__ Params P, const float* __restrict__ s0,
+                           double* __restrict__ out, int replica);
+__global__ void fields_f64(const __grid_constant__ Params P, const double* __restrict__ s0,
+                           double* __restrict__ out, int replica);
+
+void launch_rk4_f32(int stage, unsigned grid, cudaStream_t st, const Params& P, const float* s0, const float* sin,
+                    float* acc, float* sout, uint32_t k);
+void launch_rk4_f64(int stage, unsigned grid, cudaStream_t st, const Params& P, const double* s0,
+                    const double* sin, double* acc, double* sout, uint32_t k);
+void launch_unpack(bool fp64, cudaStream_t st, const double* aos, void* soa, int64_t offset, int64_t n,
+                   int64_t npad);
+void launch_pack(bool fp64, cudaStream_t st, const void* soa, double* aos, int64_t offset, int64_t n,
+                 int64_t npad);
+
+// observables (llg_observe.cu): ordered per-tile partial sums copied to
+// h_partials [ntiles][nq] = (sum mu_s Sx, Sy, Sz, sum mu_s, E_term...)
+int observe(const Params& P, const void* state, bool fp64, int replica, int first_tile, int ntiles,
+            double* d_partials, double* h_partials, int nq, cudaStream_t stream);
+int topological_charge(const Params& P, const void* state, bool fp64, int replica, int ntiles_max,
+                       double* d_partials, double* h_partials, cudaStream_t stream, double* q);
+
+}  // namespace jams_llg

@@ -1,0 +1,269 @@
+"""Python binding of libjams_llg.so through its C ABI (include/jams_llg.h).
+
+Used by the tests, the benchmark and the smoke check.  The library must have
+been built (``jams_gb300.build.build()``); there is no fallback: if the shared
+library is missing or no sm_103 device is present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import workloads as W
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libjams_llg.so")
+
+LLG_ABI_VERSION = 1
+FP64 = 0
+FP32C = 1
+HEUN = 0
+RK4 = 1
+
+ERRORS = {
+    -1: "LLG_ERR_BAD_DESC", -2: "LLG_ERR_OOM", -3: "LLG_ERR_CUDA", -4: "LLG_ERR_TIMEOUT",
+    -5: "LLG_ERR_NONFINITE", -6: "LLG_ERR_NO_DEVICE", -7: "LLG_ERR_UNSUPPORTED",
+}
+
+EXPORTED = [
+    "llg_create", "llg_destroy", "llg_last_error", "llg_num_spins", "llg_num_replicas",
+    "llg_set_state", "llg_get_state", "llg_set_state_device", "llg_get_state_device", "llg_step",
+    "llg_synchronize", "llg_iteration", "llg_set_iteration", "llg_set_temperature", "llg_set_field",
+    "llg_fields", "llg_observables", "llg_topological_charge", "llg_set_stream", "llg_last_launch_count",
+    "llg_profile_stages",
+]
+
+
+class LLGError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s: %s" % (ERRORS.get(code, code), msg))
+        self.code = code
+
+
+class LlgTerm(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32), ("order", ctypes.c_int32), ("n_int", ctypes.c_int32),
+        ("bi", ctypes.POINTER(ctypes.c_int32)), ("bj", ctypes.POINTER(ctypes.c_int32)),
+        ("T", ctypes.POINTER(ctypes.c_int32)), ("J", ctypes.POINTER(ctypes.c_double)),
+        ("K", ctypes.POINTER(ctypes.c_double)), ("axis", ctypes.POINTER(ctypes.c_double)),
+        ("B", ctypes.c_double * 3),
+    ]
+
+
+class LlgReplica(ctypes.Structure):
+    _fields_ = [("L", ctypes.c_int32 * 3), ("temperature", ctypes.c_double), ("B", ctypes.c_double * 3),
+                ("use_B", ctypes.c_int32)]
+
+
+class LlgDesc(ctypes.Structure):
+    _fields_ = [
+        ("abi_version", ctypes.c_int32), ("nb", ctypes.c_int32), ("periodic", ctypes.c_int32 * 3),
+        ("mus", ctypes.POINTER(ctypes.c_double)), ("gyro", ctypes.POINTER(ctypes.c_double)),
+        ("alpha", ctypes.POINTER(ctypes.c_double)), ("n_terms", ctypes.c_int32),
+        ("terms", ctypes.POINTER(LlgTerm)), ("dt", ctypes.c_double), ("gilbert_prefactor", ctypes.c_int32),
+        ("integrator", ctypes.c_int32), ("precision", ctypes.c_int32),
+        ("rk4_normalise_stages", ctypes.c_int32), ("seed", ctypes.c_uint64), ("n_replicas", ctypes.c_int32),
+        ("replicas", ctypes.POINTER(LlgReplica)), ("device", ctypes.c_int32),
+        ("steps_per_graph", ctypes.c_int32),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libjams_llg.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libjams_llg.so is not built: run jams_gb300.build.build() (%s)" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i32, i64, dp = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)
+        L.llg_create.argtypes = [ctypes.POINTER(LlgDesc), ctypes.POINTER(vp)]
+        L.llg_destroy.argtypes = [vp]
+        L.llg_destroy.restype = None
+        L.llg_last_error.argtypes = [vp]
+        L.llg_last_error.restype = ctypes.c_char_p
+        L.llg_num_spins.argtypes = [vp, i32]
+        L.llg_num_spins.restype = i64
+        L.llg_num_replicas.argtypes = [vp]
+        for f in ("llg_set_state", "llg_get_state", "llg_set_state_device", "llg_get_state_device"):
+            getattr(L, f).argtypes = [vp, i32, vp]
+        L.llg_step.argtypes = [vp, i32]
+        L.llg_synchronize.argtypes = [vp]
+        L.llg_iteration.argtypes = [vp]
+        L.llg_iteration.restype = i64
+        L.llg_set_iteration.argtypes = [vp, i64]
+        L.llg_set_temperature.argtypes = [vp, i32, ctypes.c_double]
+        L.llg_set_field.argtypes = [vp, i32, dp]
+        L.llg_fields.argtypes = [vp, i32, dp]
+        L.llg_observables.argtypes = [vp, i32, dp, dp]
+        L.llg_topological_charge.argtypes = [vp, i32, dp]
+        L.llg_set_stream.argtypes = [vp, vp]
+        L.llg_last_launch_count.argtypes = [vp]
+        L.llg_last_launch_count.restype = i64
+        L.llg_profile_stages.argtypes = [vp, i32, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+class Solver:
+    """A JAMS LLG solver (Heun or RK4) on one GPU for all replicas of a
+    workload: the CUDAHeunLLGSolver / CUDALLGRK4Solver of the reference with
+    its Hamiltonian terms fused into the stage kernels."""
+
+    def __init__(self, workload: W.Workload, precision: int = FP32C, device: int = 0,
+                 steps_per_graph: int = 100, rk4_normalise_stages: bool = False):
+        self.L = lib()
+        self.workload = workload
+        m = workload.model
+        self._keep = []
+        terms = (LlgTerm * max(len(m.terms), 1))()
+        for k, t in enumerate(m.terms):
+            lt = terms[k]
+            lt.kind, lt.order = t.kind, t.order
+            if t.bi is not None:
+                arrs = [np.ascontiguousarray(t.bi, dtype=np.int32), np.ascontiguousarray(t.bj, dtype=np.int32),
+                        np.ascontiguousarray(t.T, dtype=np.int32).reshape(-1),
+                        np.ascontiguousarray(t.J, dtype=np.float64).reshape(-1)]
+                self._keep += arrs
+                lt.n_int = len(arrs[0])
+                lt.bi, lt.bj, lt.T, lt.J = _ip(arrs[0]), _ip(arrs[1]), _ip(arrs[2]), _dp(arrs[3])
+            if t.K is not None:
+                K = np.ascontiguousarray(t.K, dtype=np.float64)
+                ax = np.ascontiguousarray(t.axis, dtype=np.float64).reshape(-1)
+                self._keep += [K, ax]
+                lt.K, lt.axis = _dp(K), _dp(ax)
+            for j in range(3):
+                lt.B[j] = float(t.B[j])
+        reps = (LlgReplica * len(workload.replicas))()
+        for r, rp in enumerate(workload.replicas):
+            for j in range(3):
+                reps[r].L[j] = int(rp.L[j])
+            reps[r].temperature = float(rp.temperature)
+            if rp.B is not None:
+                reps[r].use_B = 1
+                for j in range(3):
+                    reps[r].B[j] = float(rp.B[j])
+        mats = [np.ascontiguousarray(x, dtype=np.float64) for x in (m.mus, m.gyro, m.alpha)]
+        self._keep += mats
+        d = LlgDesc()
+        d.abi_version = LLG_ABI_VERSION
+        d.nb = m.nb
+        for j in range(3):
+            d.periodic[j] = int(m.periodic[j])
+        d.mus, d.gyro, d.alpha = _dp(mats[0]), _dp(mats[1]), _dp(mats[2])
+        d.n_terms = len(m.terms)
+        d.terms = ctypes.cast(terms, ctypes.POINTER(LlgTerm))
+        d.dt = m.dt
+        d.gilbert_prefactor = int(bool(m.gilbert_prefactor))
+        d.integrator = int(m.integrator)
+        d.precision = int(precision)
+        d.rk4_normalise_stages = int(bool(rk4_normalise_stages))
+        d.seed = int(workload.seed)
+        d.n_replicas = len(workload.replicas)
+        d.replicas = ctypes.cast(reps, ctypes.POINTER(LlgReplica))
+        d.device = int(device)
+        d.steps_per_graph = int(steps_per_graph)
+        self._terms, self._reps, self._desc = terms, reps, d
+        h = ctypes.c_void_p()
+        rc = self.L.llg_create(ctypes.byref(d), ctypes.byref(h))
+        if rc != 0:
+            raise LLGError(rc, self.L.llg_last_error(None).decode())
+        self.h = h
+        self.precision = precision
+        self.n_terms = len(m.terms)
+        self.n_replicas = len(workload.replicas)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.llg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise LLGError(rc, self.L.llg_last_error(self.h).decode())
+
+    def num_spins(self, replica: int = -1) -> int:
+        return int(self.L.llg_num_spins(self.h, replica))
+
+    def set_state(self, spins: np.ndarray, replica: int = -1) -> None:
+        s = np.ascontiguousarray(spins, dtype=np.float64)
+        if s.size != 3 * self.num_spins(replica):
+            raise ValueError("expected %d spins" % self.num_spins(replica))
+        self._check(self.L.llg_set_state(self.h, replica, s.ctypes.data))
+
+    def get_state(self, replica: int = -1, out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.num_spins(replica), 3))
+        self._check(self.L.llg_get_state(self.h, replica, out.ctypes.data))
+        return out
+
+    def set_state_device(self, ptr: int, replica: int = -1) -> None:
+        self._check(self.L.llg_set_state_device(self.h, replica, ptr))
+
+    def get_state_device(self, ptr: int, replica: int = -1) -> None:
+        self._check(self.L.llg_get_state_device(self.h, replica, ptr))
+
+    def step(self, nsteps: int) -> None:
+        self._check(self.L.llg_step(self.h, int(nsteps)))
+
+    def synchronize(self) -> None:
+        self._check(self.L.llg_synchronize(self.h))
+
+    @property
+    def iteration(self) -> int:
+        return int(self.L.llg_iteration(self.h))
+
+    def set_iteration(self, it: int) -> None:
+        self._check(self.L.llg_set_iteration(self.h, int(it)))
+
+    def set_temperature(self, replica: int, T: float) -> None:
+        self._check(self.L.llg_set_temperature(self.h, replica, float(T)))
+
+    def set_field(self, replica: int, B: Sequence[float]) -> None:
+        b = np.ascontiguousarray(B, dtype=np.float64)
+        self._check(self.L.llg_set_field(self.h, replica, _dp(b)))
+
+    def fields(self, replica: int = 0) -> np.ndarray:
+        out = np.empty((self.num_spins(replica), 3))
+        self._check(self.L.llg_fields(self.h, replica, _dp(out)))
+        return out
+
+    def observables(self, replica: int = 0):
+        m4 = np.empty(4)
+        e = np.empty(max(self.n_terms, 1))
+        self._check(self.L.llg_observables(self.h, replica, _dp(m4), _dp(e)))
+        return m4, e[: self.n_terms]
+
+    def topological_charge(self, replica: int = 0) -> float:
+        q = np.empty(1)
+        self._check(self.L.llg_topological_charge(self.h, replica, _dp(q)))
+        return float(q[0])
+
+    def set_stream(self, stream_ptr: int) -> None:
+        self._check(self.L.llg_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def profile_stages(self, nsteps: int) -> np.ndarray:
+        """Mean duration (ms) of each stage kernel over nsteps steps."""
+        ms = np.zeros(4)
+        self._check(self.L.llg_profile_stages(self.h, int(nsteps), _dp(ms)))
+        return ms[: 2 if self.workload.model.integrator == W.HEUN else 4]
+
+    @property
+    def last_launch_count(self) -> int:
+        return int(self.L.llg_last_launch_count(self.h))

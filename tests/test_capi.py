@@ -1,0 +1,41 @@
+"""CPU checks of the C ABI library: it builds for sm_103a, loads, and exports
+every function include/jams_llg.h declares (no device calls)."""
+import ctypes
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "jams_llg.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(llg_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(llg):
+    lib = ctypes.CDLL(llg.LIB_PATH)
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert sorted(llg.EXPORTED) == sorted(n for n in names if n in llg.EXPORTED)
+
+
+def test_library_is_sm103a_only(llg):
+    import subprocess
+
+    out = subprocess.run(["cuobjdump", "--list-elf", llg.LIB_PATH], capture_output=True, text=True)
+    if out.returncode != 0:  # cuobjdump absent: nothing to check
+        return
+    arches = set(re.findall(r"sm_(\d+a?)", out.stdout))
+    assert arches == {"103a"} or arches == {"103"}, arches
+
+
+def test_descriptor_layout_matches_header(llg):
+    """ctypes mirror of llg_desc has the field order of the header."""
+    text = open(os.path.join(ROOT, "include", "jams_llg.h")).read()
+    body = text[text.index("typedef struct {\n  int32_t abi_version;"):]
+    body = body[: body.index("} llg_desc;")]
+    fields = re.findall(r"\b([a-z_0-9]+)(?:\[\d\])?;", body)
+    assert fields == [f[0] for f in llg.LlgDesc._fields_]

@@ -1,0 +1,218 @@
+"""Parity of the sm_103a kernels (through the C ABI) with the oracle and with
+the golden vectors produced by the reference's own CPU solver.
+
+Tolerances:
+  FP64 form   bit-exact (max |dS| == 0) against the reference / oracle
+  FP32C form  max |dS| <= 1e-5 after 1000 T = 0 steps (benchmark bound);
+              fields within 2e-6 relative to the field scale
+"""
+import os
+
+import numpy as np
+import pytest
+
+from jams_gb300 import workloads as W
+from tests.golden.cases import cases
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FP32C_TOL = 1e-5
+
+
+def solver(llg, w, precision, **kw):
+    return llg.Solver(w, precision=precision, **kw)
+
+
+@pytest.mark.parametrize("name", sorted(cases().keys()))
+def test_fp64_equals_reference_golden_vectors(llg, name):
+    w = cases()[name]
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    s = solver(llg, w, llg.FP64)
+    s.set_state(g["s0"])
+    assert np.array_equal(s.fields(0), g["fields"])
+    done = 0
+    for k in (1, 10, 100):
+        s.step(k - done)
+        done = k
+        got = s.get_state(0)
+        assert np.array_equal(got, g["s%d" % k]), "max |dS| = %g after %d steps" % (
+            np.abs(got - g["s%d" % k]).max(), k)
+    s.synchronize()
+
+
+@pytest.mark.parametrize("T", [0.0, 300.0])
+def test_fp64_heun_bcc_equals_oracle(llg, oracle, T):
+    w = W.bcc_three_shell(L=8, T=T, start="random")
+    s0 = W.initial_state(w, 0)
+    ref = oracle.OracleSim(w).run(s0, 60)
+    s = solver(llg, w, llg.FP64, steps_per_graph=16)
+    s.set_state(s0)
+    s.step(60)
+    assert np.array_equal(s.get_state(0), ref)
+
+
+@pytest.mark.parametrize("T", [0.0, 5.0])
+def test_fp64_rk4_triangular_dmi_equals_oracle(llg, oracle, T):
+    w = W.triangular_dmi_field_sweep(L=16, n_fields=1, T=T)
+    w.replicas[0].B = (0.0, 0.0, 1.0)
+    s0 = W.initial_state(w, 0)
+    ref = oracle.OracleSim(w).run(s0, 40)
+    s = solver(llg, w, llg.FP64)
+    s.set_state(s0)
+    s.step(40)
+    assert np.array_equal(s.get_state(0), ref)
+
+
+def test_fp32c_sc32_1000_steps_within_bound(llg, oracle):
+    """Simple-cubic 32^3, T = 0, 1000 Heun steps (the CPU-runnable workload
+    at full size): FP32C max |dS| <= 1e-5 against the FP64 oracle."""
+    w = W.sc_ferromagnet(L=32, steps=1000)
+    s0 = W.initial_state(w, 0)
+    ref = oracle.OracleSim(w).run(s0, 1000)
+    s = solver(llg, w, llg.FP32C)
+    s.set_state(s0)
+    s.step(1000)
+    got = s.get_state(0)
+    d = np.abs(got - ref).max()
+    assert d <= FP32C_TOL, d
+    m_ref = oracle.OracleSim(w).magnetisation(ref)
+    m_got, _ = s.observables(0)
+    assert np.abs(m_got - m_ref).max() < 1e-6
+
+
+def test_fp32c_bcc_three_shell_1000_steps_within_bound(llg, oracle):
+    w = W.bcc_three_shell(L=16, T=0.0, start="random")
+    s0 = W.initial_state(w, 0)
+    ref = oracle.OracleSim(w).run(s0, 1000)
+    s = solver(llg, w, llg.FP32C)
+    s.set_state(s0)
+    s.step(1000)
+    d = np.abs(s.get_state(0) - ref).max()
+    assert d <= FP32C_TOL, d
+
+
+@pytest.mark.parametrize("normalise", [False, True])
+def test_fp32c_rk4_triangular_within_bound(llg, oracle, normalise):
+    w = W.triangular_dmi_field_sweep(L=64, n_fields=1, T=0.0)
+    w.replicas[0].B = (0.0, 0.0, 1.0)
+    s0 = W.initial_state(w, 0)
+    ref = oracle.OracleSim(w).run(s0, 1000)
+    s = solver(llg, w, llg.FP32C, rk4_normalise_stages=normalise)
+    s.set_state(s0)
+    s.step(1000)
+    d = np.abs(s.get_state(0) - ref).max()
+    assert d <= FP32C_TOL, d
+
+
+@pytest.mark.parametrize("name", sorted(cases().keys()))
+def test_fp32c_fields(llg, name):
+    w = cases()[name]
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    s = solver(llg, w, llg.FP32C)
+    s.set_state(g["s0"])
+    h = s.fields(0)
+    scale = np.abs(g["fields"]).max()
+    assert np.abs(h - g["fields"]).max() <= 2e-6 * scale
+
+
+@pytest.mark.parametrize("precision", ["FP64", "FP32C"])
+def test_observables_match_oracle(llg, oracle, precision):
+    for name, w in cases().items():
+        g = np.load(os.path.join(GOLDEN, name + ".npz"))
+        s = solver(llg, w, getattr(llg, precision))
+        s.set_state(g["s0"])
+        m, e = s.observables(0)
+        state = s.get_state(0)
+        o = oracle.OracleSim(w)
+        tol = 1e-12 if precision == "FP64" else 1e-6
+        np.testing.assert_allclose(m, o.magnetisation(state), rtol=tol, atol=tol)
+        np.testing.assert_allclose(e, o.energies(state), rtol=tol, atol=tol * np.abs(o.energies(state)).max())
+
+
+@pytest.mark.parametrize("precision", ["FP64", "FP32C"])
+def test_batched_replicas_equal_separate_runs(llg, precision):
+    """Replicas of uneven size and temperature in one handle evolve exactly as
+    they do alone (the replica index is part of the noise counter)."""
+    w = W.sc_temperature_sweep(n_replicas=5, L_min=4, L_max=9, T_max=400.0, steps=50)
+    p = getattr(llg, precision)
+    batch = solver(llg, w, p, steps_per_graph=10)
+    starts = [W.initial_state(w, r) for r in range(5)]
+    for r in range(5):
+        batch.set_state(starts[r], r)
+    batch.step(30)
+    for r in range(5):
+        single = W.Workload(name="one", model=w.model, replicas=[w.replicas[r]], steps=30, seed=w.seed)
+        # the replica index enters the noise counter: run the replica alone at
+        # its batch position by padding with empty-temperature copies
+        pad = W.Workload(name="pad", model=w.model, replicas=w.replicas[: r + 1], steps=30, seed=w.seed)
+        s1 = solver(llg, pad, p, steps_per_graph=10)
+        s1.set_state(starts[r], r)
+        s1.step(30)
+        assert np.array_equal(batch.get_state(r), s1.get_state(r))
+        del single
+
+
+@pytest.mark.parametrize("precision", ["FP64", "FP32C"])
+def test_graph_and_direct_launches_agree(llg, precision):
+    w = W.bcc_three_shell(L=6, T=200.0, start="random")
+    s0 = W.initial_state(w, 0)
+    p = getattr(llg, precision)
+    a = solver(llg, w, p, steps_per_graph=8)
+    b = solver(llg, w, p, steps_per_graph=1)
+    for x in (a, b):
+        x.set_state(s0)
+        x.step(13)
+        x.step(7)
+    assert a.iteration == b.iteration == 20
+    assert np.array_equal(a.get_state(0), b.get_state(0))
+
+
+def test_resume_from_state_and_iteration(llg):
+    """A run split at step 10 (state read back, new handle, iteration set)
+    continues the noise stream exactly."""
+    w = W.bcc_three_shell(L=6, T=300.0, start="random")
+    s0 = W.initial_state(w, 0)
+    a = solver(llg, w, llg.FP64)
+    a.set_state(s0)
+    a.step(20)
+    b = solver(llg, w, llg.FP64)
+    b.set_state(s0)
+    b.step(10)
+    mid = b.get_state(0)
+    c = solver(llg, w, llg.FP64)
+    c.set_state(mid)
+    c.set_iteration(10)
+    c.step(10)
+    assert np.array_equal(a.get_state(0), c.get_state(0))
+
+
+def test_nonfinite_spin_is_reported(llg):
+    w = W.sc_ferromagnet(L=4)
+    s = solver(llg, w, llg.FP32C)
+    st = W.initial_state(w, 0)
+    st[5] = np.nan
+    s.set_state(st)
+    s.step(2)
+    with pytest.raises(llg.LLGError, match="NONFINITE"):
+        s.synchronize()
+
+
+def test_undamped_energy_drift_is_small(llg):
+    """alpha = 0, T = 0: Heun conserves the energy to O(dt^2) per unit time."""
+    w = W.sc_ferromagnet(L=16, alpha=0.0)
+    s = solver(llg, w, llg.FP32C)
+    s.set_state(W.initial_state(w, 0))
+    _, e0 = s.observables(0)
+    s.step(500)
+    _, e1 = s.observables(0)
+    assert abs(e1.sum() - e0.sum()) < 1e-3 * abs(e0.sum())
+
+
+def test_topological_charge_matches_oracle(llg, oracle):
+    w = W.triangular_dmi_field_sweep(L=32, n_fields=1, T=0.0)
+    s0 = W.initial_state(w, 0)
+    s = solver(llg, w, llg.FP64)
+    s.set_state(s0)
+    q = s.topological_charge(0)
+    assert abs(q - oracle.topological_charge_triangular(s0, 32, 32)) < 1e-10
