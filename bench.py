@@ -53,6 +53,8 @@ STAGE_NAMES = {"heun": ["heun_predict", "heun_correct"], "rk4": ["rk4_stage1", "
 WORKLOADS = {
     # bcc 64^3 x 2, J1..J3, cubic K, 300 K, Heun dt 0.5 fs (the benchmark's headline configuration)
     "bcc64_3shell": lambda: W.bcc_three_shell(L=64, T=300.0, start="+z"),
+    # the same Hamiltonian at 128^3 x 2 (4.2 M spins): state larger than L2, for profiling
+    "bcc128_3shell": lambda: W.bcc_three_shell(L=128, T=300.0, start="+z"),
     # simple-cubic 32^3, T = 0, Heun dt 1 fs (the reference's CPU-runnable case)
     "sc32": lambda: W.sc_ferromagnet(L=32, T=0.0),
     # bcc 256^3 x 2 (33.5 M spins), 500 K, both readings of its Hamiltonian
