@@ -78,6 +78,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-steps", type=int, default=50)
+    p.add_argument("--no-tune", action="store_true")
     return p.parse_args()
 
 
@@ -261,6 +262,7 @@ def main():
         sol.set_state(W.initial_state(w, r), r)
     n_spins = sol.num_spins(-1)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    tuning = sol.autotune(trial_steps=10) if not args.no_tune else sol.kernel_info()
 
     # warm-up (also builds nothing lazily: single steps use direct launches)
     for _ in range(args.warmup):
@@ -372,7 +374,7 @@ def main():
         "config": {"workload": args.workload, "description": w.description, "spins": n_spins,
                    "replicas": len(w.replicas), "precision": args.precision, "integrator": integ,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas" if world > 1
-                   else "single GPU"},
+                   else "single GPU", "kernels": tuning},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         "steady_state_graph": steady, "wall_s_timed_region": t_wall,
     }

@@ -184,6 +184,25 @@ int64_t llg_last_launch_count(const llg_handle *h);
    (Heun: predictor, corrector; RK4: stages 1-4).  Synchronous. */
 int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
 
+/* Kernel selection of the handle: info[0] stencil family of the tiled FP32
+   kernels (0: generic gather kernels; 1 simple cubic, 2 bcc nearest
+   neighbours, 3 bcc three shells, 4 triangular monolayer), info[1] planes
+   streamed per CTA, info[2] 1 when the Heun predictor stores rhs(s0) for
+   the corrector (else the corrector recomputes it), info[3..4] CTA tile
+   (cells along the contiguous axis, rows), info[5] 1 for FP64. */
+int llg_kernel_info(const llg_handle *h, int32_t *info);
+
+/* Tiling choice of the tiled FP32 kernels (no effect on other kernels):
+   planes streamed per CTA and whether the Heun predictor stores rhs(s0). */
+int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t store_rhs);
+
+/* Times every tiling candidate (planes per CTA 1..64, stored or recomputed
+   rhs) for trial_steps steps on a copy of the state and keeps the fastest;
+   the state and iteration are restored.  With use_cache the choice is read
+   from / appended to the file named by $JAMS_LLG_TUNE_CACHE (default
+   ~/.cache/jams_llg_tuning.txt), keyed by device, lattice and terms. */
+int llg_autotune(llg_handle *h, int32_t trial_steps, int32_t use_cache);
+
 #ifdef __cplusplus
 }
 #endif

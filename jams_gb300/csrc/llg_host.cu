@@ -28,6 +28,7 @@
 #include "../../include/jams_llg.h"
 #include "llg_internal.h"
 
+#include "llg_families.h"
 #include "llg_kernels.h"
 
 using namespace jams_llg;
@@ -120,6 +121,13 @@ struct llg_handle {
   std::map<GraphKey, cudaGraphExec_t> graphs;
   int64_t last_launches = 0;
   bool params_dirty = false;
+  // tiled FP32 path (lattice matched a stencil family)
+  int family = kFamNone;
+  bool tiled = false;
+  bool store_mode = false;   // Heun: predictor stores rhs(s0) instead of the corrector recomputing it
+  int tz = 0, ty = 0;
+  TiledParams TP{};
+  DevBuf<int4> d_tiles4;
 
   ~llg_handle() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
@@ -237,6 +245,95 @@ int build_slots(llg_handle* h, const llg_term& t, ExchangeHost& X) {
     X.zmax = std::max(X.zmax, z);
   }
   return 0;
+}
+
+// Matches an exchange interaction template against a compile-time stencil
+// family: the same (basis site, translation, partner) set per basis site,
+// one isotropic J per shell (families without remainders) and nothing else.
+template <class F>
+bool match_family(const llg_desc* d, const llg_term& t, TiledParams& TP) {
+  if (d->nb != F::NB) return false;
+  for (int r = 0; r < d->n_replicas; ++r) {
+    if (F::TWO_D && d->replicas[r].L[2] != 1) return false;
+    for (int l = 0; l < 3; ++l)
+      if (d->periodic[l] && d->replicas[r].L[l] < 3 && !(F::TWO_D && l == 2)) return false;
+  }
+  std::map<std::vector<int>, int> idx;
+  for (int e = 0; e < t.n_int; ++e) {
+    double mx = 0.0;
+    for (int a = 0; a < 9; ++a) mx = std::max(mx, std::fabs(t.J[9 * e + a]));
+    if (!(mx > 0.0)) continue;
+    const int* T = t.T + 3 * e;
+    const int dX = T[0], dY = F::TWO_D ? T[2] : T[1], dZ = F::TWO_D ? T[1] : T[2];
+    std::vector<int> key = {t.bi[e], dX, dY, dZ, t.bj[e]};
+    if (idx.count(key)) return false;
+    idx[key] = e;
+  }
+  if ((int)idx.size() != F::NB * F::Z) return false;
+  TiledParams tp = TP;
+  for (int b = 0; b < F::NB; ++b) {
+    double shell_j[4] = {0, 0, 0, 0};
+    for (int k = 0; k < F::Z; ++k) {
+      const Slot sl = F::slot(b, k);
+      auto it = idx.find(std::vector<int>{b, sl.dx, sl.dy, sl.dz, sl.bj});
+      if (it == idx.end()) return false;
+      const double* J = t.J + 9 * it->second;
+      int g = 0;
+      while (k >= F::shell_end(b, g)) ++g;
+      const bool diag_equal = J[0] == J[4] && J[4] == J[8];
+      double iso = diag_equal ? J[0] : 0.0;
+      if (!F::REST) {
+        if (!diag_equal) return false;
+        for (int a = 0; a < 9; ++a)
+          if (a % 4 != 0 && J[a] != 0.0) return false;
+      }
+      const bool first = k == (g == 0 ? 0 : F::shell_end(b, g - 1));
+      if (first) shell_j[g] = iso;
+      else if (shell_j[g] != iso) return false;
+      if (F::REST) {
+        if (k >= 8) return false;
+        for (int a = 0; a < 9; ++a) tp.rest[b][k][a] = (float)(J[a] - ((a % 4 == 0) ? iso : 0.0));
+      }
+    }
+    for (int g = 0; g < F::NSHELL; ++g) {
+      const float hi = (float)shell_j[g];
+      tp.shell_hi[b][g] = hi;
+      tp.shell_lo[b][g] = (float)(shell_j[g] - (double)hi);
+    }
+  }
+  TP = tp;
+  return true;
+}
+
+int find_family(const llg_desc* d, const llg_term& t, TiledParams& TP) {
+  if (match_family<FamSC>(d, t, TP)) return kFamSC;
+  if (match_family<FamBCC>(d, t, TP)) return kFamBCC;
+  if (match_family<FamBCC3>(d, t, TP)) return kFamBCC3;
+  if (match_family<FamTRI>(d, t, TP)) return kFamTRI;
+  return kFamNone;
+}
+
+// tile work-list of the tiled kernels for the current TX
+int build_tiles4(llg_handle* h) {
+  std::vector<int4> t4;
+  for (size_t r = 0; r < h->reps.size(); ++r) {
+    const ReplicaDev& R = h->reps[r];
+    for (int x0 = 0; x0 < R.vL[0]; x0 += h->TP.TX)
+      for (int y0 = 0; y0 < R.vL[1]; y0 += h->ty)
+        for (int z0 = 0; z0 < R.vL[2]; z0 += h->tz) t4.push_back(make_int4((int)r, x0, y0, z0));
+  }
+  cudaError_t ce = h->d_tiles4.alloc(t4.size());
+  if (ce == cudaSuccess)
+    ce = cudaMemcpy(h->d_tiles4.p, t4.data(), t4.size() * sizeof(int4), cudaMemcpyHostToDevice);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "uploading tiles");
+  h->TP.tiles = h->d_tiles4.p;
+  h->TP.ntiles = (int)t4.size();
+  return 0;
+}
+
+void drop_graphs(llg_handle* h) {
+  for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
+  h->graphs.clear();
 }
 
 int build(llg_handle* h, const llg_desc* d) {
@@ -464,6 +561,43 @@ int build(llg_handle* h, const llg_desc* d) {
     h->rep_ntiles[r] = (int)h->tiles.size() - h->rep_first_tile[r];
     h->reps[r] = R;
   }
+  // tile views (X, Y, Z) of every replica
+  const bool two_d_possible = true;
+  (void)two_d_possible;
+  for (auto& R : h->reps) {
+    const int64_t nbl = d->nb;
+    R.vL[0] = R.L[0];
+    R.vL[1] = R.L[1];
+    R.vL[2] = R.L[2];
+    R.vs[0] = (int64_t)R.L[1] * R.L[2] * nbl;
+    R.vs[1] = (int64_t)R.L[2] * nbl;
+    R.vs[2] = nbl;
+    R.vper[0] = d->periodic[0];
+    R.vper[1] = d->periodic[1];
+    R.vper[2] = d->periodic[2];
+  }
+  if (!h->fp64 && ex.size() == 1) {
+    const llg_term& T = d->terms[ex[0].term];
+    h->family = find_family(d, T, h->TP);
+    if (h->family != kFamNone) {
+      h->tiled = true;
+      h->TP.exch_term = ex[0].term;
+      tiled_geometry(h->family, &h->tz, &h->ty);
+      if (h->family == kFamTRI) {
+        // monolayer: the contiguous axis is a2, the trivial axis a3
+        for (auto& R : h->reps) {
+          R.vL[1] = R.L[2];
+          R.vL[2] = R.L[1];
+          std::swap(R.vs[1], R.vs[2]);
+          R.vper[1] = d->periodic[2];
+          R.vper[2] = d->periodic[1];
+        }
+      }
+      int maxL = 1;
+      for (auto& R : h->reps) maxL = std::max(maxL, R.vL[0]);
+      h->TP.TX = std::min(8, maxL);
+    }
+  }
   h->npad = std::max<int64_t>(offset, 64);
   P.npad = h->npad;
   P.ntiles = (int)h->tiles.size();
@@ -505,7 +639,7 @@ int build(llg_handle* h, const llg_desc* d) {
     if (ce != cudaSuccess) return h->cuda_fail(ce, "allocating spin planes");
     cudaMemsetAsync(h->state[k].p, 0, (size_t)3 * h->npad * rs, h->stream);
   }
-  const bool need_aux = h->integrator == LLG_RK4 || h->fp64;
+  const bool need_aux = true;  // FP64 Heun ds, RK4 k sum, tiled Heun stored rhs
   if (need_aux) {
     ce = h->aux.alloc((size_t)3 * h->npad * rs);
     if (ce != cudaSuccess) return h->cuda_fail(ce, "allocating integrator scratch");
@@ -564,6 +698,10 @@ int build(llg_handle* h, const llg_desc* d) {
   if ((ce = h->d_partials.alloc(std::max<size_t>(max_tiles, 1) * nq)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   h->h_partials.resize(std::max<size_t>(max_tiles, 1) * nq);
   h->params_dirty = true;
+  if (h->tiled) {
+    int rc = build_tiles4(h);
+    if (rc) return rc;
+  }
   return 0;
 }
 
@@ -600,6 +738,28 @@ void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur) {
   const Params& P = h->P;
   const unsigned grid = (unsigned)P.ntiles;
   cudaStream_t st = h->stream;
+  if (h->tiled) {
+    const unsigned g4 = (unsigned)h->TP.ntiles;
+    float* aux = reinterpret_cast<float*>(h->aux.p);
+    if (h->integrator == LLG_HEUN) {
+      float* s0 = buf<float>(h, cur);
+      float* sp = buf<float>(h, 1);
+      if (stage == 0)
+        launch_tiled(h->family, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks);
+      else if (h->store_mode)
+        launch_tiled(h->family, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks);
+      else
+        launch_tiled(h->family, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks);
+    } else {
+      float* s0 = buf<float>(h, 0);
+      float* a = buf<float>(h, 1);
+      float* b = buf<float>(h, 2);
+      float* in = stage == 0 ? s0 : (stage == 2 ? b : a);
+      float* out = stage == 0 ? a : (stage == 1 ? b : (stage == 2 ? a : s0));
+      launch_tiled(h->family, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks);
+    }
+    return;
+  }
   if (h->integrator == LLG_HEUN) {
     if (h->fp64) {
       // state stays in buffer 0; 1 = predictor, aux = ds
@@ -636,7 +796,9 @@ void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur) {
   }
 }
 
-int next_buffer(const llg_handle* h, int cur) { return (!h->fp64 && h->integrator == LLG_HEUN) ? 2 - cur : cur; }
+int next_buffer(const llg_handle* h, int cur) {
+  return (!h->fp64 && h->integrator == LLG_HEUN && !(h->tiled && h->store_mode)) ? 2 - cur : cur;
+}
 
 // launches `nsteps` steps starting with the state in buffer `cur`; returns
 // the number of kernel launches
@@ -772,12 +934,12 @@ int llg_step(llg_handle* h, int32_t nsteps) {
   int rc = sync_replicas(h);
   if (rc) return rc;
   h->last_launches = 0;
-  const bool alternates = !h->fp64 && h->integrator == LLG_HEUN;
+  const bool alternates = next_buffer(h, 0) != 0;
   int K = h->steps_per_graph;
   if (alternates && (K & 1)) K += 1;  // graphs must return the state to the buffer they found it in
   int remaining = nsteps;
   while (remaining >= K && K > 1) {
-    GraphKey key{h->cur, K};
+    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->TP.TX, K};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
       cudaGraph_t g;
@@ -937,6 +1099,84 @@ int llg_set_stream(llg_handle* h, void* cuda_stream) {
 
 int64_t llg_last_launch_count(const llg_handle* h) { return h ? h->last_launches : -1; }
 
+int llg_kernel_info(const llg_handle* h, int32_t* info) {
+  if (!h || !info) return tls_fail(LLG_ERR_BAD_DESC, "null argument");
+  info[0] = h->tiled ? h->family : 0;
+  info[1] = h->tiled ? h->TP.TX : 0;
+  info[2] = h->store_mode ? 1 : 0;
+  info[3] = h->tz;
+  info[4] = h->ty;
+  info[5] = h->fp64 ? 1 : 0;
+  return 0;
+}
+
+static std::string tuning_key(const llg_handle* h) {
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, h->device);
+  std::string k = std::string(prop.name) + "|fam" + std::to_string(h->family) + "|int" +
+                  std::to_string(h->integrator) + "|nb" + std::to_string(h->nb) + "|nt" + std::to_string(h->nterms);
+  for (auto& R : h->reps)
+    k += "|" + std::to_string(R.L[0]) + "x" + std::to_string(R.L[1]) + "x" + std::to_string(R.L[2]) +
+         (R.thermal ? "T" : "0");
+  // long replica lists: keep the key short
+  if (k.size() > 400) {
+    uint64_t hsh = 1469598103934665603ull;
+    for (char c : k) hsh = (hsh ^ (unsigned char)c) * 1099511628211ull;
+    k = k.substr(0, 120) + "|h" + std::to_string(hsh);
+  }
+  return k;
+}
+
+static std::string tuning_cache_path() {
+  const char* p = getenv("JAMS_LLG_TUNE_CACHE");
+  if (p) return p;
+  const char* home = getenv("HOME");
+  return home ? std::string(home) + "/.cache/jams_llg_tuning.txt" : std::string();
+}
+
+static bool tuning_lookup(const std::string& key, int* tx, int* store) {
+  const std::string path = tuning_cache_path();
+  if (path.empty()) return false;
+  FILE* f = fopen(path.c_str(), "r");
+  if (!f) return false;
+  char line[1024];
+  bool found = false;
+  while (fgets(line, sizeof line, f)) {
+    char* tab = strchr(line, '\t');
+    if (!tab) continue;
+    *tab = 0;
+    if (key == line && sscanf(tab + 1, "%d %d", tx, store) == 2) found = true;
+  }
+  fclose(f);
+  return found;
+}
+
+static void tuning_store(const std::string& key, int tx, int store) {
+  const std::string path = tuning_cache_path();
+  if (path.empty()) return;
+  FILE* f = fopen(path.c_str(), "a");
+  if (!f) return;
+  fprintf(f, "%s\t%d %d\n", key.c_str(), tx, store);
+  fclose(f);
+}
+
+int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (!h->tiled) return 0;
+  if (planes_per_cta < 1) return h->fail(LLG_ERR_BAD_DESC, "planes_per_cta must be >= 1");
+  cudaSetDevice(h->device);
+  cudaError_t ce = cudaStreamSynchronize(h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamSynchronize");
+  drop_graphs(h);
+  h->store_mode = store_rhs != 0 && h->integrator == LLG_HEUN;
+  if (planes_per_cta != h->TP.TX) {
+    h->TP.TX = planes_per_cta;
+    int rc = build_tiles4(h);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
 int llg_profile_stages(llg_handle* h, int32_t nsteps, double* ms) {
   if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
   if (nsteps < 1 || !ms) return h->fail(LLG_ERR_BAD_DESC, "nsteps must be >= 1 and ms non-null");
@@ -972,6 +1212,75 @@ int llg_profile_stages(llg_handle* h, int32_t nsteps, double* ms) {
       ms[stg] += t / nsteps;
     }
   for (auto& e : ev) cudaEventDestroy(e);
+  return 0;
+}
+
+int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (!h->tiled) return 0;
+  if (trial_steps < 1) trial_steps = 10;
+  cudaSetDevice(h->device);
+  int rc = sync_replicas(h);
+  if (rc) return rc;
+  const std::string key = tuning_key(h);
+  int tx = 0, st = 0;
+  if (use_cache && tuning_lookup(key, &tx, &st)) return llg_set_tuning(h, tx, st);
+  // keep the state: the trials advance a copy
+  const size_t bytes = (size_t)3 * h->npad * real_size(h);
+  DevBuf<unsigned char> save;
+  cudaError_t ce = save.alloc(bytes);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "autotune scratch");
+  const int sb0 = state_buffer(h);
+  ce = cudaMemcpyAsync(save.p, h->state[sb0].p, bytes, cudaMemcpyDeviceToDevice, h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "autotune save");
+  const int64_t it0 = h->iteration;
+  const int cur0 = h->cur;
+  int maxL = 1;
+  for (auto& R : h->reps) maxL = std::max(maxL, R.vL[0]);
+  std::vector<std::pair<int, int>> cands;
+  for (int t : {1, 2, 4, 8, 16, 32, 64})
+    if (t <= std::max(1, maxL)) {
+      cands.push_back({t, 0});
+      if (h->integrator == LLG_HEUN) cands.push_back({t, 1});
+    }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  std::pair<int, int> choice = {h->TP.TX, h->store_mode ? 1 : 0};
+  for (auto& c : cands) {
+    rc = llg_set_tuning(h, c.first, c.second);
+    if (rc) break;
+    enqueue_steps(h, 2, h->cur);
+    h->cur = next_buffer(h, next_buffer(h, h->cur));
+    cudaEventRecord(e0, h->stream);
+    enqueue_steps(h, trial_steps, h->cur);
+    cudaEventRecord(e1, h->stream);
+    if (trial_steps & 1) h->cur = next_buffer(h, h->cur);
+    ce = cudaEventSynchronize(e1);
+    if (ce != cudaSuccess) {
+      rc = h->cuda_fail(ce, "autotune trial");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      choice = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  // restore state, buffer parity and the noise counter
+  h->cur = cur0;
+  rc = llg_set_tuning(h, choice.first, choice.second);
+  if (rc) return rc;
+  ce = cudaMemcpyAsync(h->state[state_buffer(h)].p, save.p, bytes, cudaMemcpyDeviceToDevice, h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "autotune restore");
+  rc = llg_set_iteration(h, it0);
+  if (rc) return rc;
+  tuning_store(key, choice.first, choice.second);
   return 0;
 }
 

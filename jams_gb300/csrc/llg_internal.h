@@ -71,6 +71,22 @@ struct ReplicaDev {
   float amp32[kMaxBasis]; // (float)(sigma_b sqrt(T))
   double B[3];            // applied field (T)
   float Bf[3];
+  // tile view for the tiled kernels: extents, spin-index strides and
+  // periodicity along (X, Y, Z); Z is the contiguous axis
+  int32_t vL[3];
+  int64_t vs[3];
+  int32_t vper[3];
+};
+
+// runtime data of the tiled FP32 kernels (llg_tiled.cu)
+struct TiledParams {
+  const int4* tiles;      // (replica, x0, y0, z0) per CTA
+  int ntiles;
+  int TX;                 // planes streamed per CTA
+  int exch_term;          // term handled by the tiled exchange
+  float shell_hi[kMaxBasis][4];
+  float shell_lo[kMaxBasis][4];
+  float rest[kMaxBasis][8][9];
 };
 
 struct Params {

@@ -42,6 +42,11 @@ void launch_unpack(bool fp64, cudaStream_t st, const double* aos, void* soa, int
 void launch_pack(bool fp64, cudaStream_t st, const void* soa, double* aos, int64_t offset, int64_t n,
                  int64_t npad);
 
+// tiled FP32 kernels (llg_tiled.cu); family ids in llg_families.h
+void tiled_geometry(int family, int* tz, int* ty);
+cudaError_t launch_tiled(int family, int stage, unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP,
+                         const float* s0, const float* sin, float* out, float* aux, uint32_t k);
+
 // observables (llg_observe.cu): ordered per-tile partial sums copied to
 // h_partials [ntiles][nq] = (sum mu_s Sx, Sy, Sz, sum mu_s, E_term...)
 int observe(const Params& P, const void* state, bool fp64, int replica, int first_tile, int ntiles,

@@ -33,7 +33,7 @@ EXPORTED = [
     "llg_set_state", "llg_get_state", "llg_set_state_device", "llg_get_state_device", "llg_step",
     "llg_synchronize", "llg_iteration", "llg_set_iteration", "llg_set_temperature", "llg_set_field",
     "llg_fields", "llg_observables", "llg_topological_charge", "llg_set_stream", "llg_last_launch_count",
-    "llg_profile_stages",
+    "llg_profile_stages", "llg_kernel_info", "llg_set_tuning", "llg_autotune",
 ]
 
 
@@ -106,6 +106,9 @@ def lib():
         L.llg_last_launch_count.argtypes = [vp]
         L.llg_last_launch_count.restype = i64
         L.llg_profile_stages.argtypes = [vp, i32, dp]
+        L.llg_kernel_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
+        L.llg_set_tuning.argtypes = [vp, i32, i32]
+        L.llg_autotune.argtypes = [vp, i32, i32]
         _lib = L
     return _lib
 
@@ -263,6 +266,20 @@ class Solver:
         ms = np.zeros(4)
         self._check(self.L.llg_profile_stages(self.h, int(nsteps), _dp(ms)))
         return ms[: 2 if self.workload.model.integrator == W.HEUN else 4]
+
+    def kernel_info(self) -> dict:
+        info = (ctypes.c_int32 * 8)()
+        self._check(self.L.llg_kernel_info(self.h, info))
+        fam = {0: "generic", 1: "sc", 2: "bcc", 3: "bcc3", 4: "triangular"}[info[0]]
+        return {"family": fam, "planes_per_cta": info[1], "store_rhs": bool(info[2]), "tile_z": info[3],
+                "tile_y": info[4], "fp64": bool(info[5])}
+
+    def autotune(self, trial_steps: int = 20, use_cache: bool = False) -> dict:
+        self._check(self.L.llg_autotune(self.h, int(trial_steps), int(bool(use_cache))))
+        return self.kernel_info()
+
+    def set_tuning(self, planes_per_cta: int, store_rhs: bool) -> None:
+        self._check(self.L.llg_set_tuning(self.h, int(planes_per_cta), int(bool(store_rhs))))
 
     @property
     def last_launch_count(self) -> int:

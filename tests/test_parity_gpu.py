@@ -216,3 +216,76 @@ def test_topological_charge_matches_oracle(llg, oracle):
     s.set_state(s0)
     q = s.topological_charge(0)
     assert abs(q - oracle.topological_charge_triangular(s0, 32, 32)) < 1e-10
+
+
+def test_tiled_families_selected(llg):
+    """FP32C picks the tiled kernel of the matching lattice family; FP64 and
+    templates outside the families use the gather kernels."""
+    cases_ = [(W.sc_ferromagnet(L=8), "sc"), (W.bcc_nearest_neighbour(L=4), "bcc"),
+              (W.bcc_three_shell(L=4), "bcc3"), (W.triangular_dmi_field_sweep(L=8, n_fields=1), "triangular")]
+    for w, fam in cases_:
+        assert solver(llg, w, llg.FP32C).kernel_info()["family"] == fam
+        assert solver(llg, w, llg.FP64).kernel_info()["family"] == "generic"
+
+
+def _split_exchange(w):
+    """The same Hamiltonian with the exchange split into two half-strength
+    terms: no tiled family applies (gather kernels)."""
+    import copy
+
+    w2 = copy.deepcopy(w)
+    ex = w2.model.terms[0]
+    half = W.Term(kind=ex.kind, bi=ex.bi, bj=ex.bj, T=ex.T, J=ex.J * 0.5, name="exchange-a")
+    w2.model.terms = [half, W.Term(kind=ex.kind, bi=ex.bi, bj=ex.bj, T=ex.T, J=ex.J * 0.5, name="exchange-b")] + \
+        w2.model.terms[1:]
+    return w2
+
+
+def test_fp32c_gather_kernels_within_bound(llg, oracle):
+    w = _split_exchange(W.bcc_three_shell(L=12, T=0.0, start="random"))
+    s0 = W.initial_state(w, 0)
+    ref = oracle.OracleSim(w).run(s0, 1000)
+    s = solver(llg, w, llg.FP32C)
+    assert s.kernel_info()["family"] == "generic"
+    s.set_state(s0)
+    s.step(1000)
+    assert np.abs(s.get_state(0) - ref).max() <= FP32C_TOL
+
+
+@pytest.mark.parametrize("name", ["bcc3", "sc", "tri"])
+def test_tiling_choices_give_identical_results(llg, name):
+    """Planes per CTA and stored vs recomputed rhs(s0) change the schedule,
+    not the arithmetic: states are bit-identical."""
+    w = {"bcc3": W.bcc_three_shell(L=10, T=300.0, start="random"),
+         "sc": W.sc_ferromagnet(L=(9, 12, 40), T=100.0),
+         "tri": W.triangular_dmi_field_sweep(L=(20, 300, 1), n_fields=2, T=5.0)}[name]
+    if name == "tri":
+        w.model.integrator = W.HEUN
+    outs = []
+    for tx, store in [(1, False), (1, True), (3, False), (8, True), (64, False)]:
+        s = solver(llg, w, llg.FP32C, steps_per_graph=4)
+        s.set_tuning(tx, store)
+        for r in range(len(w.replicas)):
+            s.set_state(W.initial_state(w, r), r)
+        s.step(11)
+        outs.append(s.get_state(-1))
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+
+
+def test_autotune_keeps_state_and_iteration(llg):
+    w = W.bcc_three_shell(L=8, T=300.0, start="random")
+    s0 = W.initial_state(w, 0)
+    a = solver(llg, w, llg.FP32C)
+    a.set_state(s0)
+    a.step(5)
+    before = a.get_state(0)
+    info = a.autotune(trial_steps=3)
+    assert info["family"] == "bcc3" and info["planes_per_cta"] >= 1
+    assert a.iteration == 5
+    assert np.array_equal(a.get_state(0), before)
+    a.step(7)
+    b = solver(llg, w, llg.FP32C)
+    b.set_state(s0)
+    b.step(12)
+    assert np.array_equal(a.get_state(0), b.get_state(0))
