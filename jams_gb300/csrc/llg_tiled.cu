@@ -13,6 +13,7 @@
 // Warps are laid out along Z (32 consecutive cells) with the basis site
 // uniform per warp, so the per-basis stencil never diverges.
 #include <cstdint>
+#include <utility>
 
 #include "llg_families.h"
 #include "llg_kernels.h"
@@ -21,6 +22,13 @@
 namespace jams_llg {
 
 namespace {
+
+// every FP32 operation below is an explicit intrinsic: the result does not
+// depend on how the compiler would contract a given kernel, so all tiling
+// choices (stored or recomputed rhs, planes per CTA) agree bit for bit
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float ff(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
 
 __device__ __forceinline__ void two_sum_t(float a, float b, float& s, float& e) {
   s = __fadd_rn(a, b);
@@ -58,22 +66,11 @@ __device__ __forceinline__ void noise_fast(uint64_t seed, uint32_t replica, uint
   float s1, c1, s2, c2;
   __sincosf(6.283185307179586f * (float)(c[1] >> 8) * 0x1.0p-24f, &s1, &c1);
   __sincosf(6.283185307179586f * (float)(c[3] >> 8) * 0x1.0p-24f, &s2, &c2);
-  w[0] = amp * r1 * c1;
-  w[1] = amp * r1 * s1;
-  w[2] = amp * r2 * c2;
+  w[0] = __fmul_rn(__fmul_rn(amp, r1), c1);
+  w[1] = __fmul_rn(__fmul_rn(amp, r1), s1);
+  w[2] = __fmul_rn(__fmul_rn(amp, r2), c2);
 }
 
-__device__ __forceinline__ int wrap(int v, int L, bool periodic, bool& valid) {
-  if (v < 0) {
-    if (!periodic) valid = false;
-    return v + L;
-  }
-  if (v >= L) {
-    if (!periodic) valid = false;
-    return v - L;
-  }
-  return v;
-}
 
 // anisotropy / applied-field terms (everything but the tiled exchange term)
 __device__ __forceinline__ void local_terms(const Params& P, const ReplicaDev& R, int b, int skip,
@@ -83,34 +80,35 @@ __device__ __forceinline__ void local_terms(const Params& P, const ReplicaDev& R
     const TermDev& T = P.term[t];
     if (T.kind == kUniaxial) {
       const float* a = T.axisf[b];
-      const float d = __fmaf_rn(a[2], s[2], __fmaf_rn(a[1], s[1], a[0] * s[0]));
+      const float d = ff(a[2], s[2], ff(a[1], s[1], fm(a[0], s[0])));
       float pw = d;
-      if (T.order >= 4) pw = d * d * d;
-      if (T.order >= 6) pw = pw * d * d;
-      const float pre = T.Kf[b] * (float)T.order * pw;
+      if (T.order >= 4) pw = fm(fm(d, d), d);
+      if (T.order >= 6) pw = fm(fm(pw, d), d);
+      const float pre = fm(fm(T.Kf[b], (float)T.order), pw);
 #pragma unroll
-      for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], pre * a[m]);
+      for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], fm(pre, a[m]));
     } else if (T.kind == kCubic) {
       const float* u = T.axisf[b];
-      const float Su = u[0] * s[0] + u[1] * s[1] + u[2] * s[2];
-      const float Sv = u[3] * s[0] + u[4] * s[1] + u[5] * s[2];
-      const float Sw = u[6] * s[0] + u[7] * s[1] + u[8] * s[2];
-      const float pre = 2.0f * T.Kf[b];
+      const float Su = ff(u[2], s[2], ff(u[1], s[1], fm(u[0], s[0])));
+      const float Sv = ff(u[5], s[2], ff(u[4], s[1], fm(u[3], s[0])));
+      const float Sw = ff(u[8], s[2], ff(u[7], s[1], fm(u[6], s[0])));
+      const float pre = fm(2.0f, T.Kf[b]);
+      const float Su2 = fm(Su, Su), Sv2 = fm(Sv, Sv), Sw2 = fm(Sw, Sw);
       float cu, cv, cw;
       if (T.order == 1) {
-        cu = Su * (Sv * Sv + Sw * Sw);
-        cv = Sv * (Sw * Sw + Su * Su);
-        cw = Sw * (Su * Su + Sv * Sv);
+        cu = fm(Su, fa(Sv2, Sw2));
+        cv = fm(Sv, fa(Sw2, Su2));
+        cw = fm(Sw, fa(Su2, Sv2));
       } else {
-        cu = Su * (Sv * Sv) * (Sw * Sw);
-        cv = Sv * (Sw * Sw) * (Su * Su);
-        cw = Sw * (Su * Su) * (Sv * Sv);
+        cu = fm(fm(Su, Sv2), Sw2);
+        cv = fm(fm(Sv, Sw2), Su2);
+        cw = fm(fm(Sw, Su2), Sv2);
       }
 #pragma unroll
-      for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], pre * (u[m] * cu + u[3 + m] * cv + u[6 + m] * cw));
+      for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], fm(pre, ff(u[6 + m], cw, ff(u[3 + m], cv, fm(u[m], cu)))));
     } else if (T.kind == kAppliedField) {
 #pragma unroll
-      for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], P.mus32[b] * R.Bf[m]);
+      for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], fm(P.mus32[b], R.Bf[m]));
     }
   }
 }
@@ -118,19 +116,21 @@ __device__ __forceinline__ void local_terms(const Params& P, const ReplicaDev& R
 __device__ __forceinline__ void llg_rhs_t(const Params& P, int b, const float s[3], const float h[3], const float w[3],
                                           float rhs[3]) {
   const float im = P.inv_mus32[b];
-  const float hh[3] = {__fmaf_rn(h[0], im, w[0]), __fmaf_rn(h[1], im, w[1]), __fmaf_rn(h[2], im, w[2])};
-  const float c1[3] = {s[1] * hh[2] - s[2] * hh[1], s[2] * hh[0] - s[0] * hh[2], s[0] * hh[1] - s[1] * hh[0]};
-  const float c2[3] = {s[1] * c1[2] - s[2] * c1[1], s[2] * c1[0] - s[0] * c1[2], s[0] * c1[1] - s[1] * c1[0]};
+  const float hh[3] = {ff(h[0], im, w[0]), ff(h[1], im, w[1]), ff(h[2], im, w[2])};
+  const float c1[3] = {ff(s[1], hh[2], -fm(s[2], hh[1])), ff(s[2], hh[0], -fm(s[0], hh[2])),
+                       ff(s[0], hh[1], -fm(s[1], hh[0]))};
+  const float c2[3] = {ff(s[1], c1[2], -fm(s[2], c1[1])), ff(s[2], c1[0], -fm(s[0], c1[2])),
+                       ff(s[0], c1[1], -fm(s[1], c1[0]))};
   const float mg = -P.gyro32[b], a = P.alpha32[b];
 #pragma unroll
-  for (int m = 0; m < 3; ++m) rhs[m] = mg * __fmaf_rn(a, c2[m], c1[m]);
+  for (int m = 0; m < 3; ++m) rhs[m] = fm(mg, ff(a, c2[m], c1[m]));
 }
 
 __device__ __forceinline__ void normalise_t(float v[3]) {
-  const float r = rsqrtf(__fmaf_rn(v[2], v[2], __fmaf_rn(v[1], v[1], v[0] * v[0])));
-  v[0] *= r;
-  v[1] *= r;
-  v[2] *= r;
+  const float r = rsqrtf(ff(v[2], v[2], ff(v[1], v[1], fm(v[0], v[0]))));
+  v[0] = fm(v[0], r);
+  v[1] = fm(v[1], r);
+  v[2] = fm(v[2], r);
 }
 
 template <class F, int TZ, int TY>
@@ -143,7 +143,44 @@ struct Geo {
   static constexpr int PER_THREAD = (PLANE + NT - 1) / NT;
 };
 
-// exchange field of basis site B at the thread's cell from one ring
+template <class F>
+__host__ __device__ constexpr int shell_of(int b, int k) {
+  int g = 0;
+  while (g + 1 < F::NSHELL && k >= F::shell_end(b, g)) ++g;
+  return g;
+}
+
+// one neighbour slot: every offset is a compile-time constant
+template <class F, int TZ, int TY, int B, int K>
+__device__ __forceinline__ void gather_slot(const float4* bm, const float4* b0, const float4* bp,
+                                            float (&a)[F::NSHELL][3], float (&r)[3], const TiledParams& TP) {
+  using G = Geo<F, TZ, TY>;
+  constexpr Slot sl = F::slot(B, K);
+  constexpr int off = (sl.bj * G::PY + sl.dy) * G::PZ + sl.dz;
+  constexpr int g = shell_of<F>(B, K);
+  const float4* p = sl.dx < 0 ? bm : (sl.dx == 0 ? b0 : bp);
+  const float4 v = p[off];
+  a[g][0] = fa(a[g][0], v.x);
+  a[g][1] = fa(a[g][1], v.y);
+  a[g][2] = fa(a[g][2], v.z);
+  if constexpr (F::REST != 0) {
+    const float* J = TP.rest[B][K];
+    r[0] = ff(J[0], v.x, ff(J[1], v.y, ff(J[2], v.z, r[0])));
+    r[1] = ff(J[3], v.x, ff(J[4], v.y, ff(J[5], v.z, r[1])));
+    r[2] = ff(J[6], v.x, ff(J[7], v.y, ff(J[8], v.z, r[2])));
+  }
+}
+
+template <class F, int TZ, int TY, int B, int... K>
+__device__ __forceinline__ void gather_all(std::integer_sequence<int, K...>, const float4* bm, const float4* b0,
+                                           const float4* bp, float (&a)[F::NSHELL][3], float (&r)[3],
+                                           const TiledParams& TP) {
+  (gather_slot<F, TZ, TY, B, K>(bm, b0, bp, a, r, TP), ...);
+}
+
+// exchange field of basis site B at the thread's cell from one ring: plain
+// FP32 sum of the neighbour spins of each shell, then h += J_shell * sum with
+// TwoProd/TwoSum compensation; 3x3 remainders (REST families) per slot
 template <class F, int TZ, int TY, int B>
 __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const float4* ring, int xs, int own,
                                                float hi[3], float lo[3]) {
@@ -151,45 +188,21 @@ __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const floa
   const float4* bm = ring + ((xs + 3) & 3) * G::PLANE + own;
   const float4* b0 = ring + (xs & 3) * G::PLANE + own;
   const float4* bp = ring + ((xs + 1) & 3) * G::PLANE + own;
-  if (!F::REST) {
-    // shell by shell: plain FP32 sum of the neighbour spins of a shell, then
-    // h += J_shell * sum with TwoProd/TwoSum compensation
+  float a[F::NSHELL][3];
+  float r[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int g = 0; g < F::NSHELL; ++g) {
-      float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+  for (int g = 0; g < F::NSHELL; ++g) a[g][0] = a[g][1] = a[g][2] = 0.f;
+  gather_all<F, TZ, TY, B>(std::make_integer_sequence<int, F::Z>{}, bm, b0, bp, a, r, TP);
 #pragma unroll
-      for (int k = (g == 0 ? 0 : F::shell_end(B, g - 1)); k < F::shell_end(B, g); ++k) {
-        const Slot sl = F::slot(B, k);
-        const float4 v = (sl.dx < 0 ? bm : sl.dx == 0 ? b0 : bp)[(sl.bj * G::PY + sl.dy) * G::PZ + sl.dz];
-        a0 += v.x;
-        a1 += v.y;
-        a2 += v.z;
-      }
-      acc_mad_t(hi[0], lo[0], TP.shell_hi[B][g], TP.shell_lo[B][g], a0);
-      acc_mad_t(hi[1], lo[1], TP.shell_hi[B][g], TP.shell_lo[B][g], a1);
-      acc_mad_t(hi[2], lo[2], TP.shell_hi[B][g], TP.shell_lo[B][g], a2);
-    }
-  } else {
-    // one isotropic shell plus a 3x3 remainder per slot
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f, r0 = 0.f, r1 = 0.f, r2 = 0.f;
-#pragma unroll
-    for (int k = 0; k < F::Z; ++k) {
-      const Slot sl = F::slot(B, k);
-      const float4 v = (sl.dx < 0 ? bm : sl.dx == 0 ? b0 : bp)[(sl.bj * G::PY + sl.dy) * G::PZ + sl.dz];
-      a0 += v.x;
-      a1 += v.y;
-      a2 += v.z;
-      const float* J = TP.rest[B][k];
-      r0 = __fmaf_rn(J[0], v.x, __fmaf_rn(J[1], v.y, __fmaf_rn(J[2], v.z, r0)));
-      r1 = __fmaf_rn(J[3], v.x, __fmaf_rn(J[4], v.y, __fmaf_rn(J[5], v.z, r1)));
-      r2 = __fmaf_rn(J[6], v.x, __fmaf_rn(J[7], v.y, __fmaf_rn(J[8], v.z, r2)));
-    }
-    acc_mad_t(hi[0], lo[0], TP.shell_hi[B][0], TP.shell_lo[B][0], a0);
-    acc_mad_t(hi[1], lo[1], TP.shell_hi[B][0], TP.shell_lo[B][0], a1);
-    acc_mad_t(hi[2], lo[2], TP.shell_hi[B][0], TP.shell_lo[B][0], a2);
-    acc_add_t(hi[0], lo[0], r0);
-    acc_add_t(hi[1], lo[1], r1);
-    acc_add_t(hi[2], lo[2], r2);
+  for (int g = 0; g < F::NSHELL; ++g) {
+    acc_mad_t(hi[0], lo[0], TP.shell_hi[B][g], TP.shell_lo[B][g], a[g][0]);
+    acc_mad_t(hi[1], lo[1], TP.shell_hi[B][g], TP.shell_lo[B][g], a[g][1]);
+    acc_mad_t(hi[2], lo[2], TP.shell_hi[B][g], TP.shell_lo[B][g], a[g][2]);
+  }
+  if constexpr (F::REST != 0) {
+    acc_add_t(hi[0], lo[0], r[0]);
+    acc_add_t(hi[1], lo[1], r[1]);
+    acc_add_t(hi[2], lo[2], r[2]);
   }
 }
 
@@ -225,31 +238,57 @@ struct PlaneRegs {
   float v[Geo<F, TZ, TY>::PER_THREAD][3];
 };
 
+// the replica's tile view, held in registers for the whole CTA
+struct View {
+  int L[3];
+  int st[3];      // spin-index strides (Z stride = basis count)
+  bool per[3];
+  int64_t offset;
+};
+
+__device__ __forceinline__ View load_view(const ReplicaDev& R) {
+  View v;
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    v.L[l] = R.vL[l];
+    v.st[l] = (int)R.vs[l];
+    v.per[l] = R.vper[l] != 0;
+  }
+  v.offset = R.offset;
+  return v;
+}
+
+// periodic wrap of a coordinate within one period of the lattice, without
+// branches; `valid` drops to false outside an open boundary or the lattice
+__device__ __forceinline__ int wrap_sel(int c, int L, bool per, bool& valid) {
+  const bool lo = c < 0, hi = c >= L;
+  valid = valid && (per || !(lo || hi));
+  const int w = c + (lo ? L : 0) - (hi ? L : 0);
+  valid = valid && w >= 0 && w < L;
+  return w;
+}
+
 template <class F, int TZ, int TY>
-__device__ __forceinline__ void fetch_plane(const ReplicaDev& R, const float* __restrict__ s, int64_t npad, int x,
+__device__ __forceinline__ void fetch_plane(const View& V, const float* __restrict__ s, int64_t npad, int x,
                                             int y0, int z0, int tid, PlaneRegs<F, TZ, TY>& pr) {
   using G = Geo<F, TZ, TY>;
   bool xvalid = true;
-  const int gx = wrap(x, R.vL[0], R.vper[0], xvalid);
+  const int gx = wrap_sel(x, V.L[0], V.per[0], xvalid);
+  const float* sx = s + V.offset;
 #pragma unroll
   for (int q = 0; q < G::PER_THREAD; ++q) {
     const int idx = tid + q * G::NT;
-    pr.v[q][0] = pr.v[q][1] = pr.v[q][2] = 0.f;
-    if (idx < G::PLANE) {
-      const int bb = idx % G::NB;
-      const int t = idx / G::NB;
-      const int zz = t % G::PZ;
-      const int yy = t / G::PZ;
-      bool valid = xvalid;
-      const int gy = wrap(y0 - F::RY + yy, R.vL[1], R.vper[1], valid);
-      const int gz = wrap(z0 - F::RZ + zz, R.vL[2], R.vper[2], valid);
-      if (valid && gy >= 0 && gy < R.vL[1] && gz >= 0 && gz < R.vL[2]) {
-        const int64_t gi = R.offset + (int64_t)gx * R.vs[0] + (int64_t)gy * R.vs[1] + (int64_t)gz * R.vs[2] + bb;
-        pr.v[q][0] = __ldg(s + gi);
-        pr.v[q][1] = __ldg(s + npad + gi);
-        pr.v[q][2] = __ldg(s + 2 * npad + gi);
-      }
-    }
+    const int bb = idx % G::NB;
+    const int t = idx / G::NB;
+    const int zz = t % G::PZ;
+    const int yy = t / G::PZ;
+    bool valid = xvalid && idx < G::PLANE;
+    const int gy = wrap_sel(y0 - F::RY + yy, V.L[1], V.per[1], valid);
+    const int gz = wrap_sel(z0 - F::RZ + zz, V.L[2], V.per[2], valid);
+    const int i = gx * V.st[0] + gy * V.st[1] + gz * V.st[2] + bb;
+    pr.v[q][0] = valid ? __ldg(sx + i) : 0.f;
+    pr.v[q][1] = valid ? __ldg(sx + npad + i) : 0.f;
+    pr.v[q][2] = valid ? __ldg(sx + 2 * npad + i) : 0.f;
   }
 }
 
@@ -288,26 +327,29 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT) tiled_stage(const __grid_c
   float4* ring1 = smem + 4 * G::PLANE;     // second ring (s0) for STAGE 1
   const int4 tile = TP.tiles[blockIdx.x];
   const ReplicaDev& R = P.rep[tile.x];
+  const View V = load_view(R);
+  const int thermal = R.thermal;
   const int x0 = tile.y, y0 = tile.z, z0 = tile.w;
   const int tid = threadIdx.x + TZ * threadIdx.y;
   const int tz = threadIdx.x;
   const int ty = threadIdx.y % TY;
   const int b = threadIdx.y / TY;
+  const float amp = R.amp32[b];
   const int y = y0 + ty, z = z0 + tz;
-  const bool active_yz = y < R.vL[1] && z < R.vL[2];
+  const bool active_yz = y < V.L[1] && z < V.L[2];
   const int own = (ty + F::RY) * G::PZ + (tz + F::RZ);
   const uint64_t step = *P.step_base + kstep;
   const float* gather_src = STAGE == 0 ? s0 : sin;
-  const int xe = min(x0 + TP.TX, R.vL[0]);
+  const int xe = min(x0 + TP.TX, V.L[0]);
 
   {
     PlaneRegs<F, TZ, TY> pr;
 #pragma unroll
     for (int d = -1; d <= 1; ++d) {
-      fetch_plane<F, TZ, TY>(R, gather_src, P.npad, x0 + d, y0, z0, tid, pr);
+      fetch_plane<F, TZ, TY>(V, gather_src, P.npad, x0 + d, y0, z0, tid, pr);
       store_plane<F, TZ, TY>(ring0, x0 + d, tid, pr);
       if (NR == 2) {
-        fetch_plane<F, TZ, TY>(R, s0, P.npad, x0 + d, y0, z0, tid, pr);
+        fetch_plane<F, TZ, TY>(V, s0, P.npad, x0 + d, y0, z0, tid, pr);
         store_plane<F, TZ, TY>(ring1, x0 + d, tid, pr);
       }
     }
@@ -318,14 +360,14 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT) tiled_stage(const __grid_c
     const bool more = x + 1 < xe;
     PlaneRegs<F, TZ, TY> pf0, pf1;
     if (more) {
-      fetch_plane<F, TZ, TY>(R, gather_src, P.npad, x + 2, y0, z0, tid, pf0);
-      if (NR == 2) fetch_plane<F, TZ, TY>(R, s0, P.npad, x + 2, y0, z0, tid, pf1);
+      fetch_plane<F, TZ, TY>(V, gather_src, P.npad, x + 2, y0, z0, tid, pf0);
+      if (NR == 2) fetch_plane<F, TZ, TY>(V, s0, P.npad, x + 2, y0, z0, tid, pf1);
     }
     if (active_yz) {
-      const int i = x * (int)R.vs[0] + y * (int)R.vs[1] + z * (int)R.vs[2] + b;  // spin index in the replica
-      const int64_t gi = R.offset + i;
+      const int i = x * V.st[0] + y * V.st[1] + z * V.st[2] + b;  // spin index in the replica
+      const int64_t gi = V.offset + i;
       float w[3] = {0.f, 0.f, 0.f};
-      if (R.thermal) noise_fast(P.seed, (uint32_t)tile.x, step, (uint32_t)i, R.amp32[b], w);
+      if (thermal) noise_fast(P.seed, (uint32_t)tile.x, step, (uint32_t)i, amp, w);
       float h[3], s[3], k[3];
       field_tiled<F, TZ, TY>(P, TP, R, b, ring0, x, own, h, s);
       llg_rhs_t(P, b, s, h, w, k);
@@ -354,9 +396,9 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT) tiled_stage(const __grid_c
           r0[1] = aux[P.npad + gi];
           r0[2] = aux[2 * P.npad + gi];
         }
-        const float hdt = 0.5f * P.dt32;
-        float v[3] = {__fmaf_rn(hdt, r0[0] + k[0], a[0]), __fmaf_rn(hdt, r0[1] + k[1], a[1]),
-                      __fmaf_rn(hdt, r0[2] + k[2], a[2])};
+        const float hdt = fm(0.5f, P.dt32);
+        float v[3] = {ff(hdt, fa(r0[0], k[0]), a[0]), ff(hdt, fa(r0[1], k[1]), a[1]),
+                      ff(hdt, fa(r0[2], k[2]), a[2])};
         normalise_t(v);
         if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
         out[gi] = v[0];
@@ -366,13 +408,13 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT) tiled_stage(const __grid_c
         const float a[3] = {s0[gi], s0[P.npad + gi], s0[2 * P.npad + gi]};
         float v[3];
         if (STAGE == 6) {
-          const float c = P.dt32 * (1.0f / 6.0f);
+          const float c = fm(P.dt32, 1.0f / 6.0f);
 #pragma unroll
-          for (int m = 0; m < 3; ++m) v[m] = __fmaf_rn(c, aux[m * P.npad + gi] + k[m], a[m]);
+          for (int m = 0; m < 3; ++m) v[m] = ff(c, fa(aux[m * P.npad + gi], k[m]), a[m]);
           normalise_t(v);
           if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
         } else {
-          const float c = STAGE == 5 ? P.dt32 : 0.5f * P.dt32;
+          const float c = STAGE == 5 ? P.dt32 : fm(0.5f, P.dt32);
 #pragma unroll
           for (int m = 0; m < 3; ++m) {
             const float acc = STAGE == 3 ? k[m] : __fmaf_rn(2.0f, k[m], aux[m * P.npad + gi]);
