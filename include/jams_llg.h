@@ -203,6 +203,22 @@ int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t store_rhs);
    ~/.cache/jams_llg_tuning.txt), keyed by device, lattice and terms. */
 int llg_autotune(llg_handle *h, int32_t trial_steps, int32_t use_cache);
 
+/* No counterpart in the reference.  Magnetisation m4 = (Mx, My, Mz, |M|),
+   M = sum mu_s S / sum mu_s, of n_spins spins already on the device (N x 3
+   doubles, basis site of spin i = i % nb, mu_s per basis site in mus[nb]),
+   written to m4_dev (4 doubles of device memory) on cuda_stream - without
+   allocating anything.  It exists for callers that cannot call cudaMalloc
+   when they need the value: code running during stream capture, host loops
+   that must not synchronise the device, memory owned by an external pool.
+   Its reduction scratch is a fixed 32 KiB device array inside the library
+   (held on every GPU that loads it until exit); n_spins above 2^30 or not a
+   multiple of nb is rejected with LLG_ERR_BAD_DESC.  The first call on a
+   device looks up that array's device address; make that first call before
+   any stream capture.  All calls share the array: calls that overlap on the
+   GPU race.  Errors are reported through llg_last_error(NULL). */
+int llg_magnetisation_noalloc(const double *spins_dev, int64_t n_spins, int32_t nb, const double *mus,
+                              double *m4_dev, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,8 +34,15 @@
 using namespace jams_llg;
 
 namespace {
-
 thread_local std::string g_tls_error;
+}
+
+namespace jams_llg {
+// thread-local message for llg_last_error(NULL), used by entry points without a handle
+void set_thread_error(const char* msg) { g_tls_error = msg; }
+}  // namespace jams_llg
+
+namespace {
 
 // src/jams/helpers/consts.h:32
 constexpr double kBoltzmannIU = 0.0861733326;

@@ -33,7 +33,7 @@ EXPORTED = [
     "llg_set_state", "llg_get_state", "llg_set_state_device", "llg_get_state_device", "llg_step",
     "llg_synchronize", "llg_iteration", "llg_set_iteration", "llg_set_temperature", "llg_set_field",
     "llg_fields", "llg_observables", "llg_topological_charge", "llg_set_stream", "llg_last_launch_count",
-    "llg_profile_stages", "llg_kernel_info", "llg_set_tuning", "llg_autotune",
+    "llg_profile_stages", "llg_kernel_info", "llg_set_tuning", "llg_autotune", "llg_magnetisation_noalloc",
 ]
 
 
@@ -109,6 +109,7 @@ def lib():
         L.llg_kernel_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
         L.llg_set_tuning.argtypes = [vp, i32, i32]
         L.llg_autotune.argtypes = [vp, i32, i32]
+        L.llg_magnetisation_noalloc.argtypes = [vp, i64, i32, dp, vp, vp]
         _lib = L
     return _lib
 
