@@ -55,6 +55,7 @@ WORKLOADS = {
     "bcc64_3shell": lambda: W.bcc_three_shell(L=64, T=300.0, start="+z"),
     # the same Hamiltonian at 128^3 x 2 (4.2 M spins): state larger than L2, for profiling
     "bcc128_3shell": lambda: W.bcc_three_shell(L=128, T=300.0, start="+z"),
+    "bcc128_nn": lambda: W.bcc_nearest_neighbour(L=128, T=500.0),
     # simple-cubic 32^3, T = 0, Heun dt 1 fs (the reference's CPU-runnable case)
     "sc32": lambda: W.sc_ferromagnet(L=32, T=0.0),
     # bcc 256^3 x 2 (33.5 M spins), 500 K, both readings of its Hamiltonian
@@ -79,6 +80,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-steps", type=int, default=50)
     p.add_argument("--no-tune", action="store_true")
+    p.add_argument("--tuning", default="", help="planes_per_cta,store_rhs,occupancy instead of autotuning")
     return p.parse_args()
 
 
@@ -262,7 +264,12 @@ def main():
         sol.set_state(W.initial_state(w, r), r)
     n_spins = sol.num_spins(-1)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    tuning = sol.autotune(trial_steps=10) if not args.no_tune else sol.kernel_info()
+    if args.tuning:
+        tx, st, oc = (int(v) for v in args.tuning.split(","))
+        sol.set_tuning(tx, bool(st), oc)
+        tuning = sol.kernel_info()
+    else:
+        tuning = sol.autotune(trial_steps=10) if not args.no_tune else sol.kernel_info()
 
     # warm-up (also builds nothing lazily: single steps use direct launches)
     for _ in range(args.warmup):

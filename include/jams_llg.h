@@ -189,12 +189,14 @@ int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
    neighbours, 3 bcc three shells, 4 triangular monolayer), info[1] planes
    streamed per CTA, info[2] 1 when the Heun predictor stores rhs(s0) for
    the corrector (else the corrector recomputes it), info[3..4] CTA tile
-   (cells along the contiguous axis, rows), info[5] 1 for FP64. */
+   (cells along the contiguous axis, rows), info[5] 1 for FP64, info[6] the
+   occupancy variant (CTAs per SM the tiled kernels were compiled for). */
 int llg_kernel_info(const llg_handle *h, int32_t *info);
 
 /* Tiling choice of the tiled FP32 kernels (no effect on other kernels):
-   planes streamed per CTA and whether the Heun predictor stores rhs(s0). */
-int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t store_rhs);
+   planes streamed per CTA; flags bit 0: the Heun predictor stores rhs(s0);
+   flags >> 4: occupancy variant, 2 (<= 128 registers) or 4 (<= 64). */
+int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t flags);
 
 /* Times every tiling candidate (planes per CTA 1..64, stored or recomputed
    rhs) for trial_steps steps on a copy of the state and keeps the fastest;

@@ -49,6 +49,7 @@ def _stale(objs) -> bool:
 
 
 def build(force: bool = False, verbose: bool = False, extra=()) -> str:
+    extra = list(extra) + os.environ.get("JAMS_LLG_NVCC_EXTRA", "").split()
     os.makedirs(OUT, exist_ok=True)
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
     if not force and not _stale(srcs):

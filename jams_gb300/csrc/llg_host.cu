@@ -132,6 +132,7 @@ struct llg_handle {
   int family = kFamNone;
   bool tiled = false;
   bool store_mode = false;   // Heun: predictor stores rhs(s0) instead of the corrector recomputing it
+  int occupancy = 2;         // tiled kernels compiled for >= 2 or >= 4 CTAs per SM
   int tz = 0, ty = 0;
   TiledParams TP{};
   DevBuf<int4> d_tiles4;
@@ -379,6 +380,15 @@ int build(llg_handle* h, const llg_desc* d) {
   P.dt = d->dt;
   P.dt32 = (float)d->dt;
   P.seed = d->seed;
+  {
+    uint32_t k0 = (uint32_t)d->seed, k1 = (uint32_t)(d->seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+      P.philox_keys[2 * r] = k0;
+      P.philox_keys[2 * r + 1] = k1;
+      k0 += 0x9E3779B9u;  // Weyl key schedule of Philox4x32
+      k1 += 0xBB67AE85u;
+    }
+  }
   P.rk4_normalise_stages = d->rk4_normalise_stages;
   for (int b = 0; b < d->nb; ++b) {
     P.mus[b] = d->mus[b];
@@ -752,18 +762,18 @@ void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur) {
       float* s0 = buf<float>(h, cur);
       float* sp = buf<float>(h, 1);
       if (stage == 0)
-        launch_tiled(h->family, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks);
+        launch_tiled(h->family, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks);
       else if (h->store_mode)
-        launch_tiled(h->family, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks);
+        launch_tiled(h->family, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks);
       else
-        launch_tiled(h->family, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks);
+        launch_tiled(h->family, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks);
     } else {
       float* s0 = buf<float>(h, 0);
       float* a = buf<float>(h, 1);
       float* b = buf<float>(h, 2);
       float* in = stage == 0 ? s0 : (stage == 2 ? b : a);
       float* out = stage == 0 ? a : (stage == 1 ? b : (stage == 2 ? a : s0));
-      launch_tiled(h->family, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks);
+      launch_tiled(h->family, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks);
     }
     return;
   }
@@ -946,7 +956,7 @@ int llg_step(llg_handle* h, int32_t nsteps) {
   if (alternates && (K & 1)) K += 1;  // graphs must return the state to the buffer they found it in
   int remaining = nsteps;
   while (remaining >= K && K > 1) {
-    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->TP.TX, K};
+    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 32 * h->TP.TX, K};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
       cudaGraph_t g;
@@ -1114,6 +1124,7 @@ int llg_kernel_info(const llg_handle* h, int32_t* info) {
   info[3] = h->tz;
   info[4] = h->ty;
   info[5] = h->fp64 ? 1 : 0;
+  info[6] = h->occupancy;
   return 0;
 }
 
@@ -1175,7 +1186,8 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
   cudaError_t ce = cudaStreamSynchronize(h->stream);
   if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamSynchronize");
   drop_graphs(h);
-  h->store_mode = store_rhs != 0 && h->integrator == LLG_HEUN;
+  h->store_mode = (store_rhs & 1) != 0 && h->integrator == LLG_HEUN;
+  h->occupancy = (store_rhs >> 4) >= 3 ? 4 : 2;
   if (planes_per_cta != h->TP.TX) {
     h->TP.TX = planes_per_cta;
     int rc = build_tiles4(h);
@@ -1244,17 +1256,18 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   const int cur0 = h->cur;
   int maxL = 1;
   for (auto& R : h->reps) maxL = std::max(maxL, R.vL[0]);
-  std::vector<std::pair<int, int>> cands;
+  std::vector<std::pair<int, int>> cands;   // (planes per CTA, store flag | occupancy << 4)
   for (int t : {1, 2, 4, 8, 16, 32, 64})
-    if (t <= std::max(1, maxL)) {
-      cands.push_back({t, 0});
-      if (h->integrator == LLG_HEUN) cands.push_back({t, 1});
-    }
+    if (t <= std::max(1, maxL))
+      for (int occ : {2, 4}) {
+        cands.push_back({t, occ << 4});
+        if (h->integrator == LLG_HEUN) cands.push_back({t, 1 | (occ << 4)});
+      }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  std::pair<int, int> choice = {h->TP.TX, h->store_mode ? 1 : 0};
+  std::pair<int, int> choice = {h->TP.TX, (h->store_mode ? 1 : 0) | (h->occupancy << 4)};
   for (auto& c : cands) {
     rc = llg_set_tuning(h, c.first, c.second);
     if (rc) break;

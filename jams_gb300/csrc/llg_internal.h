@@ -120,6 +120,7 @@ struct Params {
   int rk4_normalise_stages;
   unsigned int* status;   // bit 0: non-finite spin
   const uint64_t* step_base;  // iteration number of step 0 of a launch block
+  uint32_t philox_keys[20];   // Philox4x32-10 round keys of the seed
 };
 
 }  // namespace jams_llg

@@ -27,16 +27,33 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
       k0 += 0x9E3779B9u;
       k1 += 0xBB67AE85u;
     }
-    const uint32_t lo0 = 0xD2511F53u * c[0];
-    const uint32_t hi0 = __umulhi(0xD2511F53u, c[0]);
-    const uint32_t lo1 = 0xCD9E8D57u * c[2];
-    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]);
+    // one 32 x 32 -> 64-bit multiply per word gives both halves
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
+    const uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
     const uint32_t n0 = hi1 ^ c[1] ^ k0;
     const uint32_t n2 = hi0 ^ c[3] ^ k1;
     c[0] = n0;
     c[1] = lo1;
     c[2] = n2;
     c[3] = lo0;
+  }
+}
+
+// the same generator with the 10 round keys precomputed (keys[2r], keys[2r+1]
+// = round r key words); gives the same words as philox4x32_10
+__device__ __forceinline__ void philox4x32_10_keyed(uint32_t c[4], const uint32_t* keys) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ keys[2 * r];
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ keys[2 * r + 1];
+    c[1] = (uint32_t)p1;
+    c[3] = (uint32_t)p0;
+    c[0] = n0;
+    c[2] = n2;
   }
 }
 

@@ -17,6 +17,12 @@
 
 #include "llg_families.h"
 #include "llg_kernels.h"
+
+// neighbour sums with packed f32x2 adds for x and y (1) or scalar adds (0);
+// both give the same sums bit for bit
+#ifndef JAMS_TILED_PACKED_GATHER
+#define JAMS_TILED_PACKED_GATHER 0
+#endif
 #include "llg_noise.cuh"
 
 namespace jams_llg {
@@ -29,6 +35,53 @@ namespace {
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float ff(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+
+// packed pairs of FP32 (Blackwell f32x2 instructions, round to nearest):
+// the x and y components of a spin or field travel as one 64-bit register
+// (the 64-bit pairs are formed and split inside the PTX, so no C++ type
+// punning is involved)
+#define JAMS_F32X2_BINARY(NAME, OP)                                                              \
+  __device__ __forceinline__ float2 NAME(float2 a, float2 b) {                                    \
+    float2 d;                                                                                     \
+    asm("{.reg .b64 ra, rb, rd;\n\t"                                                              \
+        "mov.b64 ra, {%2, %3};\n\t"                                                               \
+        "mov.b64 rb, {%4, %5};\n\t" OP " rd, ra, rb;\n\t"                                       \
+        "mov.b64 {%0, %1}, rd;}"                                                                  \
+        : "=f"(d.x), "=f"(d.y)                                                                    \
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                                \
+    return d;                                                                                     \
+  }
+JAMS_F32X2_BINARY(add2, "add.rn.f32x2")
+JAMS_F32X2_BINARY(sub2, "sub.rn.f32x2")
+JAMS_F32X2_BINARY(mul2, "mul.rn.f32x2")
+#undef JAMS_F32X2_BINARY
+
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\t"
+      "mov.b64 rb, {%4, %5};\n\t"
+      "mov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\t"
+      "mov.b64 {%0, %1}, rd;}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+
+// (hi, lo) += (jhi + jlo) a for a packed pair, with TwoProd (p = jhi a,
+// pe = jhi a - p exactly) and TwoSum (hi + p = s + e exactly); jn = -jhi
+// lets the negated product feed both without extra sign flips
+__device__ __forceinline__ void acc_mad2(float2& hi, float2& lo, float jhi, float jn, float jlo, float2 a) {
+  const float2 J = make_float2(jhi, jhi), JN = make_float2(jn, jn), JL = make_float2(jlo, jlo);
+  const float2 pn = mul2(JN, a);         // -p
+  const float2 pe = fma2(J, a, pn);      // jhi a - p
+  const float2 s = sub2(hi, pn);         // hi + p
+  const float2 bb = sub2(s, hi);
+  const float2 e = sub2(sub2(hi, sub2(s, bb)), add2(pn, bb));
+  hi = s;
+  lo = add2(lo, add2(e, fma2(JL, a, pe)));
+}
 
 __device__ __forceinline__ void two_sum_t(float a, float b, float& s, float& e) {
   s = __fadd_rn(a, b);
@@ -54,10 +107,10 @@ __device__ __forceinline__ void acc_mad_t(float& hi, float& lo, float jhi, float
 
 // thermal field for the FP32 form: Philox4x32-10 words, Box-Muller with the
 // special-function unit (log2, sin, cos, rsqrt)
-__device__ __forceinline__ void noise_fast(uint64_t seed, uint32_t replica, uint64_t step, uint32_t spin, float amp,
-                                           float w[3]) {
+__device__ __forceinline__ void noise_fast(const uint32_t* keys, uint32_t replica, uint64_t step, uint32_t spin,
+                                           float amp, float w[3]) {
   uint32_t c[4] = {spin, replica, (uint32_t)step, (uint32_t)(step >> 32)};
-  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  philox4x32_10_keyed(c, keys);
   const float u1 = (float)((c[0] >> 8) + 1u) * 0x1.0p-24f;
   const float u2 = (float)((c[2] >> 8) + 1u) * 0x1.0p-24f;
   const float x1 = fmaxf(-1.3862943611198906f * __log2f(u1), 1e-30f);  // -2 ln u1
@@ -72,56 +125,98 @@ __device__ __forceinline__ void noise_fast(uint64_t seed, uint32_t replica, uint
 }
 
 
-// anisotropy / applied-field terms (everything but the tiled exchange term)
-__device__ __forceinline__ void local_terms(const Params& P, const ReplicaDev& R, int b, int skip,
-                                            const float s[3], float hi[3], float lo[3]) {
+// Anisotropy and applied-field terms of one basis site, gathered once per
+// CTA into registers (at most one uniaxial, one cubic and one applied-field
+// term; the host sends other term lists to the gather kernels).  They are
+// summed in plain FP32 and added to the compensated exchange sum once.
+struct LocalField {
+  float uk;       // K * p of the uniaxial term (0: none)
+  int upow;
+  float ua[3];
+  float ck;       // 2 K of the cubic term (0: none)
+  int corder;
+  float cu[9];
+  float hb[3];    // mu_s B
+  float inv_mus, mg, alpha;
+};
+
+__device__ __forceinline__ LocalField local_field(const Params& P, const ReplicaDev& R, int b, int skip) {
+  LocalField L;
+  L.uk = 0.f;
+  L.upow = 2;
+  L.ck = 0.f;
+  L.corder = 1;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    L.ua[m] = 0.f;
+    L.hb[m] = 0.f;
+  }
+#pragma unroll
+  for (int m = 0; m < 9; ++m) L.cu[m] = 0.f;
   for (int t = 0; t < P.nterms; ++t) {
     if (t == skip) continue;
     const TermDev& T = P.term[t];
     if (T.kind == kUniaxial) {
-      const float* a = T.axisf[b];
-      const float d = ff(a[2], s[2], ff(a[1], s[1], fm(a[0], s[0])));
-      float pw = d;
-      if (T.order >= 4) pw = fm(fm(d, d), d);
-      if (T.order >= 6) pw = fm(fm(pw, d), d);
-      const float pre = fm(fm(T.Kf[b], (float)T.order), pw);
-#pragma unroll
-      for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], fm(pre, a[m]));
+      L.uk = fm(T.Kf[b], (float)T.order);
+      L.upow = T.order;
+      for (int m = 0; m < 3; ++m) L.ua[m] = T.axisf[b][m];
     } else if (T.kind == kCubic) {
-      const float* u = T.axisf[b];
-      const float Su = ff(u[2], s[2], ff(u[1], s[1], fm(u[0], s[0])));
-      const float Sv = ff(u[5], s[2], ff(u[4], s[1], fm(u[3], s[0])));
-      const float Sw = ff(u[8], s[2], ff(u[7], s[1], fm(u[6], s[0])));
-      const float pre = fm(2.0f, T.Kf[b]);
-      const float Su2 = fm(Su, Su), Sv2 = fm(Sv, Sv), Sw2 = fm(Sw, Sw);
-      float cu, cv, cw;
-      if (T.order == 1) {
-        cu = fm(Su, fa(Sv2, Sw2));
-        cv = fm(Sv, fa(Sw2, Su2));
-        cw = fm(Sw, fa(Su2, Sv2));
-      } else {
-        cu = fm(fm(Su, Sv2), Sw2);
-        cv = fm(fm(Sv, Sw2), Su2);
-        cw = fm(fm(Sw, Su2), Sv2);
-      }
-#pragma unroll
-      for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], fm(pre, ff(u[6 + m], cw, ff(u[3 + m], cv, fm(u[m], cu)))));
+      L.ck = fm(2.0f, T.Kf[b]);
+      L.corder = T.order;
+      for (int m = 0; m < 9; ++m) L.cu[m] = T.axisf[b][m];
     } else if (T.kind == kAppliedField) {
-#pragma unroll
-      for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], fm(P.mus32[b], R.Bf[m]));
+      for (int m = 0; m < 3; ++m) L.hb[m] = fm(P.mus32[b], R.Bf[m]);
     }
   }
+  L.inv_mus = P.inv_mus32[b];
+  L.mg = -P.gyro32[b];
+  L.alpha = P.alpha32[b];
+  return L;
 }
 
-__device__ __forceinline__ void llg_rhs_t(const Params& P, int b, const float s[3], const float h[3], const float w[3],
+__device__ __forceinline__ void local_terms(const LocalField& L, const float s[3], float hi[3], float lo[3]) {
+  float l[3] = {L.hb[0], L.hb[1], L.hb[2]};
+  if (L.uk != 0.f) {
+    const float d = ff(L.ua[2], s[2], ff(L.ua[1], s[1], fm(L.ua[0], s[0])));
+    float pw = d;
+    if (L.upow >= 4) pw = fm(fm(d, d), d);
+    if (L.upow >= 6) pw = fm(fm(pw, d), d);
+    const float pre = fm(L.uk, pw);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) l[m] = ff(pre, L.ua[m], l[m]);
+  }
+  if (L.ck != 0.f) {
+    const float* u = L.cu;
+    const float Su = ff(u[2], s[2], ff(u[1], s[1], fm(u[0], s[0])));
+    const float Sv = ff(u[5], s[2], ff(u[4], s[1], fm(u[3], s[0])));
+    const float Sw = ff(u[8], s[2], ff(u[7], s[1], fm(u[6], s[0])));
+    const float Su2 = fm(Su, Su), Sv2 = fm(Sv, Sv), Sw2 = fm(Sw, Sw);
+    float cu, cv, cw;
+    if (L.corder == 1) {
+      cu = fm(Su, fa(Sv2, Sw2));
+      cv = fm(Sv, fa(Sw2, Su2));
+      cw = fm(Sw, fa(Su2, Sv2));
+    } else {
+      cu = fm(fm(Su, Sv2), Sw2);
+      cv = fm(fm(Sv, Sw2), Su2);
+      cw = fm(fm(Sw, Su2), Sv2);
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) l[m] = ff(L.ck, ff(u[6 + m], cw, ff(u[3 + m], cv, fm(u[m], cu))), l[m]);
+  }
+#pragma unroll
+  for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], l[m]);
+}
+
+__device__ __forceinline__ void llg_rhs_t(const LocalField& L, const float s[3], const float h[3], const float w[3],
                                           float rhs[3]) {
-  const float im = P.inv_mus32[b];
+  const float im = L.inv_mus;
   const float hh[3] = {ff(h[0], im, w[0]), ff(h[1], im, w[1]), ff(h[2], im, w[2])};
   const float c1[3] = {ff(s[1], hh[2], -fm(s[2], hh[1])), ff(s[2], hh[0], -fm(s[0], hh[2])),
                        ff(s[0], hh[1], -fm(s[1], hh[0]))};
   const float c2[3] = {ff(s[1], c1[2], -fm(s[2], c1[1])), ff(s[2], c1[0], -fm(s[0], c1[2])),
                        ff(s[0], c1[1], -fm(s[1], c1[0]))};
-  const float mg = -P.gyro32[b], a = P.alpha32[b];
+  const float mg = L.mg, a = L.alpha;
 #pragma unroll
   for (int m = 0; m < 3; ++m) rhs[m] = fm(mg, ff(a, c2[m], c1[m]));
 }
@@ -153,16 +248,21 @@ __host__ __device__ constexpr int shell_of(int b, int k) {
 // one neighbour slot: every offset is a compile-time constant
 template <class F, int TZ, int TY, int B, int K>
 __device__ __forceinline__ void gather_slot(const float4* bm, const float4* b0, const float4* bp,
-                                            float (&a)[F::NSHELL][3], float (&r)[3], const TiledParams& TP) {
+                                            float2 (&axy)[F::NSHELL], float (&az)[F::NSHELL], float (&r)[3],
+                                            const TiledParams& TP) {
   using G = Geo<F, TZ, TY>;
   constexpr Slot sl = F::slot(B, K);
   constexpr int off = (sl.bj * G::PY + sl.dy) * G::PZ + sl.dz;
   constexpr int g = shell_of<F>(B, K);
   const float4* p = sl.dx < 0 ? bm : (sl.dx == 0 ? b0 : bp);
   const float4 v = p[off];
-  a[g][0] = fa(a[g][0], v.x);
-  a[g][1] = fa(a[g][1], v.y);
-  a[g][2] = fa(a[g][2], v.z);
+#if JAMS_TILED_PACKED_GATHER
+  axy[g] = add2(axy[g], make_float2(v.x, v.y));
+#else
+  axy[g].x = fa(axy[g].x, v.x);
+  axy[g].y = fa(axy[g].y, v.y);
+#endif
+  az[g] = fa(az[g], v.z);
   if constexpr (F::REST != 0) {
     const float* J = TP.rest[B][K];
     r[0] = ff(J[0], v.x, ff(J[1], v.y, ff(J[2], v.z, r[0])));
@@ -173,14 +273,15 @@ __device__ __forceinline__ void gather_slot(const float4* bm, const float4* b0, 
 
 template <class F, int TZ, int TY, int B, int... K>
 __device__ __forceinline__ void gather_all(std::integer_sequence<int, K...>, const float4* bm, const float4* b0,
-                                           const float4* bp, float (&a)[F::NSHELL][3], float (&r)[3],
-                                           const TiledParams& TP) {
-  (gather_slot<F, TZ, TY, B, K>(bm, b0, bp, a, r, TP), ...);
+                                           const float4* bp, float2 (&axy)[F::NSHELL], float (&az)[F::NSHELL],
+                                           float (&r)[3], const TiledParams& TP) {
+  (gather_slot<F, TZ, TY, B, K>(bm, b0, bp, axy, az, r, TP), ...);
 }
 
 // exchange field of basis site B at the thread's cell from one ring: plain
-// FP32 sum of the neighbour spins of each shell, then h += J_shell * sum with
-// TwoProd/TwoSum compensation; 3x3 remainders (REST families) per slot
+// FP32 sum of the neighbour spins of each shell (x and y packed), then
+// h += J_shell * sum with TwoProd/TwoSum compensation; 3x3 remainders (REST
+// families) per slot
 template <class F, int TZ, int TY, int B>
 __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const float4* ring, int xs, int own,
                                                float hi[3], float lo[3]) {
@@ -188,17 +289,25 @@ __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const floa
   const float4* bm = ring + ((xs + 3) & 3) * G::PLANE + own;
   const float4* b0 = ring + (xs & 3) * G::PLANE + own;
   const float4* bp = ring + ((xs + 1) & 3) * G::PLANE + own;
-  float a[F::NSHELL][3];
+  float2 axy[F::NSHELL];
+  float az[F::NSHELL];
   float r[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-  for (int g = 0; g < F::NSHELL; ++g) a[g][0] = a[g][1] = a[g][2] = 0.f;
-  gather_all<F, TZ, TY, B>(std::make_integer_sequence<int, F::Z>{}, bm, b0, bp, a, r, TP);
+  for (int g = 0; g < F::NSHELL; ++g) {
+    axy[g] = make_float2(0.f, 0.f);
+    az[g] = 0.f;
+  }
+  gather_all<F, TZ, TY, B>(std::make_integer_sequence<int, F::Z>{}, bm, b0, bp, axy, az, r, TP);
+  float2 hxy = make_float2(hi[0], hi[1]), lxy = make_float2(lo[0], lo[1]);
 #pragma unroll
   for (int g = 0; g < F::NSHELL; ++g) {
-    acc_mad_t(hi[0], lo[0], TP.shell_hi[B][g], TP.shell_lo[B][g], a[g][0]);
-    acc_mad_t(hi[1], lo[1], TP.shell_hi[B][g], TP.shell_lo[B][g], a[g][1]);
-    acc_mad_t(hi[2], lo[2], TP.shell_hi[B][g], TP.shell_lo[B][g], a[g][2]);
+    acc_mad2(hxy, lxy, TP.shell_hi[B][g], -TP.shell_hi[B][g], TP.shell_lo[B][g], axy[g]);
+    acc_mad_t(hi[2], lo[2], TP.shell_hi[B][g], TP.shell_lo[B][g], az[g]);
   }
+  hi[0] = hxy.x;
+  hi[1] = hxy.y;
+  lo[0] = lxy.x;
+  lo[1] = lxy.y;
   if constexpr (F::REST != 0) {
     acc_add_t(hi[0], lo[0], r[0]);
     acc_add_t(hi[1], lo[1], r[1]);
@@ -218,8 +327,8 @@ __device__ __forceinline__ void exchange_dispatch(int b, const TiledParams& TP, 
 
 // total field (meV) of the thread's spin from ring `ring`
 template <class F, int TZ, int TY>
-__device__ __forceinline__ void field_tiled(const Params& P, const TiledParams& TP, const ReplicaDev& R, int b,
-                                           const float4* ring, int xs, int own, float h[3], float s[3]) {
+__device__ __forceinline__ void field_tiled(const LocalField& L, const TiledParams& TP, int b, const float4* ring,
+                                           int xs, int own, float h[3], float s[3]) {
   using G = Geo<F, TZ, TY>;
   const float4 c = ring[(xs & 3) * G::PLANE + own + b * G::PY * G::PZ];
   s[0] = c.x;
@@ -227,7 +336,7 @@ __device__ __forceinline__ void field_tiled(const Params& P, const TiledParams& 
   s[2] = c.z;
   float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
   exchange_dispatch<F, TZ, TY>(b, TP, ring, xs, own, hi, lo);
-  local_terms(P, R, b, TP.exch_term, s, hi, lo);
+  local_terms(L, s, hi, lo);
 #pragma unroll
   for (int m = 0; m < 3; ++m) h[m] = hi[m] + lo[m];
 }
@@ -268,13 +377,17 @@ __device__ __forceinline__ int wrap_sel(int c, int L, bool per, bool& valid) {
   return w;
 }
 
+// the part of a thread's halo loads that does not change from plane to
+// plane: which (row, column, basis site) it loads and where it stores it
 template <class F, int TZ, int TY>
-__device__ __forceinline__ void fetch_plane(const View& V, const float* __restrict__ s, int64_t npad, int x,
-                                            int y0, int z0, int tid, PlaneRegs<F, TZ, TY>& pr) {
+struct FetchPlan {
+  int idx[Geo<F, TZ, TY>::PER_THREAD];   // spin index in the plane (-1: zero / unused)
+  int dst[Geo<F, TZ, TY>::PER_THREAD];   // ring slot offset
+};
+
+template <class F, int TZ, int TY>
+__device__ __forceinline__ void plan_fetch(const View& V, int y0, int z0, int tid, FetchPlan<F, TZ, TY>& fp) {
   using G = Geo<F, TZ, TY>;
-  bool xvalid = true;
-  const int gx = wrap_sel(x, V.L[0], V.per[0], xvalid);
-  const float* sx = s + V.offset;
 #pragma unroll
   for (int q = 0; q < G::PER_THREAD; ++q) {
     const int idx = tid + q * G::NT;
@@ -282,10 +395,25 @@ __device__ __forceinline__ void fetch_plane(const View& V, const float* __restri
     const int t = idx / G::NB;
     const int zz = t % G::PZ;
     const int yy = t / G::PZ;
-    bool valid = xvalid && idx < G::PLANE;
+    bool valid = idx < G::PLANE;
     const int gy = wrap_sel(y0 - F::RY + yy, V.L[1], V.per[1], valid);
     const int gz = wrap_sel(z0 - F::RZ + zz, V.L[2], V.per[2], valid);
-    const int i = gx * V.st[0] + gy * V.st[1] + gz * V.st[2] + bb;
+    fp.idx[q] = valid ? gy * V.st[1] + gz * V.st[2] + bb : -1;
+    fp.dst[q] = idx < G::PLANE ? (bb * G::PY + yy) * G::PZ + zz : -1;
+  }
+}
+
+template <class F, int TZ, int TY>
+__device__ __forceinline__ void fetch_plane(const View& V, const float* __restrict__ s, int64_t npad, int x,
+                                            const FetchPlan<F, TZ, TY>& fp, PlaneRegs<F, TZ, TY>& pr) {
+  using G = Geo<F, TZ, TY>;
+  bool xvalid = true;
+  const int gx = wrap_sel(x, V.L[0], V.per[0], xvalid);
+  const float* sx = s + V.offset + gx * V.st[0];
+#pragma unroll
+  for (int q = 0; q < G::PER_THREAD; ++q) {
+    const bool valid = xvalid && fp.idx[q] >= 0;
+    const int i = fp.idx[q];
     pr.v[q][0] = valid ? __ldg(sx + i) : 0.f;
     pr.v[q][1] = valid ? __ldg(sx + npad + i) : 0.f;
     pr.v[q][2] = valid ? __ldg(sx + 2 * npad + i) : 0.f;
@@ -293,20 +421,13 @@ __device__ __forceinline__ void fetch_plane(const View& V, const float* __restri
 }
 
 template <class F, int TZ, int TY>
-__device__ __forceinline__ void store_plane(float4* ring, int x, int tid, const PlaneRegs<F, TZ, TY>& pr) {
+__device__ __forceinline__ void store_plane(float4* ring, int x, const FetchPlan<F, TZ, TY>& fp,
+                                            const PlaneRegs<F, TZ, TY>& pr) {
   using G = Geo<F, TZ, TY>;
   float4* slot = ring + (x & 3) * G::PLANE;
 #pragma unroll
-  for (int q = 0; q < G::PER_THREAD; ++q) {
-    const int idx = tid + q * G::NT;
-    if (idx < G::PLANE) {
-      const int bb = idx % G::NB;
-      const int t = idx / G::NB;
-      const int zz = t % G::PZ;
-      const int yy = t / G::PZ;
-      slot[(bb * G::PY + yy) * G::PZ + zz] = make_float4(pr.v[q][0], pr.v[q][1], pr.v[q][2], 0.f);
-    }
-  }
+  for (int q = 0; q < G::PER_THREAD; ++q)
+    if (fp.dst[q] >= 0) slot[fp.dst[q]] = make_float4(pr.v[q][0], pr.v[q][1], pr.v[q][2], 0.f);
 }
 
 }  // namespace
@@ -315,8 +436,8 @@ __device__ __forceinline__ void store_plane(float4* ring, int x, int tid, const 
 //        1 Heun corrector recomputing rhs(s0) (rings of s0 and sp)
 //        2 Heun corrector from stored rhs0 (ring of sp; own s0 and aux)
 //        3..6 RK4 stages 1..4 (ring of sin; own s0, aux = k accumulator)
-template <class F, int TZ, int TY, int STAGE>
-__global__ void __launch_bounds__(Geo<F, TZ, TY>::NT) tiled_stage(const __grid_constant__ Params P,
+template <class F, int TZ, int TY, int STAGE, int MINB>
+__global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __grid_constant__ Params P,
                                                                   const __grid_constant__ TiledParams TP,
                                                                   const float* s0, const float* sin, float* out,
                                                                   float* aux, uint32_t kstep) {
@@ -340,17 +461,32 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT) tiled_stage(const __grid_c
   const int own = (ty + F::RY) * G::PZ + (tz + F::RZ);
   const uint64_t step = *P.step_base + kstep;
   const float* gather_src = STAGE == 0 ? s0 : sin;
+  const LocalField L = local_field(P, R, b, TP.exch_term);
+  const float dt = P.dt32;
+  const int yz = y * V.st[1] + z * V.st[2] + b;
+  // planes of this replica (outputs, stored rhs / k sum, own start state)
+  float* ox = out + V.offset;
+  float* oy = ox + P.npad;
+  float* oz = oy + P.npad;
+  float* ax = aux ? aux + V.offset : nullptr;
+  float* ay = aux ? ax + P.npad : nullptr;
+  float* az = aux ? ay + P.npad : nullptr;
+  const float* s0x = s0 + V.offset;
+  const float* s0y = s0x + P.npad;
+  const float* s0z = s0y + P.npad;
   const int xe = min(x0 + TP.TX, V.L[0]);
+  FetchPlan<F, TZ, TY> fp;
+  plan_fetch<F, TZ, TY>(V, y0, z0, tid, fp);
 
   {
     PlaneRegs<F, TZ, TY> pr;
 #pragma unroll
     for (int d = -1; d <= 1; ++d) {
-      fetch_plane<F, TZ, TY>(V, gather_src, P.npad, x0 + d, y0, z0, tid, pr);
-      store_plane<F, TZ, TY>(ring0, x0 + d, tid, pr);
+      fetch_plane<F, TZ, TY>(V, gather_src, P.npad, x0 + d, fp, pr);
+      store_plane<F, TZ, TY>(ring0, x0 + d, fp, pr);
       if (NR == 2) {
-        fetch_plane<F, TZ, TY>(V, s0, P.npad, x0 + d, y0, z0, tid, pr);
-        store_plane<F, TZ, TY>(ring1, x0 + d, tid, pr);
+        fetch_plane<F, TZ, TY>(V, s0, P.npad, x0 + d, fp, pr);
+        store_plane<F, TZ, TY>(ring1, x0 + d, fp, pr);
       }
     }
   }
@@ -360,77 +496,77 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT) tiled_stage(const __grid_c
     const bool more = x + 1 < xe;
     PlaneRegs<F, TZ, TY> pf0, pf1;
     if (more) {
-      fetch_plane<F, TZ, TY>(V, gather_src, P.npad, x + 2, y0, z0, tid, pf0);
-      if (NR == 2) fetch_plane<F, TZ, TY>(V, s0, P.npad, x + 2, y0, z0, tid, pf1);
+      fetch_plane<F, TZ, TY>(V, gather_src, P.npad, x + 2, fp, pf0);
+      if (NR == 2) fetch_plane<F, TZ, TY>(V, s0, P.npad, x + 2, fp, pf1);
     }
     if (active_yz) {
-      const int i = x * V.st[0] + y * V.st[1] + z * V.st[2] + b;  // spin index in the replica
-      const int64_t gi = V.offset + i;
+      const int i = x * V.st[0] + yz;   // spin index in the replica
       float w[3] = {0.f, 0.f, 0.f};
-      if (thermal) noise_fast(P.seed, (uint32_t)tile.x, step, (uint32_t)i, amp, w);
+      if (thermal) noise_fast(P.philox_keys, (uint32_t)tile.x, step, (uint32_t)i, amp, w);
       float h[3], s[3], k[3];
-      field_tiled<F, TZ, TY>(P, TP, R, b, ring0, x, own, h, s);
-      llg_rhs_t(P, b, s, h, w, k);
+      field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own, h, s);
+      llg_rhs_t(L, s, h, w, k);
       if (STAGE == 0) {
-        float v[3] = {__fmaf_rn(P.dt32, k[0], s[0]), __fmaf_rn(P.dt32, k[1], s[1]), __fmaf_rn(P.dt32, k[2], s[2])};
+        float v[3] = {ff(dt, k[0], s[0]), ff(dt, k[1], s[1]), ff(dt, k[2], s[2])};
         normalise_t(v);
-        out[gi] = v[0];
-        out[P.npad + gi] = v[1];
-        out[2 * P.npad + gi] = v[2];
-        if (aux) {
-          aux[gi] = k[0];
-          aux[P.npad + gi] = k[1];
-          aux[2 * P.npad + gi] = k[2];
+        ox[i] = v[0];
+        oy[i] = v[1];
+        oz[i] = v[2];
+        if (ax) {
+          ax[i] = k[0];
+          ay[i] = k[1];
+          az[i] = k[2];
         }
       } else if (STAGE == 1 || STAGE == 2) {
         float a[3], r0[3];
         if (STAGE == 1) {
           float h0[3];
-          field_tiled<F, TZ, TY>(P, TP, R, b, ring1, x, own, h0, a);
-          llg_rhs_t(P, b, a, h0, w, r0);
+          field_tiled<F, TZ, TY>(L, TP, b, ring1, x, own, h0, a);
+          llg_rhs_t(L, a, h0, w, r0);
         } else {
-          a[0] = s0[gi];
-          a[1] = s0[P.npad + gi];
-          a[2] = s0[2 * P.npad + gi];
-          r0[0] = aux[gi];
-          r0[1] = aux[P.npad + gi];
-          r0[2] = aux[2 * P.npad + gi];
+          a[0] = s0x[i];
+          a[1] = s0y[i];
+          a[2] = s0z[i];
+          r0[0] = ax[i];
+          r0[1] = ay[i];
+          r0[2] = az[i];
         }
-        const float hdt = fm(0.5f, P.dt32);
+        const float hdt = fm(0.5f, dt);
         float v[3] = {ff(hdt, fa(r0[0], k[0]), a[0]), ff(hdt, fa(r0[1], k[1]), a[1]),
                       ff(hdt, fa(r0[2], k[2]), a[2])};
         normalise_t(v);
         if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
-        out[gi] = v[0];
-        out[P.npad + gi] = v[1];
-        out[2 * P.npad + gi] = v[2];
+        ox[i] = v[0];
+        oy[i] = v[1];
+        oz[i] = v[2];
       } else {
-        const float a[3] = {s0[gi], s0[P.npad + gi], s0[2 * P.npad + gi]};
+        const float a[3] = {s0x[i], s0y[i], s0z[i]};
+        float* acc[3] = {ax, ay, az};
         float v[3];
         if (STAGE == 6) {
-          const float c = fm(P.dt32, 1.0f / 6.0f);
+          const float c = fm(dt, 1.0f / 6.0f);
 #pragma unroll
-          for (int m = 0; m < 3; ++m) v[m] = ff(c, fa(aux[m * P.npad + gi], k[m]), a[m]);
+          for (int m = 0; m < 3; ++m) v[m] = ff(c, fa(acc[m][i], k[m]), a[m]);
           normalise_t(v);
           if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
         } else {
-          const float c = STAGE == 5 ? P.dt32 : fm(0.5f, P.dt32);
+          const float c = STAGE == 5 ? dt : fm(0.5f, dt);
 #pragma unroll
           for (int m = 0; m < 3; ++m) {
-            const float acc = STAGE == 3 ? k[m] : __fmaf_rn(2.0f, k[m], aux[m * P.npad + gi]);
-            aux[m * P.npad + gi] = acc;
-            v[m] = __fmaf_rn(c, k[m], a[m]);
+            const float an = STAGE == 3 ? k[m] : ff(2.0f, k[m], acc[m][i]);
+            acc[m][i] = an;
+            v[m] = ff(c, k[m], a[m]);
           }
           if (P.rk4_normalise_stages) normalise_t(v);
         }
-        out[gi] = v[0];
-        out[P.npad + gi] = v[1];
-        out[2 * P.npad + gi] = v[2];
+        ox[i] = v[0];
+        oy[i] = v[1];
+        oz[i] = v[2];
       }
     }
     if (more) {
-      store_plane<F, TZ, TY>(ring0, x + 2, tid, pf0);
-      if (NR == 2) store_plane<F, TZ, TY>(ring1, x + 2, tid, pf1);
+      store_plane<F, TZ, TY>(ring0, x + 2, fp, pf0);
+      if (NR == 2) store_plane<F, TZ, TY>(ring1, x + 2, fp, pf1);
     }
     __syncthreads();
   }
@@ -445,34 +581,42 @@ size_t smem_bytes(int stage) {
   return (size_t)(stage == 1 ? 2 : 1) * 4 * Geo<F, TZ, TY>::PLANE * sizeof(float4);
 }
 
-template <class F, int TZ, int TY, int STAGE>
+template <class F, int TZ, int TY, int STAGE, int MINB>
 cudaError_t launch_one(unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP, const float* s0,
                        const float* sin, float* out, float* aux, uint32_t k) {
   const size_t sm = smem_bytes<F, TZ, TY>(STAGE);
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tiled_stage<F, TZ, TY, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(tiled_stage<F, TZ, TY, STAGE, MINB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     attr = true;
   }
   const dim3 block(TZ, TY * F::NB);
-  tiled_stage<F, TZ, TY, STAGE><<<grid, block, sm, st>>>(P, TP, s0, sin, out, aux, k);
+  tiled_stage<F, TZ, TY, STAGE, MINB><<<grid, block, sm, st>>>(P, TP, s0, sin, out, aux, k);
   return cudaSuccess;
 }
 
-template <class F, int TZ, int TY>
+template <class F, int TZ, int TY, int MINB>
 cudaError_t launch_family(int stage, unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP,
                           const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
   switch (stage) {
-    case 0: return launch_one<F, TZ, TY, 0>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 1: return launch_one<F, TZ, TY, 1>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 2: return launch_one<F, TZ, TY, 2>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 3: return launch_one<F, TZ, TY, 3>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 4: return launch_one<F, TZ, TY, 4>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 5: return launch_one<F, TZ, TY, 5>(grid, st, P, TP, s0, sin, out, aux, k);
-    default: return launch_one<F, TZ, TY, 6>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 0: return launch_one<F, TZ, TY, 0, MINB>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 1: return launch_one<F, TZ, TY, 1, MINB>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 2: return launch_one<F, TZ, TY, 2, MINB>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 3: return launch_one<F, TZ, TY, 3, MINB>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 4: return launch_one<F, TZ, TY, 4, MINB>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 5: return launch_one<F, TZ, TY, 5, MINB>(grid, st, P, TP, s0, sin, out, aux, k);
+    default: return launch_one<F, TZ, TY, 6, MINB>(grid, st, P, TP, s0, sin, out, aux, k);
   }
+}
+
+template <class F, int TZ, int TY>
+cudaError_t launch_occ(int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
+                       const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
+  // occupancy variant: at least 2 (up to 128 registers) or 4 (up to 64) CTAs per SM
+  if (occupancy >= 3) return launch_family<F, TZ, TY, 4>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  return launch_family<F, TZ, TY, 2>(stage, grid, st, P, TP, s0, sin, out, aux, k);
 }
 
 }  // namespace
@@ -487,13 +631,14 @@ void tiled_geometry(int family, int* tz, int* ty) {
   }
 }
 
-cudaError_t launch_tiled(int family, int stage, unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP,
-                         const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
+cudaError_t launch_tiled(int family, int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
+                         const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux,
+                         uint32_t k) {
   switch (family) {
-    case kFamSC: return launch_family<FamSC, 32, 8>(stage, grid, st, P, TP, s0, sin, out, aux, k);
-    case kFamBCC: return launch_family<FamBCC, 32, 4>(stage, grid, st, P, TP, s0, sin, out, aux, k);
-    case kFamBCC3: return launch_family<FamBCC3, 32, 4>(stage, grid, st, P, TP, s0, sin, out, aux, k);
-    case kFamTRI: return launch_family<FamTRI, 256, 1>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+    case kFamSC: return launch_occ<FamSC, 32, 8>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    case kFamBCC: return launch_occ<FamBCC, 32, 4>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    case kFamBCC3: return launch_occ<FamBCC3, 32, 4>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    case kFamTRI: return launch_occ<FamTRI, 256, 1>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
     default: return cudaErrorInvalidValue;
   }
 }

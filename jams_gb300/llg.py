@@ -273,14 +273,15 @@ class Solver:
         self._check(self.L.llg_kernel_info(self.h, info))
         fam = {0: "generic", 1: "sc", 2: "bcc", 3: "bcc3", 4: "triangular"}[info[0]]
         return {"family": fam, "planes_per_cta": info[1], "store_rhs": bool(info[2]), "tile_z": info[3],
-                "tile_y": info[4], "fp64": bool(info[5])}
+                "tile_y": info[4], "fp64": bool(info[5]), "occupancy": info[6]}
 
     def autotune(self, trial_steps: int = 20, use_cache: bool = False) -> dict:
         self._check(self.L.llg_autotune(self.h, int(trial_steps), int(bool(use_cache))))
         return self.kernel_info()
 
-    def set_tuning(self, planes_per_cta: int, store_rhs: bool) -> None:
-        self._check(self.L.llg_set_tuning(self.h, int(planes_per_cta), int(bool(store_rhs))))
+    def set_tuning(self, planes_per_cta: int, store_rhs: bool, occupancy: int = 2) -> None:
+        flags = int(bool(store_rhs)) | (int(occupancy) << 4)
+        self._check(self.L.llg_set_tuning(self.h, int(planes_per_cta), flags))
 
     @property
     def last_launch_count(self) -> int:
