@@ -124,6 +124,28 @@ typedef struct llg_handle llg_handle;
    src/jams/core/hamiltonian.cc:80-115).  Spins start at +z. */
 int llg_create(const llg_desc *desc, llg_handle **out);
 
+/* Creates a solver from the text of a JAMS config file and an optional patch
+   string merged over it (src/jams/core/jams++.cc:48-84,
+   src/jams/interface/config.cc:15-167): materials, unitcell, lattice,
+   hamiltonians (exchange with inline interactions and symmetry operations,
+   uniaxial, cubic, applied-field, zeeman dc field), solver (llg-heun-gpu,
+   llg-rk4-gpu; t_step, t_max in seconds; gilbert_prefactor), physics
+   (temperature), sim (seed).  Initial spins from the materials' spin
+   settings ("random": uniform directions drawn from sim.seed). */
+int llg_create_from_config(const char *config_text, const char *patch_text,
+                           int32_t precision, int32_t device, llg_handle **out);
+
+/* The model a config file describes, as JSON (lattice, per-basis-site
+   parameters, every term with its interaction template), without touching
+   a GPU; for checking a config.  LLG_ERR_BAD_DESC when the config is invalid
+   or json_len is too small (the message gives the size needed). */
+int llg_config_describe(const char *config_text, const char *patch_text,
+                        char *json, int64_t json_len);
+
+/* int(t_max / t_step) of the solver section a handle was created from
+   (src/jams/solvers/cuda_llg_heun.cu:23-29); -1 for llg_create handles. */
+int64_t llg_max_steps(const llg_handle *h);
+
 void llg_destroy(llg_handle *h);
 
 /* message of the last failure on h (thread-local when h is NULL) */

@@ -33,6 +33,10 @@
 
 using namespace jams_llg;
 
+namespace jams_llg {
+void set_max_steps(llg_handle* h, int64_t max_steps);
+}
+
 namespace {
 thread_local std::string g_tls_error;
 }
@@ -128,6 +132,7 @@ struct llg_handle {
   std::map<GraphKey, cudaGraphExec_t> graphs;
   int64_t last_launches = 0;
   bool params_dirty = false;
+  int64_t max_steps = -1;    // from a config file's solver section
   // tiled FP32 path (lattice matched a stencil family)
   int family = kFamNone;
   bool tiled = false;
@@ -1115,6 +1120,14 @@ int llg_set_stream(llg_handle* h, void* cuda_stream) {
 }
 
 int64_t llg_last_launch_count(const llg_handle* h) { return h ? h->last_launches : -1; }
+
+int64_t llg_max_steps(const llg_handle* h) { return h ? h->max_steps : -1; }
+
+}  // extern "C"
+
+void jams_llg::set_max_steps(llg_handle* h, int64_t max_steps) { h->max_steps = max_steps; }
+
+extern "C" {
 
 int llg_kernel_info(const llg_handle* h, int32_t* info) {
   if (!h || !info) return tls_fail(LLG_ERR_BAD_DESC, "null argument");

@@ -34,6 +34,7 @@ EXPORTED = [
     "llg_synchronize", "llg_iteration", "llg_set_iteration", "llg_set_temperature", "llg_set_field",
     "llg_fields", "llg_observables", "llg_topological_charge", "llg_set_stream", "llg_last_launch_count",
     "llg_profile_stages", "llg_kernel_info", "llg_set_tuning", "llg_autotune", "llg_magnetisation_noalloc",
+    "llg_create_from_config", "llg_config_describe", "llg_max_steps",
 ]
 
 
@@ -110,6 +111,10 @@ def lib():
         L.llg_set_tuning.argtypes = [vp, i32, i32]
         L.llg_autotune.argtypes = [vp, i32, i32]
         L.llg_magnetisation_noalloc.argtypes = [vp, i64, i32, dp, vp, vp]
+        L.llg_create_from_config.argtypes = [ctypes.c_char_p, ctypes.c_char_p, i32, i32, ctypes.POINTER(vp)]
+        L.llg_config_describe.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, i64]
+        L.llg_max_steps.argtypes = [vp]
+        L.llg_max_steps.restype = i64
         _lib = L
     return _lib
 
@@ -120,6 +125,24 @@ def _dp(a):
 
 def _ip(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def describe_config(text: str, patch: str = "") -> dict:
+    """The model a JAMS config file describes (no GPU needed)."""
+    import json
+
+    L = lib()
+    n = 1 << 22
+    while True:
+        buf = ctypes.create_string_buffer(n)
+        rc = L.llg_config_describe(text.encode(), patch.encode(), buf, n)
+        if rc == 0:
+            return json.loads(buf.value.decode())
+        msg = L.llg_last_error(None).decode()
+        if "buffer too small" in msg and n < (1 << 30):
+            n *= 4
+            continue
+        raise LLGError(rc, msg)
 
 
 class Solver:
@@ -189,6 +212,28 @@ class Solver:
         self.precision = precision
         self.n_terms = len(m.terms)
         self.n_replicas = len(workload.replicas)
+
+    @classmethod
+    def from_config(cls, text: str, patch: str = "", precision: int = FP32C, device: int = 0) -> "Solver":
+        """A solver built from the text of a JAMS config file (and patch)."""
+        self = cls.__new__(cls)
+        self.L = lib()
+        h = ctypes.c_void_p()
+        rc = self.L.llg_create_from_config(text.encode(), patch.encode(), int(precision), int(device), ctypes.byref(h))
+        if rc != 0:
+            raise LLGError(rc, self.L.llg_last_error(None).decode())
+        self.h = h
+        d = describe_config(text, patch)
+        self.workload = None
+        self.precision = precision
+        self.n_terms = len(d["terms"])
+        self.n_replicas = 1
+        self._integrator = d["integrator"]
+        return self
+
+    @property
+    def max_steps(self) -> int:
+        return int(self.L.llg_max_steps(self.h))
 
     def close(self):
         if getattr(self, "h", None):
@@ -266,7 +311,8 @@ class Solver:
         """Mean duration (ms) of each stage kernel over nsteps steps."""
         ms = np.zeros(4)
         self._check(self.L.llg_profile_stages(self.h, int(nsteps), _dp(ms)))
-        return ms[: 2 if self.workload.model.integrator == W.HEUN else 4]
+        integ = self.workload.model.integrator if self.workload is not None else self._integrator
+        return ms[: 2 if integ == W.HEUN else 4]
 
     def kernel_info(self) -> dict:
         info = (ctypes.c_int32 * 8)()

@@ -1,0 +1,117 @@
+"""CPU tests of the config-file front end (llg_config_describe): the model a
+JAMS config describes equals the workload builders' model; parser, patch
+merge, units and error reporting."""
+import numpy as np
+import pytest
+
+from jams_gb300 import configs as C
+from jams_gb300 import workloads as W
+
+
+def template_set(term):
+    out = set()
+    for e in range(len(term["bi"])):
+        J = tuple(round(v, 12) for v in term["J"][9 * e: 9 * e + 9])
+        out.add((int(term["bi"][e]), int(term["bj"][e]), tuple(int(v) for v in term["T"][3 * e: 3 * e + 3]), J))
+    return out
+
+
+def workload_set(t):
+    return {(int(t.bi[e]), int(t.bj[e]), tuple(int(v) for v in t.T[e]),
+             tuple(round(v, 12) for v in np.asarray(t.J[e]).reshape(-1))) for e in range(len(t.bi))}
+
+
+def check_model(d, w):
+    m = w.model
+    assert d["nb"] == m.nb
+    assert d["L"] == list(w.replicas[0].L)
+    np.testing.assert_array_equal(d["mus"], m.mus)
+    np.testing.assert_array_equal(d["gyro"], m.gyro)
+    np.testing.assert_array_equal(d["alpha"], m.alpha)
+    assert d["dt"] == m.dt
+    assert d["integrator"] == m.integrator
+    assert len(d["terms"]) == len(m.terms)
+    for td, tw in zip(d["terms"], m.terms):
+        assert td["kind"] == tw.kind
+        if tw.kind == W.TERM_EXCHANGE:
+            assert template_set(td) == workload_set(tw)
+        elif tw.kind in (W.TERM_UNIAXIAL, W.TERM_CUBIC):
+            assert td["order"] == tw.order
+            np.testing.assert_allclose(td["K"], tw.K, rtol=1e-15)
+            np.testing.assert_allclose(td["axis"], np.asarray(tw.axis).reshape(-1), atol=1e-15)
+
+
+def test_sc_config_matches_workload(llg):
+    d = llg.describe_config(C.sc_ferromagnet(L=32))
+    check_model(d, W.sc_ferromagnet(L=32))
+    assert d["max_steps"] == 1000
+    assert d["terms"][2]["B"] == [0.0, 0.0, 1.0]
+
+
+def test_bcc_symmetry_expansion_gives_26_neighbours(llg):
+    """One interaction vector per shell expands by the site point group to
+    8 + 6 + 12 neighbours per basis site, as spglib's operations do."""
+    d = llg.describe_config(C.bcc_three_shell(L=8))
+    w = W.bcc_three_shell(L=8)
+    check_model(d, w)
+    ex = d["terms"][0]
+    assert len(ex["bi"]) == 52
+    assert d["max_steps"] == 20000
+
+
+def test_triangular_tensor_config(llg):
+    d = llg.describe_config(C.triangular_dmi(L=16))
+    w = W.triangular_dmi_field_sweep(L=16, n_fields=1)
+    check_model(d, w)
+    assert d["periodic"] == [1, 1, 0]
+
+
+def test_patch_merges_over_config(llg):
+    base = C.sc_ferromagnet(L=8)
+    d = llg.describe_config(base, 'physics : { temperature = 100.0; }; lattice : { size = [4, 5, 6]; };')
+    assert d["temperature"] == 100.0
+    assert d["L"] == [4, 5, 6]
+    d = llg.describe_config(base, 'hamiltonians = ( { interactions = ( ("A", "A", [1.0, 0.0, 0.0], 2.5) ); } );')
+    assert set(round(v, 9) for v in d["terms"][0]["J"] if v != 0.0) == {2.5}
+
+
+def test_energy_units_joules_default(llg):
+    """Without energy_units the reference reads joules (kJoule2meV)."""
+    cfg = C.sc_ferromagnet(L=4).replace('{ module = "exchange"; energy_units = "meV";', '{ module = "exchange";')
+    cfg = cfg.replace("], 1.0) ); },", "], 1.602176634e-22) ); },")
+    d = llg.describe_config(cfg)
+    J = [v for v in d["terms"][0]["J"] if v != 0.0]
+    np.testing.assert_allclose(J, 1.602176634e-22 * 6.24150907e21, rtol=1e-15)
+
+
+def test_parser_comments_and_syntax(llg):
+    cfg = C.sc_ferromagnet(L=4)
+    cfg = "/* block\n comment */\n# hash comment\n" + cfg.replace("lattice : {", "lattice = { // trailing\n")
+    d = llg.describe_config(cfg)
+    assert d["L"] == [4, 4, 4]
+
+
+@pytest.mark.parametrize("bad,msg", [
+    ("lattice : { size = [4, 4, 4] ", "missing '}'"),
+    ('hamiltonians = ( { module = "dipole-fft"; } );', "not on the LLG hot path"),
+    ('solver : { module = "monte-carlo-metropolis-cpu"; t_step = 1e-15; t_max = 1e-12; };', "unknown solver"),
+])
+def test_config_errors_are_reported(llg, bad, msg):
+    cfg = C.sc_ferromagnet(L=4)
+    if bad.startswith("lattice"):
+        cfg = cfg.replace("lattice : { size = [4, 4, 4]; periodic = [true, true, true]; };", bad)
+    elif bad.startswith("hamiltonians"):
+        cfg = cfg[: cfg.index("hamiltonians")] + bad + cfg[cfg.index("solver"):]
+    else:
+        cfg = cfg[: cfg.index("solver")] + bad + cfg[cfg.index("physics"):]
+    with pytest.raises(llg.LLGError, match=msg):
+        llg.describe_config(cfg)
+
+
+def test_duplicate_site_pair_is_rejected_at_create(llg):
+    """Reaching the same site twice is an error in the reference
+    (interactions.cc:371-380); it is raised by llg_create before any device
+    work, so this runs without a GPU."""
+    w = W.sc_ferromagnet(L=(2, 4, 4))
+    with pytest.raises(llg.LLGError, match="Multiple interactions"):
+        llg.Solver(w, precision=llg.FP64)
