@@ -598,7 +598,12 @@ int build(llg_handle* h, const llg_desc* d) {
     R.vper[1] = d->periodic[1];
     R.vper[2] = d->periodic[2];
   }
-  if (!h->fp64 && ex.size() == 1) {
+  int n_uni = 0, n_cub = 0;
+  for (int t = 0; t < d->n_terms; ++t) {
+    n_uni += d->terms[t].kind == LLG_TERM_UNIAXIAL;
+    n_cub += d->terms[t].kind == LLG_TERM_CUBIC;
+  }
+  if (!h->fp64 && ex.size() == 1 && n_uni <= 1 && n_cub <= 1) {
     const llg_term& T = d->terms[ex[0].term];
     h->family = find_family(d, T, h->TP);
     if (h->family != kFamNone) {

@@ -128,7 +128,8 @@ __device__ __forceinline__ void noise_fast(const uint32_t* keys, uint32_t replic
 // Anisotropy and applied-field terms of one basis site, gathered once per
 // CTA into registers (at most one uniaxial, one cubic and one applied-field
 // term; the host sends other term lists to the gather kernels).  They are
-// summed in plain FP32 and added to the compensated exchange sum once.
+// summed in plain FP32 and added to the low word of the compensated
+// exchange sum.
 struct LocalField {
   float uk;       // K * p of the uniaxial term (0: none)
   int upow;
@@ -204,8 +205,10 @@ __device__ __forceinline__ void local_terms(const LocalField& L, const float s[3
 #pragma unroll
     for (int m = 0; m < 3; ++m) l[m] = ff(L.ck, ff(u[6 + m], cw, ff(u[3 + m], cv, fm(u[m], cu))), l[m]);
   }
+  // these terms are small next to the exchange field: added to the low
+  // word, their rounding stays at their own magnitude
 #pragma unroll
-  for (int m = 0; m < 3; ++m) acc_add_t(hi[m], lo[m], l[m]);
+  for (int m = 0; m < 3; ++m) lo[m] = fa(lo[m], l[m]);
 }
 
 __device__ __forceinline__ void llg_rhs_t(const LocalField& L, const float s[3], const float h[3], const float w[3],
@@ -298,9 +301,22 @@ __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const floa
     az[g] = 0.f;
   }
   gather_all<F, TZ, TY, B>(std::make_integer_sequence<int, F::Z>{}, bm, b0, bp, axy, az, r, TP);
-  float2 hxy = make_float2(hi[0], hi[1]), lxy = make_float2(lo[0], lo[1]);
+  // first shell: (hi, lo) is the exact product J a (TwoProd) plus the J
+  // low word, no TwoSum needed; the other shells are added with TwoSum
+  float2 hxy, lxy;
+  {
+    const float2 J = make_float2(TP.shell_hi[B][0], TP.shell_hi[B][0]);
+    const float2 JN = make_float2(-TP.shell_hi[B][0], -TP.shell_hi[B][0]);
+    const float2 JL = make_float2(TP.shell_lo[B][0], TP.shell_lo[B][0]);
+    const float2 pn = mul2(JN, axy[0]);
+    hxy = make_float2(-pn.x, -pn.y);
+    lxy = fma2(JL, axy[0], fma2(J, axy[0], pn));
+    const float p = fm(TP.shell_hi[B][0], az[0]);
+    hi[2] = p;
+    lo[2] = ff(TP.shell_lo[B][0], az[0], ff(TP.shell_hi[B][0], az[0], -p));
+  }
 #pragma unroll
-  for (int g = 0; g < F::NSHELL; ++g) {
+  for (int g = 1; g < F::NSHELL; ++g) {
     acc_mad2(hxy, lxy, TP.shell_hi[B][g], -TP.shell_hi[B][g], TP.shell_lo[B][g], axy[g]);
     acc_mad_t(hi[2], lo[2], TP.shell_hi[B][g], TP.shell_lo[B][g], az[g]);
   }
@@ -334,7 +350,7 @@ __device__ __forceinline__ void field_tiled(const LocalField& L, const TiledPara
   s[0] = c.x;
   s[1] = c.y;
   s[2] = c.z;
-  float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
+  float hi[3], lo[3];
   exchange_dispatch<F, TZ, TY>(b, TP, ring, xs, own, hi, lo);
   local_terms(L, s, hi, lo);
 #pragma unroll
