@@ -216,11 +216,12 @@ int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
 int llg_kernel_info(const llg_handle *h, int32_t *info);
 
 /* Tiling choice of the tiled FP32 kernels (no effect on other kernels):
-   planes streamed per CTA; flags bit 0: the Heun predictor stores rhs(s0);
+   planes streamed per CTA (rounded up to even: a thread computes two
+   consecutive planes per iteration); flags bit 0: the Heun predictor stores rhs(s0);
    flags >> 4: occupancy variant, 2 (<= 128 registers) or 4 (<= 64). */
 int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t flags);
 
-/* Times every tiling candidate (planes per CTA 1..64, stored or recomputed
+/* Times every tiling candidate (planes per CTA 2..64, stored or recomputed
    rhs) for trial_steps steps on a copy of the state and keeps the fastest;
    the state and iteration are restored.  With use_cache the choice is read
    from / appended to the file named by $JAMS_LLG_TUNE_CACHE (default

@@ -622,7 +622,7 @@ int build(llg_handle* h, const llg_desc* d) {
       }
       int maxL = 1;
       for (auto& R : h->reps) maxL = std::max(maxL, R.vL[0]);
-      h->TP.TX = std::min(8, maxL);
+      h->TP.TX = std::min(8, maxL + (maxL & 1));
     }
   }
   h->npad = std::max<int64_t>(offset, 64);
@@ -1200,6 +1200,9 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
   if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
   if (!h->tiled) return 0;
   if (planes_per_cta < 1) return h->fail(LLG_ERR_BAD_DESC, "planes_per_cta must be >= 1");
+  // each thread computes two consecutive planes, the pair starting at an even
+  // x (the pair shares one noise counter): the count is rounded up to even
+  planes_per_cta += planes_per_cta & 1;
   cudaSetDevice(h->device);
   cudaError_t ce = cudaStreamSynchronize(h->stream);
   if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamSynchronize");
@@ -1275,8 +1278,8 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   int maxL = 1;
   for (auto& R : h->reps) maxL = std::max(maxL, R.vL[0]);
   std::vector<std::pair<int, int>> cands;   // (planes per CTA, store flag | occupancy << 4)
-  for (int t : {1, 2, 4, 8, 16, 32, 64})
-    if (t <= std::max(1, maxL))
+  for (int t : {2, 4, 8, 16, 32, 64})
+    if (t <= std::max(2, maxL))
       for (int occ : {2, 4}) {
         cands.push_back({t, occ << 4});
         if (h->integrator == LLG_HEUN) cands.push_back({t, 1 | (occ << 4)});

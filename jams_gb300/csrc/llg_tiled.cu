@@ -105,25 +105,36 @@ __device__ __forceinline__ void acc_mad_t(float& hi, float& lo, float jhi, float
   lo = __fadd_rn(lo, __fadd_rn(e, __fmaf_rn(jlo, a, pe)));
 }
 
-// thermal field for the FP32 form: Philox4x32-10 words, Box-Muller with the
-// special-function unit (log2, sin, cos, rsqrt)
-__device__ __forceinline__ void noise_fast(const uint32_t* keys, uint32_t replica, uint64_t step, uint32_t spin,
-                                           float amp, float w[3]) {
-  uint32_t c[4] = {spin, replica, (uint32_t)step, (uint32_t)(step >> 32)};
-  philox4x32_10_keyed(c, keys);
-  const float u1 = (float)((c[0] >> 8) + 1u) * 0x1.0p-24f;
-  const float u2 = (float)((c[2] >> 8) + 1u) * 0x1.0p-24f;
-  const float x1 = fmaxf(-1.3862943611198906f * __log2f(u1), 1e-30f);  // -2 ln u1
-  const float x2 = fmaxf(-1.3862943611198906f * __log2f(u2), 1e-30f);
-  const float r1 = x1 * rsqrtf(x1), r2 = x2 * rsqrtf(x2);
-  float s1, c1, s2, c2;
-  __sincosf(6.283185307179586f * (float)(c[1] >> 8) * 0x1.0p-24f, &s1, &c1);
-  __sincosf(6.283185307179586f * (float)(c[3] >> 8) * 0x1.0p-24f, &s2, &c2);
-  w[0] = __fmul_rn(__fmul_rn(amp, r1), c1);
-  w[1] = __fmul_rn(__fmul_rn(amp, r1), s1);
-  w[2] = __fmul_rn(__fmul_rn(amp, r2), c2);
+// thermal field for the FP32 form, Box-Muller with the special-function
+// unit (log2, sin, cos, rsqrt): two spins (planes x and x + 1 of one column,
+// x even) from one Philox4x32-10 call keyed by the even spin's index; six
+// 21-bit uniforms (the four words' top 21 bits, and their low bits
+// recombined) make three Box-Muller pairs.  The largest normal is
+// sqrt(-2 ln 2^-21) = 5.4.
+__device__ __forceinline__ float bm_radius(uint32_t k) {
+  const float u = (float)(k + 1u) * 0x1.0p-21f;  // (0, 1]
+  const float x = fmaxf(-1.3862943611198906f * __log2f(u), 1e-30f);  // -2 ln u
+  return x * rsqrtf(x);
 }
 
+__device__ __forceinline__ void noise_pair(const uint32_t* keys, uint32_t replica, uint64_t step, uint32_t spin,
+                                           float amp, float wa[3], float wb[3]) {
+  uint32_t c[4] = {spin, replica, (uint32_t)step, (uint32_t)(step >> 32)};
+  philox4x32_10_keyed(c, keys);
+  const uint32_t k4 = ((c[0] & 0x7FFu) << 10) | (c[1] & 0x3FFu);
+  const uint32_t k5 = ((c[2] & 0x7FFu) << 10) | (c[3] & 0x3FFu);
+  const float r0 = fm(amp, bm_radius(c[0] >> 11)), r1 = fm(amp, bm_radius(c[2] >> 11)), r2 = fm(amp, bm_radius(k4));
+  float s0, c0, s1, c1, s2, c2;
+  __sincosf(6.283185307179586f * (float)(c[1] >> 11) * 0x1.0p-21f, &s0, &c0);
+  __sincosf(6.283185307179586f * (float)(c[3] >> 11) * 0x1.0p-21f, &s1, &c1);
+  __sincosf(6.283185307179586f * (float)k5 * 0x1.0p-21f, &s2, &c2);
+  wa[0] = fm(r0, c0);
+  wa[1] = fm(r0, s0);
+  wa[2] = fm(r1, c1);
+  wb[0] = fm(r1, s1);
+  wb[1] = fm(r2, c2);
+  wb[2] = fm(r2, s2);
+}
 
 // Anisotropy and applied-field terms of one basis site, gathered once per
 // CTA into registers (at most one uniaxial, one cubic and one applied-field
@@ -508,6 +519,9 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
   }
   __syncthreads();
 
+  // noise of plane x + 1, drawn with plane x's when x is even (the host keeps
+  // planes per CTA even, so x0 is even)
+  float wn[3] = {0.f, 0.f, 0.f};
   for (int x = x0; x < xe; ++x) {
     const bool more = x + 1 < xe;
     PlaneRegs<F, TZ, TY> pf0, pf1;
@@ -517,8 +531,8 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
     }
     if (active_yz) {
       const int i = x * V.st[0] + yz;   // spin index in the replica
-      float w[3] = {0.f, 0.f, 0.f};
-      if (thermal) noise_fast(P.philox_keys, (uint32_t)tile.x, step, (uint32_t)i, amp, w);
+      float w[3] = {wn[0], wn[1], wn[2]};
+      if (thermal && (x & 1) == 0) noise_pair(P.philox_keys, (uint32_t)tile.x, step, (uint32_t)i, amp, w, wn);
       float h[3], s[3], k[3];
       field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own, h, s);
       llg_rhs_t(L, s, h, w, k);

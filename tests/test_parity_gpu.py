@@ -255,7 +255,8 @@ def test_fp32c_gather_kernels_within_bound(llg, oracle):
 @pytest.mark.parametrize("name", ["bcc3", "sc", "tri"])
 def test_tiling_choices_give_identical_results(llg, name):
     """Planes per CTA and stored vs recomputed rhs(s0) change the schedule,
-    not the arithmetic: states are bit-identical."""
+    not the arithmetic: states are bit-identical.  Odd plane counts are
+    rounded up to even (a thread computes two planes)."""
     w = {"bcc3": W.bcc_three_shell(L=10, T=300.0, start="random"),
          "sc": W.sc_ferromagnet(L=(9, 12, 40), T=100.0),
          "tri": W.triangular_dmi_field_sweep(L=(20, 300, 1), n_fields=2, T=5.0)}[name]
