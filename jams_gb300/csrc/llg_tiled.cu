@@ -533,6 +533,19 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
       const int i = x * V.st[0] + yz;   // spin index in the replica
       float w[3] = {wn[0], wn[1], wn[2]};
       if (thermal && (x & 1) == 0) noise_pair(P.philox_keys, (uint32_t)tile.x, step, (uint32_t)i, amp, w, wn);
+      // the spin's own start-of-step state and stored rhs / k sum: loaded
+      // before the exchange sum so that the sum covers their latency
+      float own_s0[3] = {0.f, 0.f, 0.f}, own_r[3] = {0.f, 0.f, 0.f};
+      if (STAGE >= 2) {
+        own_s0[0] = __ldg(s0x + i);
+        own_s0[1] = __ldg(s0y + i);
+        own_s0[2] = __ldg(s0z + i);
+      }
+      if (STAGE == 2 || STAGE >= 4) {
+        own_r[0] = ax[i];
+        own_r[1] = ay[i];
+        own_r[2] = az[i];
+      }
       float h[3], s[3], k[3];
       field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own, h, s);
       llg_rhs_t(L, s, h, w, k);
@@ -554,12 +567,11 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
           field_tiled<F, TZ, TY>(L, TP, b, ring1, x, own, h0, a);
           llg_rhs_t(L, a, h0, w, r0);
         } else {
-          a[0] = s0x[i];
-          a[1] = s0y[i];
-          a[2] = s0z[i];
-          r0[0] = ax[i];
-          r0[1] = ay[i];
-          r0[2] = az[i];
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            a[m] = own_s0[m];
+            r0[m] = own_r[m];
+          }
         }
         const float hdt = fm(0.5f, dt);
         float v[3] = {ff(hdt, fa(r0[0], k[0]), a[0]), ff(hdt, fa(r0[1], k[1]), a[1]),
@@ -570,20 +582,20 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
         oy[i] = v[1];
         oz[i] = v[2];
       } else {
-        const float a[3] = {s0x[i], s0y[i], s0z[i]};
+        const float* a = own_s0;
         float* acc[3] = {ax, ay, az};
         float v[3];
         if (STAGE == 6) {
           const float c = fm(dt, 1.0f / 6.0f);
 #pragma unroll
-          for (int m = 0; m < 3; ++m) v[m] = ff(c, fa(acc[m][i], k[m]), a[m]);
+          for (int m = 0; m < 3; ++m) v[m] = ff(c, fa(own_r[m], k[m]), a[m]);
           normalise_t(v);
           if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
         } else {
           const float c = STAGE == 5 ? dt : fm(0.5f, dt);
 #pragma unroll
           for (int m = 0; m < 3; ++m) {
-            const float an = STAGE == 3 ? k[m] : ff(2.0f, k[m], acc[m][i]);
+            const float an = STAGE == 3 ? k[m] : ff(2.0f, k[m], own_r[m]);
             acc[m][i] = an;
             v[m] = ff(c, k[m], a[m]);
           }
