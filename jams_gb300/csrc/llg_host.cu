@@ -137,7 +137,7 @@ struct llg_handle {
   int family = kFamNone;
   bool tiled = false;
   bool store_mode = false;   // Heun: predictor stores rhs(s0) instead of the corrector recomputing it
-  int occupancy = 2;         // tiled kernels compiled for >= 2 or >= 4 CTAs per SM
+  int occupancy = 2;         // tiled kernels compiled for >= 2, 3 or 4 CTAs per SM
   int tz = 0, ty = 0;
   TiledParams TP{};
   DevBuf<int4> d_tiles4;
@@ -966,7 +966,7 @@ int llg_step(llg_handle* h, int32_t nsteps) {
   if (alternates && (K & 1)) K += 1;  // graphs must return the state to the buffer they found it in
   int remaining = nsteps;
   while (remaining >= K && K > 1) {
-    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 32 * h->TP.TX, K};
+    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX, K};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
       cudaGraph_t g;
@@ -1208,7 +1208,8 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
   if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamSynchronize");
   drop_graphs(h);
   h->store_mode = (store_rhs & 1) != 0 && h->integrator == LLG_HEUN;
-  h->occupancy = (store_rhs >> 4) >= 3 ? 4 : 2;
+  const int occ = store_rhs >> 4;
+  h->occupancy = occ >= 4 ? 4 : (occ == 3 ? 3 : 2);
   if (planes_per_cta != h->TP.TX) {
     h->TP.TX = planes_per_cta;
     int rc = build_tiles4(h);
@@ -1280,7 +1281,7 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   std::vector<std::pair<int, int>> cands;   // (planes per CTA, store flag | occupancy << 4)
   for (int t : {2, 4, 8, 16, 32, 64})
     if (t <= std::max(2, maxL))
-      for (int occ : {2, 4}) {
+      for (int occ : {2, 3, 4}) {
         cands.push_back({t, occ << 4});
         if (h->integrator == LLG_HEUN) cands.push_back({t, 1 | (occ << 4)});
       }

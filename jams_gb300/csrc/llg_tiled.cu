@@ -656,8 +656,10 @@ cudaError_t launch_family(int stage, unsigned grid, cudaStream_t st, const Param
 template <class F, int TZ, int TY>
 cudaError_t launch_occ(int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
                        const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
-  // occupancy variant: at least 2 (up to 128 registers) or 4 (up to 64) CTAs per SM
-  if (occupancy >= 3) return launch_family<F, TZ, TY, 4>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  // occupancy variant: at least 2 (up to 128 registers), 3 (up to 80) or 4
+  // (up to 64) CTAs per SM
+  if (occupancy >= 4) return launch_family<F, TZ, TY, 4>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  if (occupancy == 3) return launch_family<F, TZ, TY, 3>(stage, grid, st, P, TP, s0, sin, out, aux, k);
   return launch_family<F, TZ, TY, 2>(stage, grid, st, P, TP, s0, sin, out, aux, k);
 }
 

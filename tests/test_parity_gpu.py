@@ -263,7 +263,7 @@ def test_tiling_choices_give_identical_results(llg, name):
     if name == "tri":
         w.model.integrator = W.HEUN
     outs = []
-    for tx, store, occ in [(1, False, 2), (1, True, 4), (3, False, 4), (8, True, 2), (64, False, 2)]:
+    for tx, store, occ in [(1, False, 2), (1, True, 4), (3, False, 4), (4, True, 3), (8, True, 2), (64, False, 2)]:
         s = solver(llg, w, llg.FP32C, steps_per_graph=4)
         s.set_tuning(tx, store, occ)
         for r in range(len(w.replicas)):
