@@ -10,7 +10,8 @@ four stages) over every spin of the workload.  Default workload: bcc,
 to the third shell, cubic anisotropy, T = 300 K thermal field, Heun,
 FP32 spins with compensated neighbour sums (the benchmark's FP32 form).
 
-Timing: W untimed steps, then K timed steps, each bracketed by CUDA events
+Timing: W untimed steps, then K timed steps (K defaults to the workload's
+own run length: 20,000 steps for the default), each bracketed by CUDA events
 on the solver's stream with an L2 flush (a 256 MiB write) between steps, a
 barrier + synchronize on both sides, max over ranks.  value = spins x K /
 sum of step times.  e2e: the same steps through the C ABI with the FP64
@@ -20,6 +21,10 @@ mean CUDA-event duration, against the measured HBM copy bandwidth.
 cpu_baseline / --impl reference: the oracle's restatement of the
 reference's CPU Heun path (CSR SpMV, per-term field arrays, serial noise
 draw as the reference does) on all host cores.
+
+Several GPUs (torchrun, one process per GPU): replicas only.  Each rank
+integrates its own independent copy of the workload (seed offset by the
+rank); value = all ranks' spin-steps / the slowest rank's time.
 """
 from __future__ import annotations
 
@@ -65,13 +70,33 @@ WORKLOADS = {
     "sc_sweep256": lambda: W.sc_temperature_sweep(),
     # triangular 2048^2 x 16 fields, tensor exchange + DMI, RK4, 5 K
     "tri2048_dmi_x16": lambda: W.triangular_dmi_field_sweep(),
+    # profiling cases: state larger than L2 (129 MB) but a few GB on the device
+    "bcc192_nn": lambda: W.bcc_nearest_neighbour(L=192, T=500.0),
+    "bcc192_3shell": lambda: W.bcc_three_shell(L=192, T=500.0),
+    "tri2048_dmi_x4": lambda: W.triangular_dmi_field_sweep(n_fields=4),
 }
 
 
-def parse():
+def kernel_name(info: dict, integ: str, stage: int, precision: str) -> str:
+    """Name of the kernel that runs stage `stage` of a step, as ncu prints it."""
+    if info.get("family", "generic") != "generic" and precision == "fp32c":
+        fam = {"sc": "FamSC", "bcc": "FamBCC", "bcc3": "FamBCC3", "triangular": "FamTRI"}[info["family"]]
+        if integ == "heun":
+            st = 0 if stage == 0 else (2 if info["store_rhs"] else 1)
+        else:
+            st = 3 + stage
+        return "tiled_stage<%s, %d, %d, %d, %d>" % (fam, info["tile_z"], info["tile_y"], st, info["occupancy"])
+    suffix = "_f32" if precision == "fp32c" else "_f64"
+    if integ == "heun":
+        return ("heun_predict" if stage == 0 else "heun_correct") + suffix
+    return "rk4_stage%s<%d>" % (suffix, stage + 1)
+
+
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=2000)
+    p.add_argument("--steps", type=int, default=None,
+                   help="timed steps (default: the workload's own run length, e.g. 20000 for bcc64_3shell)")
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--workload", default="bcc64_3shell", choices=sorted(WORKLOADS))
     p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
@@ -81,7 +106,7 @@ def parse():
     p.add_argument("--profile-steps", type=int, default=50)
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--tuning", default="", help="planes_per_cta,store_rhs,occupancy instead of autotuning")
-    return p.parse_args()
+    return p.parse_args(argv)
 
 
 def dist_env():
@@ -109,6 +134,49 @@ def barrier(world: int):
         dist.barrier()
 
 
+def init_ranks(world: int, local: int, backend: str = "nccl"):
+    """One process per GPU (replicas only: no collective on the data path;
+    the process group carries the barrier, the max of the timings and the
+    end-of-run scalars)."""
+    if world <= 1:
+        return
+    import torch
+    import torch.distributed as dist
+
+    if backend == "nccl":
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        dist.init_process_group(backend)
+
+
+def rank_workload(name: str, rank: int):
+    """The workload of one rank: the named configuration with the seed offset
+    by the rank, so every rank integrates its own independent replicas
+    (distinct noise streams and starts) of the same size: weak scaling."""
+    w = WORKLOADS[name]()
+    w.seed = w.seed + rank
+    return w
+
+
+def job_rate(spins_per_rank: int, world: int, steps: int, seconds: float) -> float:
+    """Whole-job spin-steps/s: every rank's spins over the slowest rank's time."""
+    return world * spins_per_rank * steps / seconds
+
+
+def gather_scalars(values, world: int, device=None):
+    """Per-rank scalar lists (e.g. |M| of every replica) gathered on every
+    rank, in rank order."""
+    if world <= 1:
+        return [list(values)]
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    out = [torch.empty_like(t) for _ in range(world)]
+    dist.all_gather(out, t)
+    return [o.cpu().tolist() for o in out]
+
+
 # ------------------------------------------------------------------ clocks --
 
 class ClockSampler:
@@ -127,7 +195,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except OSError:
@@ -195,6 +263,8 @@ def run_reference(args, rank, world):
     from oracle import oracle as O
 
     w = WORKLOADS[args.workload]()
+    if args.steps is None:
+        args.steps = w.steps
     O.build()
     threads = os.cpu_count() or 1
     sim = O.OracleSim(w, 0, serial_noise=True, threads=threads)
@@ -209,6 +279,7 @@ def run_reference(args, rank, world):
     sim.run(s, k, first_step=args.warmup + 1)
     dt = time.perf_counter() - t0
     value = sim.n * k / dt
+
     line = {
         "metric": "LLG spin-steps/s", "value": value, "unit": "spin-steps/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": k, "warmup": args.warmup, "ms_per_step": 1e3 * dt / k,
@@ -226,13 +297,20 @@ def run_reference(args, rank, world):
 # -------------------------------------------------------------------- GPU --
 
 def traffic_from_profiles(workload: str, kernel: str, precision: str):
+    """DRAM bytes (read + write) of one launch of `kernel` on `workload`, from
+    the committed ncu summary profiles/dram_traffic.json, or None."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if not os.path.exists(path):
         return None
     try:
-        d = json.load(open(path))
-        return d.get(workload, {}).get(precision, {}).get(kernel)
-    except (ValueError, OSError):
+        d = json.load(open(path)).get(workload, {}).get(precision, {})
+        e = d.get(kernel)
+        if e is None and kernel.startswith("tiled_stage<"):
+            # the same stage compiled for another occupancy moves the same bytes
+            stem = kernel.rsplit(",", 1)[0]
+            e = next((v for k, v in d.items() if k.rsplit(",", 1)[0] == stem), None)
+        return None if e is None else float(e["dram_bytes_per_launch"])
+    except (ValueError, OSError, KeyError, TypeError):
         return None
 
 
@@ -244,16 +322,15 @@ def main():
 
     import torch
 
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    init_ranks(world, local)
     torch.cuda.set_device(local)
     from jams_gb300 import build as B
     from jams_gb300 import llg
 
     B.build()
-    w = WORKLOADS[args.workload]()
+    w = rank_workload(args.workload, rank)
+    if args.steps is None:
+        args.steps = w.steps
     prec = llg.FP32C if args.precision == "fp32c" else llg.FP64
     integ = "heun" if w.model.integrator == W.HEUN else "rk4"
     stream = torch.cuda.Stream()
@@ -269,7 +346,9 @@ def main():
         sol.set_tuning(tx, bool(st), oc)
         tuning = sol.kernel_info()
     else:
-        tuning = sol.autotune(trial_steps=10) if not args.no_tune else sol.kernel_info()
+        # the choice is cached per lattice shape ($JAMS_LLG_TUNE_CACHE), so a
+        # second run of the same command launches no trial kernels
+        tuning = sol.autotune(trial_steps=10, use_cache=True) if not args.no_tune else sol.kernel_info()
 
     # warm-up (also builds nothing lazily: single steps use direct launches)
     for _ in range(args.warmup):
@@ -297,7 +376,7 @@ def main():
     step_ms = [a.elapsed_time(b) for a, b in evs]
     total_ms = max_over_ranks(sum(step_ms), world, torch.device("cuda", local))
     ms_per_step = total_ms / args.steps
-    value = world * n_spins * args.steps / (total_ms * 1e-3)
+    value = job_rate(n_spins, world, args.steps, total_ms * 1e-3)
     sol.synchronize()
 
     # ---- per-stage kernel durations (same flush between steps)
@@ -318,10 +397,10 @@ def main():
     peak = peaks.get("hbm_gbs")
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
-    kernel_name = STAGE_NAMES[integ][dom] + ("_f32" if args.precision == "fp32c" else "_f64")
-    traffic = traffic_from_profiles(args.workload, kernel_name, args.precision)
+    kname = kernel_name(tuning, integ, dom, args.precision)
+    traffic = traffic_from_profiles(args.workload, kname, args.precision)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": kernel_name, "peak_source": peak_src,
+                "traffic": traffic, "kernel": kname, "stage": STAGE_NAMES[integ][dom], "peak_source": peak_src,
                 "stage_ms": [float(x) for x in stage_ms],
                 "algorithmic_bytes_per_spin_step": int(sum(STAGE_BYTES[(integ, args.precision)])),
                 "step_frac": (sum(STAGE_BYTES[(integ, args.precision)]) * n_spins / (ms_per_step * 1e-3) / 1e9)
@@ -362,7 +441,7 @@ def main():
             sol.get_state(-1, out=host_np)
         dt = time.perf_counter() - t0
         dt = max_over_ranks(dt, world, torch.device("cuda", local))
-        e2e = {"value": world * n_spins * ke / dt, "unit": "spin-steps/s", "h2d_bytes_per_step": n_spins * 24,
+        e2e = {"value": job_rate(n_spins, world, ke, dt), "unit": "spin-steps/s", "h2d_bytes_per_step": n_spins * 24,
                "d2h_bytes_per_step": n_spins * 24, "steps": ke}
 
     # ---- CPU baseline (rank 0, N = 1 only)
@@ -372,6 +451,10 @@ def main():
         cpu = {"value": rate, "unit": "spin-steps/s", "cores": cores, "kind": "port",
                "sample": "%d Heun/RK4 steps of replica 0 (%d spins), oracle restatement of the reference CPU path"
                          % (n_steps, n_rep)}
+
+    # |M| of every replica of every rank at the end of the run
+    mags = [float(sol.observables(r)[0][3]) for r in range(len(w.replicas))]
+    mags = gather_scalars(mags, world, torch.device("cuda", local))
 
     line = {
         "metric": "LLG spin-steps/s", "value": value, "unit": "spin-steps/s", "n_gpus": world,
@@ -384,6 +467,7 @@ def main():
                    else "single GPU", "kernels": tuning},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         "steady_state_graph": steady, "wall_s_timed_region": t_wall,
+        "final_abs_m": {"mean": float(np.mean([m for r in mags for m in r])), "ranks": len(mags)},
     }
     if rank == 0:
         print(json.dumps(line))

@@ -48,7 +48,8 @@ enum {
   LLG_ERR_TIMEOUT = -4,      /* a device-side wait ran out of iterations */
   LLG_ERR_NONFINITE = -5,    /* a spin became NaN or infinite */
   LLG_ERR_NO_DEVICE = -6,    /* no usable sm_103 device */
-  LLG_ERR_UNSUPPORTED = -7   /* combination not implemented */
+  LLG_ERR_UNSUPPORTED = -7,  /* combination not implemented */
+  LLG_ERR_IO = -8            /* a file could not be read, written or parsed */
 };
 
 /* arithmetic form */
@@ -244,6 +245,46 @@ int llg_autotune(llg_handle *h, int32_t trial_steps, int32_t use_cache);
    GPU race.  Errors are reported through llg_last_error(NULL). */
 int llg_magnetisation_noalloc(const double *spins_dev, int64_t n_spins, int32_t nb, const double *mus,
                               double *m4_dev, void *cuda_stream);
+
+/* ---- spin files and checkpoints ------------------------------------ */
+
+/* Writes a rows x cols array (row-major doubles) to `path`: HDF5 when the
+   name ends in ".h5" (one contiguous float64 dataset named `dataset` in the
+   root group, the file the reference's HDF5 monitor writes with
+   HighFive's createDataSet<double>, src/jams/monitors/hdf5.cc:292-307),
+   else text, one row per line, 17 significant digits.  Needs no device. */
+int llg_write_array_file(const char *path, const char *dataset, const double *data, int64_t rows, int64_t cols);
+
+/* Reads an array the way the reference loads spins and per-spin parameters
+   (load_array_from_file, src/jams/helpers/load.h:14-60): HDF5 dataset
+   `dataset` of a ".h5" file (contiguous or compact float64/float32; chunked
+   or compressed datasets give LLG_ERR_IO), else every number of a text file
+   ('#' and '//' comment lines skipped) with rows = count, cols = 1.
+   With data == NULL only *rows and *cols are set; LLG_ERR_BAD_DESC when
+   rows x cols exceeds capacity.  Needs no device. */
+int llg_read_array_file(const char *path, const char *dataset, double *data, int64_t capacity, int64_t *rows,
+                        int64_t *cols);
+
+/* /spins of one replica (N x 3, reference site order) to / from a file in
+   the formats above: the HDF5 monitor's spin output
+   (src/jams/monitors/hdf5.cc:94-150) and init_h5's "spins" input
+   (src/jams/initializer/init_h5.cc:10-34).  Reading requires exactly 3N
+   values, as the reference does. */
+int llg_write_spins(llg_handle *h, int32_t replica, const char *path);
+int llg_read_spins(llg_handle *h, int32_t replica, const char *path);
+
+/* Checkpoint: every replica's state (FP64, exact for both precisions), the
+   iteration (which is also the noise step counter), each replica's
+   temperature and applied field, and a fingerprint of the model (replica
+   count and sizes, basis, precision, integrator, dt, seed).  Loading it into
+   a solver created from the same description continues the trajectory bit
+   for bit, thermal noise included.  The file is written beside `path` and
+   renamed into place; a checksum guards the load, which changes nothing
+   unless the whole file verifies.  The reference restarts from the HDF5
+   monitor's spins through init_h5 and a fresh noise stream; this call has
+   no single reference counterpart. */
+int llg_save_checkpoint(llg_handle *h, const char *path);
+int llg_load_checkpoint(llg_handle *h, const char *path);
 
 #ifdef __cplusplus
 }

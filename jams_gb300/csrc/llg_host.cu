@@ -29,6 +29,7 @@
 #include "llg_internal.h"
 
 #include "llg_families.h"
+#include "llg_io.h"
 #include "llg_kernels.h"
 
 using namespace jams_llg;
@@ -1324,6 +1325,220 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   if (rc) return rc;
   tuning_store(key, choice.first, choice.second);
   return 0;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------- spin files, checkpoints --
+
+namespace {
+
+constexpr char kCkptMagic[8] = {'J', 'L', 'L', 'G', 'C', 'K', 'P', 'T'};
+constexpr uint32_t kCkptVersion = 1;
+
+struct Bytes {
+  std::vector<uint8_t> b;
+  void u32(uint64_t v) { for (int i = 0; i < 4; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
+  void u64(uint64_t v) { for (int i = 0; i < 8; ++i) b.push_back((uint8_t)(v >> (8 * i))); }
+  void f64(double x) {
+    uint64_t u;
+    std::memcpy(&u, &x, 8);
+    u64(u);
+  }
+};
+
+struct Reader {
+  const std::vector<uint8_t>& b;
+  size_t p = 0;
+  bool ok = true;
+  uint64_t un(int n) {
+    if (p + n > b.size()) {
+      ok = false;
+      return 0;
+    }
+    uint64_t v = 0;
+    for (int i = 0; i < n; ++i) v |= (uint64_t)b[p + i] << (8 * i);
+    p += n;
+    return v;
+  }
+  double f64() {
+    const uint64_t u = un(8);
+    double x;
+    std::memcpy(&x, &u, 8);
+    return x;
+  }
+};
+
+// FNV-1a, 64 bit
+uint64_t fnv1a(const uint8_t* p, size_t n) {
+  uint64_t h = 1469598103934665603ull;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+// header fields that must match between the writing and the loading solver
+void ckpt_fingerprint(const llg_handle* h, Bytes& o) {
+  o.u32(h->fp64 ? LLG_FP64 : LLG_FP32C);
+  o.u32(h->integrator);
+  o.u32(h->nb);
+  o.u32(h->reps.size());
+  o.f64(h->dt);
+  o.u64(h->P.seed);
+  for (const ReplicaDev& R : h->reps) {
+    o.u32(R.L[0]);
+    o.u32(R.L[1]);
+    o.u32(R.L[2]);
+    o.u32(R.n);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int llg_write_array_file(const char* path, const char* dataset, const double* data, int64_t rows, int64_t cols) {
+  if (!path || !data || rows < 0 || cols < 1) return tls_fail(LLG_ERR_BAD_DESC, "bad array file arguments");
+  std::string err;
+  std::vector<llgio::Dataset> sets{{llgio::dataset_name(dataset ? dataset : "data"), data, rows, cols}};
+  if (llgio::write_array(path, sets, err)) return tls_fail(LLG_ERR_IO, "%s", err.c_str());
+  return 0;
+}
+
+int llg_read_array_file(const char* path, const char* dataset, double* data, int64_t capacity, int64_t* rows,
+                        int64_t* cols) {
+  if (!path || !rows || !cols) return tls_fail(LLG_ERR_BAD_DESC, "bad array file arguments");
+  std::string err;
+  std::vector<double> v;
+  int64_t r = 0, c = 0;
+  if (llgio::read_array(path, dataset ? dataset : "data", v, r, c, err)) return tls_fail(LLG_ERR_IO, "%s", err.c_str());
+  *rows = r;
+  *cols = c;
+  if (!data) return 0;
+  if ((int64_t)v.size() > capacity)
+    return tls_fail(LLG_ERR_BAD_DESC, "%s holds %lld values, the buffer %lld", path, (long long)v.size(),
+                    (long long)capacity);
+  std::memcpy(data, v.data(), v.size() * sizeof(double));
+  return 0;
+}
+
+int llg_write_spins(llg_handle* h, int32_t replica, const char* path) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (replica < 0 || replica >= (int32_t)h->reps.size() || !path)
+    return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
+  const int64_t n = h->reps[replica].n;
+  std::vector<double> s((size_t)n * 3);
+  int rc = llg_get_state(h, replica, s.data());
+  if (rc) return rc;
+  std::string err;
+  std::vector<llgio::Dataset> sets{{"spins", s.data(), n, 3}};
+  if (llgio::write_array(path, sets, err)) return h->fail(LLG_ERR_IO, "%s", err.c_str());
+  return 0;
+}
+
+int llg_read_spins(llg_handle* h, int32_t replica, const char* path) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (replica < 0 || replica >= (int32_t)h->reps.size() || !path)
+    return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
+  const int64_t n = h->reps[replica].n;
+  std::string err;
+  std::vector<double> v;
+  int64_t r = 0, c = 0;
+  if (llgio::read_array(path, "spins", v, r, c, err)) return h->fail(LLG_ERR_IO, "%s", err.c_str());
+  if ((int64_t)v.size() != 3 * n)
+    return h->fail(LLG_ERR_IO, "loading array from file: '%s' expected size: %lld actual size: %lld", path,
+                   (long long)(3 * n), (long long)v.size());
+  return llg_set_state(h, replica, v.data());
+}
+
+int llg_save_checkpoint(llg_handle* h, const char* path) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (!path) return h->fail(LLG_ERR_BAD_DESC, "null path");
+  Bytes o;
+  o.b.insert(o.b.end(), kCkptMagic, kCkptMagic + 8);
+  o.u32(kCkptVersion);
+  ckpt_fingerprint(h, o);
+  o.u64((uint64_t)h->iteration);
+  for (size_t r = 0; r < h->reps.size(); ++r) {
+    o.f64(h->rep_T[r]);
+    for (int a = 0; a < 3; ++a) o.f64(h->reps[r].B[a]);
+  }
+  std::vector<double> s;
+  for (size_t r = 0; r < h->reps.size(); ++r) {
+    s.resize((size_t)h->reps[r].n * 3);
+    int rc = llg_get_state(h, (int32_t)r, s.data());
+    if (rc) return rc;
+    for (double x : s) o.f64(x);
+  }
+  o.u64(fnv1a(o.b.data(), o.b.size()));
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return h->fail(LLG_ERR_IO, "cannot open %s for writing", tmp.c_str());
+  bool ok = std::fwrite(o.b.data(), 1, o.b.size(), f) == o.b.size();
+  ok = std::fflush(f) == 0 && ok;
+  ok = std::fclose(f) == 0 && ok;
+  if (!ok || std::rename(tmp.c_str(), path) != 0) {
+    std::remove(tmp.c_str());
+    return h->fail(LLG_ERR_IO, "writing checkpoint %s failed", path);
+  }
+  return 0;
+}
+
+int llg_load_checkpoint(llg_handle* h, const char* path) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (!path) return h->fail(LLG_ERR_BAD_DESC, "null path");
+  std::vector<uint8_t> b;
+  {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return h->fail(LLG_ERR_IO, "cannot open checkpoint %s", path);
+    std::fseek(f, 0, SEEK_END);
+    const long n = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    b.resize(n > 0 ? (size_t)n : 0);
+    const bool ok = n > 0 && std::fread(b.data(), 1, b.size(), f) == b.size();
+    std::fclose(f);
+    if (!ok) return h->fail(LLG_ERR_IO, "cannot read checkpoint %s", path);
+  }
+  if (b.size() < 8 + 4 + 8 || std::memcmp(b.data(), kCkptMagic, 8) != 0)
+    return h->fail(LLG_ERR_IO, "%s is not a checkpoint of this library", path);
+  {
+    Reader t{b, b.size() - 8};
+    if (t.un(8) != fnv1a(b.data(), b.size() - 8)) return h->fail(LLG_ERR_IO, "checkpoint %s: checksum mismatch", path);
+  }
+  Reader rd{b, 8};
+  if (rd.un(4) != kCkptVersion) return h->fail(LLG_ERR_IO, "checkpoint %s: unknown format version", path);
+  Bytes fp;
+  ckpt_fingerprint(h, fp);
+  if (rd.p + fp.b.size() > b.size() || std::memcmp(&b[rd.p], fp.b.data(), fp.b.size()) != 0)
+    return h->fail(LLG_ERR_BAD_DESC,
+                   "checkpoint %s was written by a different model (replicas, sizes, basis, precision, "
+                   "integrator, dt or seed differ)",
+                   path);
+  rd.p += fp.b.size();
+  const int64_t iteration = (int64_t)rd.un(8);
+  std::vector<double> T(h->reps.size()), B(3 * h->reps.size());
+  for (size_t r = 0; r < h->reps.size(); ++r) {
+    T[r] = rd.f64();
+    for (int a = 0; a < 3; ++a) B[3 * r + a] = rd.f64();
+  }
+  size_t need = 0;
+  for (const ReplicaDev& R : h->reps) need += (size_t)R.n * 3 * 8;
+  if (!rd.ok || rd.p + need + 8 != b.size()) return h->fail(LLG_ERR_IO, "checkpoint %s: truncated", path);
+  std::vector<double> s;
+  for (size_t r = 0; r < h->reps.size(); ++r) {
+    s.resize((size_t)h->reps[r].n * 3);
+    for (double& x : s) x = rd.f64();
+    int rc = llg_set_state(h, (int32_t)r, s.data());
+    if (rc) return rc;
+  }
+  for (size_t r = 0; r < h->reps.size(); ++r) {
+    int rc = llg_set_temperature(h, (int32_t)r, T[r]);
+    if (!rc) rc = llg_set_field(h, (int32_t)r, &B[3 * r]);
+    if (rc) return rc;
+  }
+  return llg_set_iteration(h, iteration);
 }
 
 }  // extern "C"

@@ -25,7 +25,7 @@ RK4 = 1
 
 ERRORS = {
     -1: "LLG_ERR_BAD_DESC", -2: "LLG_ERR_OOM", -3: "LLG_ERR_CUDA", -4: "LLG_ERR_TIMEOUT",
-    -5: "LLG_ERR_NONFINITE", -6: "LLG_ERR_NO_DEVICE", -7: "LLG_ERR_UNSUPPORTED",
+    -5: "LLG_ERR_NONFINITE", -6: "LLG_ERR_NO_DEVICE", -7: "LLG_ERR_UNSUPPORTED", -8: "LLG_ERR_IO",
 }
 
 EXPORTED = [
@@ -35,6 +35,8 @@ EXPORTED = [
     "llg_fields", "llg_observables", "llg_topological_charge", "llg_set_stream", "llg_last_launch_count",
     "llg_profile_stages", "llg_kernel_info", "llg_set_tuning", "llg_autotune", "llg_magnetisation_noalloc",
     "llg_create_from_config", "llg_config_describe", "llg_max_steps",
+    "llg_write_array_file", "llg_read_array_file", "llg_write_spins", "llg_read_spins",
+    "llg_save_checkpoint", "llg_load_checkpoint",
 ]
 
 
@@ -115,6 +117,13 @@ def lib():
         L.llg_config_describe.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, i64]
         L.llg_max_steps.argtypes = [vp]
         L.llg_max_steps.restype = i64
+        cp = ctypes.c_char_p
+        L.llg_write_array_file.argtypes = [cp, cp, dp, i64, i64]
+        L.llg_read_array_file.argtypes = [cp, cp, dp, i64, ctypes.POINTER(i64), ctypes.POINTER(i64)]
+        for f in ("llg_write_spins", "llg_read_spins"):
+            getattr(L, f).argtypes = [vp, i32, cp]
+        for f in ("llg_save_checkpoint", "llg_load_checkpoint"):
+            getattr(L, f).argtypes = [vp, cp]
         _lib = L
     return _lib
 
@@ -143,6 +152,31 @@ def describe_config(text: str, patch: str = "") -> dict:
             n *= 4
             continue
         raise LLGError(rc, msg)
+
+
+def write_array_file(path: str, array: np.ndarray, dataset: str = "/spins") -> None:
+    """Writes a 1-D or 2-D array of doubles: HDF5 dataset `dataset` when
+    `path` ends in ".h5", else text (no GPU needed)."""
+    a = np.ascontiguousarray(array, dtype=np.float64)
+    rows, cols = (a.shape[0], 1) if a.ndim == 1 else a.shape
+    rc = lib().llg_write_array_file(os.fsencode(path), dataset.encode(), _dp(a), rows, cols)
+    if rc != 0:
+        raise LLGError(rc, lib().llg_last_error(None).decode())
+
+
+def read_array_file(path: str, dataset: str = "/spins") -> np.ndarray:
+    """Reads an array as the reference's load_array_from_file does: HDF5
+    dataset (rows x cols) or every number of a text file (flat)."""
+    L = lib()
+    rows, cols = ctypes.c_int64(), ctypes.c_int64()
+    rc = L.llg_read_array_file(os.fsencode(path), dataset.encode(), None, 0, ctypes.byref(rows), ctypes.byref(cols))
+    if rc == 0:
+        out = np.empty((rows.value, cols.value))
+        rc = L.llg_read_array_file(os.fsencode(path), dataset.encode(), _dp(out), out.size, ctypes.byref(rows),
+                                   ctypes.byref(cols))
+    if rc != 0:
+        raise LLGError(rc, L.llg_last_error(None).decode())
+    return out if cols.value > 1 else out.reshape(-1)
 
 
 class Solver:
@@ -261,6 +295,20 @@ class Solver:
             out = np.empty((self.num_spins(replica), 3))
         self._check(self.L.llg_get_state(self.h, replica, out.ctypes.data))
         return out
+
+    def write_spins(self, path: str, replica: int = 0) -> None:
+        """/spins (N x 3) of one replica to an HDF5 (".h5") or text file."""
+        self._check(self.L.llg_write_spins(self.h, replica, os.fsencode(path)))
+
+    def read_spins(self, path: str, replica: int = 0) -> None:
+        """Sets one replica's state from /spins of an HDF5 file or a text file."""
+        self._check(self.L.llg_read_spins(self.h, replica, os.fsencode(path)))
+
+    def save_checkpoint(self, path: str) -> None:
+        self._check(self.L.llg_save_checkpoint(self.h, os.fsencode(path)))
+
+    def load_checkpoint(self, path: str) -> None:
+        self._check(self.L.llg_load_checkpoint(self.h, os.fsencode(path)))
 
     def set_state_device(self, ptr: int, replica: int = -1) -> None:
         self._check(self.L.llg_set_state_device(self.h, replica, ptr))
