@@ -1291,15 +1291,19 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   cudaEventCreate(&e1);
   float best = 1e30f;
   std::pair<int, int> choice = {h->TP.TX, (h->store_mode ? 1 : 0) | (h->occupancy << 4)};
+  // each trial runs as llg_step runs steps: one CUDA graph of trial_steps
+  // steps (captured and run once untimed, then timed)
+  const int spg0 = h->steps_per_graph;
+  trial_steps += trial_steps & 1;
+  h->steps_per_graph = trial_steps;
   for (auto& c : cands) {
     rc = llg_set_tuning(h, c.first, c.second);
+    if (!rc) rc = llg_step(h, trial_steps);
     if (rc) break;
-    enqueue_steps(h, 2, h->cur);
-    h->cur = next_buffer(h, next_buffer(h, h->cur));
     cudaEventRecord(e0, h->stream);
-    enqueue_steps(h, trial_steps, h->cur);
+    rc = llg_step(h, trial_steps);
     cudaEventRecord(e1, h->stream);
-    if (trial_steps & 1) h->cur = next_buffer(h, h->cur);
+    if (rc) break;
     ce = cudaEventSynchronize(e1);
     if (ce != cudaSuccess) {
       rc = h->cuda_fail(ce, "autotune trial");
@@ -1314,6 +1318,7 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  h->steps_per_graph = spg0;
   if (rc) return rc;
   // restore state, buffer parity and the noise counter
   h->cur = cur0;
