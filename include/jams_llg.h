@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define LLG_ABI_VERSION 1
+#define LLG_ABI_VERSION 2
 
 /* status codes */
 enum {
@@ -68,7 +68,10 @@ enum {
   LLG_TERM_EXCHANGE = 0,      /* module "exchange": bilinear 3x3 tensors */
   LLG_TERM_UNIAXIAL = 1,      /* module "uniaxial": -K (S.a)^p, p = 2, 4, 6 */
   LLG_TERM_CUBIC = 2,         /* module "cubic": K1 or K2 cubic anisotropy */
-  LLG_TERM_APPLIED_FIELD = 3  /* module "applied-field"/"zeeman": mu_s B */
+  LLG_TERM_APPLIED_FIELD = 3, /* module "applied-field"/"zeeman": mu_s B */
+  LLG_TERM_DIPOLE = 4         /* modules "dipole-fft" (and its brute-force,
+                                 tensor, neighbour-list, near-tree twins):
+                                 magnetic dipole-dipole field within a cutoff */
 };
 
 typedef struct {
@@ -88,6 +91,18 @@ typedef struct {
   const double *K;
   const double *axis;
   double B[3];            /* applied field (T) */
+  /* dipole: h_i = mu_i sum_j mu_j mu0 (3 r (r.S_j) - r^2 S_j) / (4 pi a^3 |r|^5)
+     over every site pair closer than r_cutoff + distance_tolerance
+     (src/jams/hamiltonian/dipole_fft.cc:205-265, dipole_bruteforce.cc:80-119):
+     r in lattice parameters from the lattice vectors (rows a1, a2, a3, in
+     lattice parameters) and the fractional basis positions, minimum image
+     along periodic axes; r_cutoff must not exceed the inradius of the
+     periodic supercell.  lattice_parameter a in metres. */
+  double r_cutoff;
+  double distance_tolerance;
+  double lattice_parameter;
+  const double *lattice_vectors;  /* 9 */
+  const double *positions;        /* 3 nb */
 } llg_term;
 
 typedef struct {

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libjams_llg.so")
 SOURCES = ["llg_kernels.cu", "llg_tiled.cu", "llg_observe.cu", "llg_host.cu", "llg_noalloc.cu", "llg_config.cu",
-           "llg_io.cu"]
+           "llg_io.cu", "llg_dipole.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler",
               "-fPIC,-ffp-contract=off,-Wall", "-I" + os.path.join(HERE, "..", "include")]
@@ -57,7 +57,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
         return LIB
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
-    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", LIB, *objs]
+    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", LIB, *objs, "-lcufft"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), res.stdout + res.stderr))

@@ -39,7 +39,8 @@ sim : { seed = %d; };
 """ % (L, L, L, J, dz, Bz, t_step, t_step * steps, T, seed)
 
 
-def bcc_three_shell(L=64, T=300.0, t_step=0.5e-15, steps=20000, seed=1, spin="[0.0, 0.0, 1.0]") -> str:
+def bcc_three_shell(L=64, T=300.0, t_step=0.5e-15, steps=20000, seed=1, spin="[0.0, 0.0, 1.0]",
+                    dipole_cutoff=None) -> str:
     return _header("Fe", 2.2, 0.05, spin) + """
 // conventional cubic cell, two-site basis
 unitcell : {
@@ -60,13 +61,14 @@ hamiltonians = (
       ("Fe", "Fe", [1.0, 1.0, 0.0], -0.1)    // shell 3: 12 at a<110>
     );
   },
-  { module = "cubic"; energy_units = "meV"; K1 = ( (0.005, [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]) ); }
+  { module = "cubic"; energy_units = "meV"; K1 = ( (0.005, [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]) ); }%s
 );
 
 solver : { module = "llg-heun-gpu"; t_step = %r; t_max = %r; };
 physics : { temperature = %r; };
 sim : { seed = %d; };
-""" % (L, L, L, t_step, t_step * steps, T, seed)
+""" % (L, L, L, (',\n  { module = "dipole-fft"; r_cutoff = %r; }' % dipole_cutoff) if dipole_cutoff else "",
+       t_step, t_step * steps, T, seed)
 
 
 def triangular_dmi(L=2048, T=5.0, Bz=0.0, t_step=1e-15, steps=5000, seed=1, J1=1.0, D=0.3) -> str:

@@ -382,6 +382,7 @@ struct Basis {
 struct Model {
   // lattice
   M3 cell{};        // columns are a1, a2, a3 (units of the lattice parameter)
+  double parameter = 0.0;   // lattice parameter (m)
   M3 cell_inv{};
   std::vector<Basis> basis;
   int L[3] = {1, 1, 1};
@@ -399,6 +400,7 @@ struct Model {
     std::string module;
     std::vector<int32_t> bi, bj, T;
     std::vector<double> J, K, axis;
+    std::vector<double> vectors, positions;   // dipole geometry
   };
   std::vector<Term> terms;
   // solver / physics / sim
@@ -743,6 +745,7 @@ Model build_model(const Node& root) {
     for (int j = 0; j < 3; ++j) m.cell[i][j] = row[j];
   }
   m.cell_inv = inverse(m.cell);
+  if (const Node* n = uc.find("parameter")) m.parameter = n->num();
   std::string pos_format = "fractional";
   if (const Node* n = uc.find("coordinate_format")) pos_format = lower(n->str());
   const Node& pos = uc.at("positions");
@@ -823,6 +826,20 @@ Model build_model(const Node& root) {
           if (!approx_eq(vec3(dc->at(q)), B, 0.0)) throw CfgError("zeeman: per-material fields differ");
         for (int c = 0; c < 3; ++c) t.t.B[c] = B[c];
       }
+    } else if (t.module == "dipole-fft" || t.module == "dipole-bruteforce" || t.module == "dipole-tensor" ||
+               t.module == "dipole-neighbour-list" || t.module == "dipole-neartree") {
+      // the same sum by every method (docs/source/hamiltonians/dipole.rst);
+      // here always by FFT convolution
+      t.t.kind = LLG_TERM_DIPOLE;
+      t.t.r_cutoff = h.at("r_cutoff").num();
+      t.t.distance_tolerance = 1e-4;   // jams::defaults::lattice_tolerance
+      if (const Node* n = h.find("distance_tolerance")) t.t.distance_tolerance = n->num();
+      if (!(m.parameter > 0.0)) throw CfgError(t.module + ": unitcell.parameter (m) is required");
+      t.t.lattice_parameter = m.parameter;
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) t.vectors.push_back(m.cell[c][r]);   // rows a1, a2, a3
+      for (const Basis& b : m.basis)
+        for (int c = 0; c < 3; ++c) t.positions.push_back(b.frac[c]);
     } else {
       throw CfgError("hamiltonian module '" + t.module + "' is not on the LLG hot path");
     }
@@ -842,6 +859,8 @@ void fill_desc(Model& m, llg_desc& d, llg_replica& rep, std::vector<llg_term>& t
     lt.J = t.J.data();
     lt.K = t.K.empty() ? nullptr : t.K.data();
     lt.axis = t.axis.empty() ? nullptr : t.axis.data();
+    lt.lattice_vectors = t.vectors.empty() ? nullptr : t.vectors.data();
+    lt.positions = t.positions.empty() ? nullptr : t.positions.data();
     terms.push_back(lt);
   }
   d = llg_desc{};
@@ -987,6 +1006,11 @@ int llg_config_describe(const char* config_text, const char* patch_text, char* j
       arr("K", t.K);
       arr("axis", t.axis);
       arr("B", std::vector<double>{t.t.B[0], t.t.B[1], t.t.B[2]});
+      if (t.t.kind == LLG_TERM_DIPOLE) {
+        arr("dipole", std::vector<double>{t.t.r_cutoff, t.t.distance_tolerance, t.t.lattice_parameter});
+        arr("lattice_vectors", t.vectors);
+        arr("positions", t.positions);
+      }
       o << "}";
     }
     o << "]}";

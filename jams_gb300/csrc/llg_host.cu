@@ -28,6 +28,7 @@
 #include "../../include/jams_llg.h"
 #include "llg_internal.h"
 
+#include "llg_dipole.h"
 #include "llg_families.h"
 #include "llg_io.h"
 #include "llg_kernels.h"
@@ -142,8 +143,16 @@ struct llg_handle {
   int tz = 0, ty = 0;
   TiledParams TP{};
   DevBuf<int4> d_tiles4;
+  // dipole-dipole term: FFT convolution state and the field planes of the
+  // stage input (0: start-of-step state, 1: Heun predictor state)
+  bool has_dipole = false;
+  DipoleGeometry dip_geom{};
+  DipoleField* dipole = nullptr;
+  DevBuf<unsigned char> d_hdip[2];
+  std::string async_err;     // a failure inside an enqueue (reported by llg_step)
 
   ~llg_handle() {
+    if (dipole) dipole_destroy(dipole);
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
@@ -464,6 +473,23 @@ int build(llg_handle* h, const llg_desc* d) {
         for (int a = 0; a < 3; ++a) h->term_B[3 * t + a] = T.B[a];
         ++field_terms;
         break;
+      case LLG_TERM_DIPOLE: {
+        if (h->has_dipole) return h->fail(LLG_ERR_UNSUPPORTED, "more than one dipole term");
+        if (!T.lattice_vectors || !T.positions)
+          return h->fail(LLG_ERR_BAD_DESC, "dipole term %d needs lattice_vectors and positions", t);
+        if (!(T.r_cutoff > 0.0) || !(T.lattice_parameter > 0.0) || !(T.distance_tolerance >= 0.0) ||
+            !std::isfinite(T.r_cutoff) || !std::isfinite(T.lattice_parameter))
+          return h->fail(LLG_ERR_BAD_DESC, "dipole term %d: r_cutoff and lattice_parameter must be positive", t);
+        DipoleGeometry& G = h->dip_geom;
+        G.r_cutoff = T.r_cutoff;
+        G.tolerance = T.distance_tolerance;
+        G.a = T.lattice_parameter;
+        for (int a = 0; a < 9; ++a) G.A[a] = T.lattice_vectors[a];
+        for (int b = 0; b < d->nb; ++b)
+          for (int a = 0; a < 3; ++a) G.frac[b][a] = T.positions[3 * b + a];
+        h->has_dipole = true;
+        break;
+      }
       default:
         return h->fail(LLG_ERR_BAD_DESC, "unknown term kind %d", T.kind);
     }
@@ -730,7 +756,41 @@ int build(llg_handle* h, const llg_desc* d) {
     int rc = build_tiles4(h);
     if (rc) return rc;
   }
+  if (h->has_dipole) {
+    std::vector<DipoleReplicaSpec> specs;
+    for (auto& R : h->reps) {
+      DipoleReplicaSpec sp;
+      for (int a = 0; a < 3; ++a) sp.L[a] = R.L[a];
+      sp.offset = R.offset;
+      specs.push_back(sp);
+    }
+    std::string err;
+    h->dipole = dipole_create(h->dip_geom, d->nb, d->periodic, d->mus, specs, h->fp64, err);
+    if (!h->dipole) return h->fail(LLG_ERR_BAD_DESC, "%s", err.c_str());
+    for (auto& b : h->d_hdip)
+      if ((ce = b.alloc((size_t)3 * h->npad * real_size(h))) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  }
   return 0;
+}
+
+// Params of one launch: the dipole field planes of the launch's input state
+// (computed here, on the stream, when the model has a dipole term) and of
+// the start-of-step state
+Params launch_params(llg_handle* h, const void* input, int slot) {
+  Params P = h->P;
+  if (!h->dipole) return P;
+  if (input) {
+    const std::string err = dipole_compute(h->dipole, input, h->d_hdip[slot].p, h->npad, h->stream);
+    if (!err.empty() && h->async_err.empty()) h->async_err = err;
+  }
+  if (h->fp64) {
+    P.hdip64 = reinterpret_cast<const double*>(h->d_hdip[slot].p);
+    P.hdip64_s0 = reinterpret_cast<const double*>(h->d_hdip[0].p);
+  } else {
+    P.hdip32 = reinterpret_cast<const float*>(h->d_hdip[slot].p);
+    P.hdip32_s0 = reinterpret_cast<const float*>(h->d_hdip[0].p);
+  }
+  return P;
 }
 
 // uploads replica records (temperature- and field-dependent parts)
@@ -763,7 +823,13 @@ int num_stages(const llg_handle* h) { return h->integrator == LLG_HEUN ? 2 : 4; 
 // launches stage `stage` of step `ks` of a block; `cur` is the buffer that
 // holds the state at the start of the step (FP32 Heun alternates 0 and 2)
 void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur) {
-  const Params& P = h->P;
+  // the stage's input state (whose dipole field the stage needs)
+  const void* input;
+  if (h->integrator == LLG_HEUN)
+    input = stage == 0 ? h->state[h->fp64 ? 0 : cur].p : h->state[1].p;
+  else
+    input = stage == 0 ? h->state[0].p : (stage == 2 ? h->state[2].p : h->state[1].p);
+  const Params P = launch_params(h, input, (h->integrator == LLG_HEUN && stage == 1) ? 1 : 0);
   const unsigned grid = (unsigned)P.ntiles;
   cudaStream_t st = h->stream;
   if (h->tiled) {
@@ -993,6 +1059,11 @@ int llg_step(llg_handle* h, int32_t nsteps) {
     if (remaining & 1) h->cur = next_buffer(h, h->cur);
     h->iteration += remaining;
   }
+  if (!h->async_err.empty()) {
+    const std::string e = h->async_err;
+    h->async_err.clear();
+    return h->fail(LLG_ERR_CUDA, "%s", e.c_str());
+  }
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) return h->cuda_fail(ce, "launching LLG steps");
   return 0;
@@ -1057,10 +1128,16 @@ int llg_fields(llg_handle* h, int32_t replica, double* h_host) {
   const ReplicaDev& R = h->reps[replica];
   const dim3 grid((unsigned)h->P.ntiles);
   const int sb = state_buffer(h);
+  const Params P = launch_params(h, h->state[sb].p, 0);
+  if (!h->async_err.empty()) {
+    const std::string e = h->async_err;
+    h->async_err.clear();
+    return h->fail(LLG_ERR_CUDA, "%s", e.c_str());
+  }
   if (h->fp64)
-    fields_f64<<<grid, kBlock, 0, h->stream>>>(h->P, buf<double>(h, sb), h->d_scratch.p, replica);
+    fields_f64<<<grid, kBlock, 0, h->stream>>>(P, buf<double>(h, sb), h->d_scratch.p, replica);
   else
-    fields_f32<<<grid, kBlock, 0, h->stream>>>(h->P, buf<float>(h, sb), h->d_scratch.p, replica);
+    fields_f32<<<grid, kBlock, 0, h->stream>>>(P, buf<float>(h, sb), h->d_scratch.p, replica);
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) return h->cuda_fail(ce, "fields kernel");
   ce = cudaMemcpyAsync(h_host, h->d_scratch.p, (size_t)R.n * 3 * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1079,7 +1156,13 @@ int llg_observables(llg_handle* h, int32_t replica, double* m4, double* e_terms)
   if (rc) return rc;
   const int nq = 4 + h->nterms;
   const int sb = state_buffer(h);
-  rc = observe(h->P, h->state[sb].p, h->fp64, replica, h->rep_first_tile[replica], h->rep_ntiles[replica],
+  const Params P = launch_params(h, h->state[sb].p, 0);
+  if (!h->async_err.empty()) {
+    const std::string e = h->async_err;
+    h->async_err.clear();
+    return h->fail(LLG_ERR_CUDA, "%s", e.c_str());
+  }
+  rc = observe(P, h->state[sb].p, h->fp64, replica, h->rep_first_tile[replica], h->rep_ntiles[replica],
                h->d_partials.p, h->h_partials.data(), nq, h->stream);
   if (rc) return h->cuda_fail(cudaGetLastError(), "observables");
   // ordered sums over tiles (deterministic), Neumaier compensation

@@ -25,7 +25,7 @@ constexpr int kMaxSlots = 96;      // neighbour slots per basis site and term
 constexpr int kBlock = 256;        // threads per CTA, one spin per thread
 constexpr int32_t kMissing = INT32_MIN;  // neighbour outside an open boundary
 
-enum TermKind { kExchange = 0, kUniaxial = 1, kCubic = 2, kAppliedField = 3 };
+enum TermKind { kExchange = 0, kUniaxial = 1, kCubic = 2, kAppliedField = 3, kDipole = 4 };
 
 // per exchange term, FP32 form: isotropic parts grouped into shells
 // (sum of neighbour spins times one J), anisotropic remainders per slot
@@ -121,6 +121,20 @@ struct Params {
   unsigned int* status;   // bit 0: non-finite spin
   const uint64_t* step_base;  // iteration number of step 0 of a launch block
   uint32_t philox_keys[20];   // Philox4x32-10 round keys of the seed
+  // dipole field planes (meV, three planes of npad) of the stage's input
+  // state and of the start-of-step state; null without a dipole term
+  const float* hdip32;
+  const float* hdip32_s0;
+  const double* hdip64;
+  const double* hdip64_s0;
 };
+
+// the dipole planes of the input state in the precision Real
+template <class Real>
+__device__ __forceinline__ const Real* dipole_planes(const Params& P);
+template <>
+__device__ __forceinline__ const float* dipole_planes<float>(const Params& P) { return P.hdip32; }
+template <>
+__device__ __forceinline__ const double* dipole_planes<double>(const Params& P) { return P.hdip64; }
 
 }  // namespace jams_llg

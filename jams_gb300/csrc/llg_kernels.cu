@@ -152,7 +152,8 @@ __device__ __forceinline__ void exchange_f32(const Params& P, int t, const Repli
 
 // total field (meV) of all terms at spin s, compensated, FP32
 __device__ __forceinline__ void field_f32(const Params& P, const ReplicaDev& R, Site st, int64_t gi,
-                                          const Planes<const float>& S, const float s[3], float h[3]) {
+                                          const Planes<const float>& S, const float s[3], float h[3],
+                                          const float* hd) {
   float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
   const int b = st.b;
   for (int t = 0; t < P.nterms; ++t) {
@@ -194,6 +195,12 @@ __device__ __forceinline__ void field_f32(const Params& P, const ReplicaDev& R, 
         for (int m = 0; m < 3; ++m) acc_add(hi[m], lo[m], pre * (u[m] * cu + v[m] * cv + w[m] * cw));
         break;
       }
+      case kDipole:  // precomputed by FFT convolution for these spins
+        if (hd) {
+#pragma unroll
+          for (int m = 0; m < 3; ++m) acc_add(hi[m], lo[m], hd[m * P.npad + gi]);
+        }
+        break;
       default: {  // applied field: mu_s B
 #pragma unroll
         for (int m = 0; m < 3; ++m) acc_add(hi[m], lo[m], P.mus32[b] * R.Bf[m]);
@@ -281,7 +288,7 @@ __device__ __forceinline__ void exchange_f64(const Params& P, int t, const Repli
 // one term's field, FP64, reference association order
 __device__ __forceinline__ void term_field_f64(const Params& P, const TermDev& T, const ReplicaDev& R,
                                                Site st, int64_t gi, const Planes<const double>& S,
-                                               const double s[3], double f[3]) {
+                                               const double s[3], double f[3], const double* hd) {
   const int b = st.b;
   switch (T.kind) {
     case kExchange:
@@ -323,6 +330,11 @@ __device__ __forceinline__ void term_field_f64(const Params& P, const TermDev& T
       }
       break;
     }
+    case kDipole:
+      // precomputed by FFT convolution (cuda_dipole_fft.cu:184-209)
+#pragma unroll
+      for (int m = 0; m < 3; ++m) f[m] = hd ? hd[m * P.npad + gi] : 0.0;
+      break;
     default: {
       // src/jams/hamiltonian/applied_field.cc:146-148
 #pragma unroll
@@ -334,11 +346,12 @@ __device__ __forceinline__ void term_field_f64(const Params& P, const TermDev& T
 
 // Solver::compute_fields: copy of term 0 then daxpy(1.0) of the others
 __device__ __forceinline__ void field_f64(const Params& P, const ReplicaDev& R, Site st, int64_t gi,
-                                          const Planes<const double>& S, const double s[3], double h[3]) {
+                                          const Planes<const double>& S, const double s[3], double h[3],
+                                          const double* hd) {
   h[0] = h[1] = h[2] = 0.0;
   for (int t = 0; t < P.nterms; ++t) {
     double f[3];
-    term_field_f64(P, P.term[t], R, st, gi, S, s, f);
+    term_field_f64(P, P.term[t], R, st, gi, S, s, f, hd);
     if (t == 0) {
       h[0] = f[0];
       h[1] = f[1];
@@ -425,7 +438,7 @@ __global__ void __launch_bounds__(kBlock) heun_predict_f32(const __grid_constant
   const Planes<const float> S = planes(s0, P.npad);
   const float s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
   float h[3], w[3], rhs[3];
-  field_f32(P, R, st, me.gi, S, s, h);
+  field_f32(P, R, st, me.gi, S, s, h, P.hdip32);
   noise_f32(P, R, me.r, st.b, me.i, step, w);
   rhs_f32(P, st.b, s, h, w, rhs);
   float v[3];
@@ -455,9 +468,9 @@ __global__ void __launch_bounds__(kBlock) heun_correct_f32(const __grid_constant
   float w[3];
   noise_f32(P, R, me.r, st.b, me.i, step, w);
   float h[3], r0[3], r1[3];
-  field_f32(P, R, st, me.gi, SP, p, h);
+  field_f32(P, R, st, me.gi, SP, p, h, P.hdip32);
   rhs_f32(P, st.b, p, h, w, r1);
-  field_f32(P, R, st, me.gi, S0, a, h);
+  field_f32(P, R, st, me.gi, S0, a, h, P.hdip32_s0);
   rhs_f32(P, st.b, a, h, w, r0);
   const float hdt = 0.5f * P.dt32;
   float v[3];
@@ -484,7 +497,7 @@ __global__ void __launch_bounds__(kBlock) heun_predict_f64(const __grid_constant
   const Planes<const double> S = planes(s0, P.npad);
   const double s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
   double h[3], w[3], rhs[3];
-  field_f64(P, R, st, me.gi, S, s, h);
+  field_f64(P, R, st, me.gi, S, s, h, P.hdip64);
   noise_f64(P, R, me.r, st.b, me.i, step, w);
   rhs_f64(P, st.b, R.thermal != 0, s, h, w, rhs);
   const Planes<double> D = planes(ds, P.npad);
@@ -514,7 +527,7 @@ __global__ void __launch_bounds__(kBlock) heun_correct_f64(const __grid_constant
   const Planes<const double> SP = planes(sp, P.npad);
   const double p[3] = {SP.x[me.gi], SP.y[me.gi], SP.z[me.gi]};
   double h[3], w[3], rhs[3];
-  field_f64(P, R, st, me.gi, SP, p, h);
+  field_f64(P, R, st, me.gi, SP, p, h, P.hdip64);
   noise_f64(P, R, me.r, st.b, me.i, step, w);
   rhs_f64(P, st.b, R.thermal != 0, p, h, w, rhs);
   const Planes<const double> S0 = planes(s0, P.npad);
@@ -552,7 +565,7 @@ __global__ void __launch_bounds__(kBlock) rk4_stage_f32(const __grid_constant__ 
   const Planes<const float> SI = planes(sin, P.npad);
   const float s[3] = {SI.x[me.gi], SI.y[me.gi], SI.z[me.gi]};
   float h[3], w[3], k[3];
-  field_f32(P, R, st, me.gi, SI, s, h);
+  field_f32(P, R, st, me.gi, SI, s, h, P.hdip32);
   noise_f32(P, R, me.r, st.b, me.i, step, w);
   rhs_f32(P, st.b, s, h, w, k);
   const Planes<const float> S0 = planes(s0, P.npad);
@@ -604,7 +617,7 @@ __global__ void __launch_bounds__(kBlock) rk4_stage_f64(const __grid_constant__ 
   const Planes<const double> SI = planes(sin, P.npad);
   const double s[3] = {SI.x[me.gi], SI.y[me.gi], SI.z[me.gi]};
   double h[3], w[3], k[3];
-  field_f64(P, R, st, me.gi, SI, s, h);
+  field_f64(P, R, st, me.gi, SI, s, h, P.hdip64);
   noise_f64(P, R, me.r, st.b, me.i, step, w);
   rhs_f64(P, st.b, R.thermal != 0, s, h, w, k);
   const Planes<const double> S0 = planes(s0, P.npad);
@@ -696,7 +709,7 @@ __global__ void __launch_bounds__(kBlock) fields_f32(const __grid_constant__ Par
   const Planes<const float> S = planes(s0, P.npad);
   const float s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
   float h[3];
-  field_f32(P, R, st, me.gi, S, s, h);
+  field_f32(P, R, st, me.gi, S, s, h, P.hdip32);
   out[3 * (int64_t)me.i] = h[0];
   out[3 * (int64_t)me.i + 1] = h[1];
   out[3 * (int64_t)me.i + 2] = h[2];
@@ -712,7 +725,7 @@ __global__ void __launch_bounds__(kBlock) fields_f64(const __grid_constant__ Par
   const Planes<const double> S = planes(s0, P.npad);
   const double s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
   double h[3];
-  field_f64(P, R, st, me.gi, S, s, h);
+  field_f64(P, R, st, me.gi, S, s, h, P.hdip64);
   out[3 * (int64_t)me.i] = h[0];
   out[3 * (int64_t)me.i + 1] = h[1];
   out[3 * (int64_t)me.i + 2] = h[2];

@@ -96,6 +96,12 @@ __global__ void __launch_bounds__(kBlock) observe_kernel(const __grid_constant__
         const double Sw = u[6] * sv[0] + u[7] * sv[1] + u[8] * sv[2];
         const double Su2 = Su * Su, Sv2 = Sv * Sv, Sw2 = Sw * Sw;
         e = T.order == 1 ? -T.K[b] * (Su2 * Sv2 + Sv2 * Sw2 + Sw2 * Su2) : -T.K[b] * (Su2 * Sv2 * Sw2);
+      } else if (T.kind == kDipole) {
+        // -1/2 S . h_dip   (cuda_dipole_fft.cu:156-167); planes computed for s
+        const Real* hd = dipole_planes<Real>(P);
+        if (hd)
+          e = -0.5 * (sv[0] * (double)hd[gi] + sv[1] * (double)hd[P.npad + gi] +
+                      sv[2] * (double)hd[2 * P.npad + gi]);
       } else {
         // -S . (mu_s B)   (applied_field.cc:150-155)
         e = -(sv[0] * mu * R.B[0] + sv[1] * mu * R.B[1] + sv[2] * mu * R.B[2]);

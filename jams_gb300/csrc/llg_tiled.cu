@@ -355,7 +355,8 @@ __device__ __forceinline__ void exchange_dispatch(int b, const TiledParams& TP, 
 // total field (meV) of the thread's spin from ring `ring`
 template <class F, int TZ, int TY>
 __device__ __forceinline__ void field_tiled(const LocalField& L, const TiledParams& TP, int b, const float4* ring,
-                                           int xs, int own, float h[3], float s[3]) {
+                                           int xs, int own, float h[3], float s[3], bool has_dip,
+                                           const float dip[3]) {
   using G = Geo<F, TZ, TY>;
   const float4 c = ring[(xs & 3) * G::PLANE + own + b * G::PY * G::PZ];
   s[0] = c.x;
@@ -364,6 +365,10 @@ __device__ __forceinline__ void field_tiled(const LocalField& L, const TiledPara
   float hi[3], lo[3];
   exchange_dispatch<F, TZ, TY>(b, TP, ring, xs, own, hi, lo);
   local_terms(L, s, hi, lo);
+  if (has_dip) {   // the dipole field of this spin, precomputed by FFT convolution
+#pragma unroll
+    for (int m = 0; m < 3; ++m) lo[m] = fa(lo[m], dip[m]);
+  }
 #pragma unroll
   for (int m = 0; m < 3; ++m) h[m] = hi[m] + lo[m];
 }
@@ -489,6 +494,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
   const uint64_t step = *P.step_base + kstep;
   const float* gather_src = STAGE == 0 ? s0 : sin;
   const LocalField L = local_field(P, R, b, TP.exch_term);
+  const bool has_dip = P.hdip32 != nullptr;
   const float dt = P.dt32;
   const int yz = y * V.st[1] + z * V.st[2] + b;
   // planes of this replica (outputs, stored rhs / k sum, own start state)
@@ -546,8 +552,18 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
         own_r[1] = ay[i];
         own_r[2] = az[i];
       }
+      // dipole field of the spin (input state; s0 for the recomputed rhs)
+      float dip[3] = {0.f, 0.f, 0.f}, dip0[3] = {0.f, 0.f, 0.f};
+      if (has_dip) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) dip[m] = __ldg(P.hdip32 + m * P.npad + V.offset + i);
+        if (STAGE == 1) {
+#pragma unroll
+          for (int m = 0; m < 3; ++m) dip0[m] = __ldg(P.hdip32_s0 + m * P.npad + V.offset + i);
+        }
+      }
       float h[3], s[3], k[3];
-      field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own, h, s);
+      field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own, h, s, has_dip, dip);
       llg_rhs_t(L, s, h, w, k);
       if (STAGE == 0) {
         float v[3] = {ff(dt, k[0], s[0]), ff(dt, k[1], s[1]), ff(dt, k[2], s[2])};
@@ -564,7 +580,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
         float a[3], r0[3];
         if (STAGE == 1) {
           float h0[3];
-          field_tiled<F, TZ, TY>(L, TP, b, ring1, x, own, h0, a);
+          field_tiled<F, TZ, TY>(L, TP, b, ring1, x, own, h0, a, has_dip, dip0);
           llg_rhs_t(L, a, h0, w, r0);
         } else {
 #pragma unroll

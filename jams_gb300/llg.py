@@ -17,7 +17,7 @@ from . import workloads as W
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libjams_llg.so")
 
-LLG_ABI_VERSION = 1
+LLG_ABI_VERSION = 2
 FP64 = 0
 FP32C = 1
 HEUN = 0
@@ -53,6 +53,9 @@ class LlgTerm(ctypes.Structure):
         ("T", ctypes.POINTER(ctypes.c_int32)), ("J", ctypes.POINTER(ctypes.c_double)),
         ("K", ctypes.POINTER(ctypes.c_double)), ("axis", ctypes.POINTER(ctypes.c_double)),
         ("B", ctypes.c_double * 3),
+        ("r_cutoff", ctypes.c_double), ("distance_tolerance", ctypes.c_double),
+        ("lattice_parameter", ctypes.c_double), ("lattice_vectors", ctypes.POINTER(ctypes.c_double)),
+        ("positions", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -208,6 +211,13 @@ class Solver:
                 lt.K, lt.axis = _dp(K), _dp(ax)
             for j in range(3):
                 lt.B[j] = float(t.B[j])
+            if t.kind == W.TERM_DIPOLE:
+                vec = np.ascontiguousarray(t.lattice_vectors, dtype=np.float64).reshape(-1)
+                pos = np.ascontiguousarray(t.positions, dtype=np.float64).reshape(-1)
+                self._keep += [vec, pos]
+                lt.r_cutoff, lt.distance_tolerance = float(t.r_cutoff), float(t.distance_tolerance)
+                lt.lattice_parameter = float(t.lattice_parameter)
+                lt.lattice_vectors, lt.positions = _dp(vec), _dp(pos)
         reps = (LlgReplica * len(workload.replicas))()
         for r, rp in enumerate(workload.replicas):
             for j in range(3):

@@ -36,6 +36,7 @@ TERM_EXCHANGE = 0
 TERM_UNIAXIAL = 1
 TERM_CUBIC = 2
 TERM_APPLIED_FIELD = 3
+TERM_DIPOLE = 4
 
 HEUN = 0
 RK4 = 1
@@ -58,6 +59,13 @@ class Term:
     axis: Optional[np.ndarray] = None  # float64 (nb, 3) or (nb, 3, 3)
     # applied field
     B: Sequence[float] = (0.0, 0.0, 0.0)
+    # dipole: cutoff and tolerance in lattice parameters, lattice parameter (m),
+    # lattice vectors (rows, lattice parameters), fractional basis positions
+    r_cutoff: float = 0.0
+    distance_tolerance: float = 1e-4
+    lattice_parameter: float = 0.0
+    lattice_vectors: Optional[np.ndarray] = None  # (3, 3)
+    positions: Optional[np.ndarray] = None  # (nb, 3)
     name: str = ""
 
 
@@ -141,6 +149,15 @@ def field_term(B) -> Term:
     return Term(kind=TERM_APPLIED_FIELD, B=tuple(float(b) for b in B), name="applied-field")
 
 
+def dipole_term(cell, basis_frac, r_cutoff: float, lattice_parameter: float, tolerance: float = 1e-4) -> Term:
+    """Dipole-dipole interaction within r_cutoff (lattice parameters); `cell`
+    holds the lattice vectors as columns (as Model.cell)."""
+    return Term(kind=TERM_DIPOLE, r_cutoff=float(r_cutoff), distance_tolerance=float(tolerance),
+                lattice_parameter=float(lattice_parameter),
+                lattice_vectors=np.ascontiguousarray(np.asarray(cell, dtype=np.float64).T),
+                positions=np.ascontiguousarray(basis_frac, dtype=np.float64).reshape(-1, 3), name="dipole")
+
+
 # --------------------------------------------------------------------------
 # lattices
 # --------------------------------------------------------------------------
@@ -211,12 +228,16 @@ def triangular_dmi_entries(J1: float, D: float):
 # --------------------------------------------------------------------------
 
 def sc_ferromagnet(L=32, steps=1000, T=0.0, seed=1, J=1.0, dz=0.1, B=(0.0, 0.0, 1.0),
-                   mu=2.0, alpha=0.1, t_step=1e-15, precision_note="") -> Workload:
+                   mu=2.0, alpha=0.1, t_step=1e-15, precision_note="", periodic=(1, 1, 1),
+                   dipole_cutoff=None, lattice_parameter=3.0e-10) -> Workload:
     """Simple-cubic ferromagnet, isotropic NN exchange J (meV), uniaxial K1 = dz
-    along z, Zeeman B (T), Heun, dt = 1 fs, random-sphere start."""
+    along z, Zeeman B (T), Heun, dt = 1 fs, random-sphere start; with
+    dipole_cutoff (lattice parameters) also the dipole-dipole term."""
     mus, gyro, al = material(mu, 1.0, alpha)
     terms = [exchange_term(sc_nn_entries(J)), uniaxial_term(1, dz), field_term(B)]
-    model = Model(nb=1, periodic=(1, 1, 1), mus=np.array([mus]), gyro=np.array([gyro]),
+    if dipole_cutoff:
+        terms.append(dipole_term(np.eye(3), np.zeros((1, 3)), dipole_cutoff, lattice_parameter))
+    model = Model(nb=1, periodic=tuple(periodic), mus=np.array([mus]), gyro=np.array([gyro]),
                   alpha=np.array([al]), terms=terms, t_step=t_step, integrator=HEUN,
                   cell=np.eye(3), basis_frac=np.zeros((1, 3)))
     Ls = (L, L, L) if np.isscalar(L) else tuple(L)
@@ -226,18 +247,25 @@ def sc_ferromagnet(L=32, steps=1000, T=0.0, seed=1, J=1.0, dz=0.1, B=(0.0, 0.0, 
                     description="simple-cubic FM, NN J=%g meV, K1=%g meV z, B=%s T, Heun" % (J, dz, B))
 
 
-def bcc_three_shell(L=64, steps=20000, T=300.0, seed=1, start="+z", t_step=0.5e-15) -> Workload:
+def bcc_three_shell(L=64, steps=20000, T=300.0, seed=1, start="+z", t_step=0.5e-15,
+                    dipole_cutoff=None, lattice_parameter=2.87e-10) -> Workload:
     """bcc, 2-site conventional basis, isotropic J1=2.0, J2=1.2, J3=-0.1 meV,
-    mu_s = 2.2 muB, cubic K1 = 0.005 meV (x, y, z axes), Heun alpha = 0.05."""
+    mu_s = 2.2 muB, cubic K1 = 0.005 meV (x, y, z axes), Heun alpha = 0.05;
+    with dipole_cutoff (lattice parameters) also the dipole-dipole term."""
     mus, gyro, al = material(2.2, 1.0, 0.05)
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0.5]], dtype=np.float64)
     terms = [exchange_term(bcc_shell_entries(2.0, 1.2, -0.1)), cubic_term(2, 0.005)]
+    desc = "bcc 2-site basis, J1=2.0 J2=1.2 J3=-0.1 meV, cubic K1=0.005 meV, Heun a=0.05 dt=0.5fs"
+    if dipole_cutoff:
+        terms.append(dipole_term(np.eye(3), basis, dipole_cutoff, lattice_parameter))
+        desc += ", dipole r_c=%g a" % dipole_cutoff
     model = Model(nb=2, periodic=(1, 1, 1), mus=np.full(2, mus), gyro=np.full(2, gyro),
                   alpha=np.full(2, al), terms=terms, t_step=t_step, integrator=HEUN,
-                  cell=np.eye(3), basis_frac=np.array([[0, 0, 0], [0.5, 0.5, 0.5]]))
+                  cell=np.eye(3), basis_frac=basis)
     Ls = (L, L, L) if np.isscalar(L) else tuple(L)
-    return Workload(name=f"bcc{Ls[0]}_3shell", model=model,
+    return Workload(name=f"bcc{Ls[0]}_3shell" + ("_dipole" if dipole_cutoff else ""), model=model,
                     replicas=[Replica(L=Ls, temperature=T)], steps=steps, seed=seed, start=start,
-                    description="bcc 2-site basis, J1=2.0 J2=1.2 J3=-0.1 meV, cubic K1=0.005 meV, Heun a=0.05 dt=0.5fs")
+                    description=desc)
 
 
 def bcc_nearest_neighbour(L=256, steps=2000, T=500.0, seed=1, start="+z", t_step=0.5e-15) -> Workload:
@@ -275,14 +303,16 @@ def sc_temperature_sweep(n_replicas=256, L_min=16, L_max=64, T_max=1200.0, steps
 
 
 def triangular_dmi_field_sweep(L=2048, n_fields=16, B_max=2.0, steps=5000, T=5.0, seed=1,
-                               t_step=1e-15) -> Workload:
+                               t_step=1e-15, dipole_cutoff=None, lattice_parameter=3.0e-10) -> Workload:
     """Triangular monolayer, tensor exchange J1 = 1.0 meV + interfacial DMI
     D = 0.3 meV, K1 = 0.2 meV z, mu_s = 2 muB, RK4 alpha = 0.3, one replica per
-    field B_z in 0..B_max."""
+    field B_z in 0..B_max; with dipole_cutoff also the dipole-dipole term."""
     mus, gyro, al = material(2.0, 1.0, 0.3)
     terms = [exchange_term(triangular_dmi_entries(1.0, 0.3)), uniaxial_term(1, 0.2),
              field_term((0.0, 0.0, 0.0))]
     cell = np.array([[1.0, 0.5, 0.0], [0.0, math.sqrt(3.0) / 2.0, 0.0], [0.0, 0.0, 1.0]])
+    if dipole_cutoff:
+        terms.append(dipole_term(cell, np.zeros((1, 3)), dipole_cutoff, lattice_parameter))
     model = Model(nb=1, periodic=(1, 1, 0), mus=np.array([mus]), gyro=np.array([gyro]),
                   alpha=np.array([al]), terms=terms, t_step=t_step, integrator=RK4,
                   cell=cell, basis_frac=np.zeros((1, 3)))

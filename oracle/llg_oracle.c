@@ -23,6 +23,9 @@
 
 /* src/jams/helpers/consts.h:32 */
 static const double kBoltzmannIU = 0.0861733326;
+/* src/jams/helpers/consts.h:35,38: mu0 in internal units (4 pi 1e-7 / kJoule2meV) */
+static const double kPi = 3.14159265358979323846;
+static const double kJoule2meV = 6.24150907e21;
 
 static char g_err[512];
 
@@ -160,12 +163,27 @@ typedef struct {
   int64_t nnz;
 } csr_t;
 
+/* dipole term: for basis site b, entries start[b] .. start[b+1]-1 of the
+   source sites (basis bj at cell offset d) within the cutoff and their
+   tensors w (xx, xy, xz, yy, yz, zz) x mu0 / (4 pi a^3) */
+typedef struct {
+  int32_t bj;
+  int32_t d[3];
+  double w[6];
+} dip_entry_t;
+
+typedef struct {
+  int64_t start[9];   /* nb + 1 <= 9 */
+  dip_entry_t *e;
+} dip_t;
+
 struct orc_sim {
   orc_model m;
   int64_t n;
   int32_t nt;
   orc_term *terms;
   csr_t *csr;        /* one per term (only exchange terms are filled) */
+  dip_t *dip;        /* one per term (only dipole terms are filled) */
   /* per-spin parameter arrays, as globals::mus/gyro/alpha */
   double *mus, *gyro, *alpha, *sigma;
   /* scratch */
@@ -288,6 +306,103 @@ static int build_exchange_csr(orc_sim *s, const orc_term *t, csr_t *out) {
   return err;
 }
 
+/* inradius of the periodic part of the supercell (lattice parameters):
+   jams::maximum_interaction_length, src/jams/core/lattice.cc:1155-1200 */
+static double cross_norm(const double *a, const double *b) {
+  const double c0 = a[1] * b[2] - a[2] * b[1], c1 = a[2] * b[0] - a[0] * b[2], c2 = a[0] * b[1] - a[1] * b[0];
+  return sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+}
+
+static double vnorm(const double *a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
+
+static double max_interaction_radius(const orc_model *m, const double *A) {
+  double v[3][3];
+  for (int k = 0; k < 3; ++k)
+    for (int c = 0; c < 3; ++c) v[k][c] = m->L[k] * A[3 * k + c];
+  const int p0 = m->periodic[0] != 0, p1 = m->periodic[1] != 0, p2 = m->periodic[2] != 0;
+  if (p0 && p1 && p2) {
+    const double c0 = v[1][1] * v[2][2] - v[1][2] * v[2][1], c1 = v[1][2] * v[2][0] - v[1][0] * v[2][2],
+                 c2 = v[1][0] * v[2][1] - v[1][1] * v[2][0];
+    const double vol = fabs(v[0][0] * c0 + v[0][1] * c1 + v[0][2] * c2);
+    double h = vol / cross_norm(v[1], v[2]);
+    if (vol / cross_norm(v[2], v[0]) < h) h = vol / cross_norm(v[2], v[0]);
+    if (vol / cross_norm(v[0], v[1]) < h) h = vol / cross_norm(v[0], v[1]);
+    return 0.5 * h;
+  }
+  if (p0 + p1 + p2 == 2) {
+    const double *a = p0 ? v[0] : v[1];
+    const double *b = p2 ? v[2] : v[1];
+    const double area = cross_norm(a, b);
+    const double h1 = area / vnorm(a), h2 = area / vnorm(b);
+    return 0.5 * (h1 < h2 ? h1 : h2);
+  }
+  if (p0 + p1 + p2 == 1) return 0.5 * vnorm(p0 ? v[0] : (p1 ? v[1] : v[2]));
+  double d[3] = {v[0][0] + v[1][0] + v[2][0], v[0][1] + v[1][1] + v[2][1], v[0][2] + v[1][2] + v[2][2]};
+  return vnorm(d);
+}
+
+/* every source site within r_cutoff + distance_tolerance of each basis site:
+   the real-space tensor the reference's FFT term builds
+   (src/jams/hamiltonian/dipole_fft.cc:205-265), listed per target site */
+static int build_dipole(orc_sim *s, const orc_term *tm, dip_t *out) {
+  const orc_model *m = &s->m;
+  if (m->nb > 8) return fail("dipole: at most 8 basis sites");
+  if (!tm->lattice_vectors || !tm->positions || !(tm->lattice_parameter > 0.0) || !(tm->r_cutoff > 0.0))
+    return fail("dipole: lattice vectors, positions, lattice parameter and r_cutoff are required");
+  const double *A = tm->lattice_vectors;
+  if (tm->r_cutoff > max_interaction_radius(m, A))
+    return fail("dipole: r_cutoff is larger than the inradius of the periodic supercell");
+  const double rc = tm->r_cutoff + tm->distance_tolerance;
+  const double a = tm->lattice_parameter;
+  const double w0 = (4.0 * kPi * 1e-7 / kJoule2meV) / (4.0 * kPi * a * a * a);
+  int lo[3], hi[3];
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = m->periodic[k] ? 0 : -(m->L[k] - 1);
+    hi[k] = m->L[k] - 1;
+  }
+  size_t cap = 1024, n = 0;
+  out->e = malloc(cap * sizeof(dip_entry_t));
+  for (int bi = 0; bi < m->nb; ++bi) {
+    out->start[bi] = (int64_t)n;
+    const double *fi = tm->positions + 3 * bi;
+    for (int bj = 0; bj < m->nb; ++bj) {
+      const double *fj = tm->positions + 3 * bj;
+      for (int d0 = lo[0]; d0 <= hi[0]; ++d0)
+        for (int d1 = lo[1]; d1 <= hi[1]; ++d1)
+          for (int d2 = lo[2]; d2 <= hi[2]; ++d2) {
+            const int d[3] = {d0, d1, d2};
+            if (d0 == 0 && d1 == 0 && d2 == 0 && bi == bj) continue;   /* self */
+            double x[3];
+            for (int k = 0; k < 3; ++k) {
+              x[k] = d[k] + fj[k] - fi[k];
+              if (m->periodic[k]) x[k] -= m->L[k] * floor(x[k] / m->L[k] + 0.5);
+            }
+            double r[3];
+            for (int c = 0; c < 3; ++c) r[c] = x[0] * A[c] + x[1] * A[3 + c] + x[2] * A[6 + c];
+            const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+            if (!(r2 > 0.0)) return fail("dipole: two sites at the same position");
+            if (r2 > rc * rc) continue;
+            const double r5 = pow(sqrt(r2), 5);
+            if (n == cap) {
+              cap *= 2;
+              out->e = realloc(out->e, cap * sizeof(dip_entry_t));
+            }
+            dip_entry_t *e = &out->e[n++];
+            e->bj = bj;
+            for (int k = 0; k < 3; ++k) e->d[k] = d[k];
+            e->w[0] = w0 * (3.0 * r[0] * r[0] - r2) / r5;
+            e->w[1] = w0 * (3.0 * r[0] * r[1]) / r5;
+            e->w[2] = w0 * (3.0 * r[0] * r[2]) / r5;
+            e->w[3] = w0 * (3.0 * r[1] * r[1] - r2) / r5;
+            e->w[4] = w0 * (3.0 * r[1] * r[2]) / r5;
+            e->w[5] = w0 * (3.0 * r[2] * r[2] - r2) / r5;
+          }
+    }
+  }
+  out->start[m->nb] = (int64_t)n;
+  return 0;
+}
+
 void orc_destroy(orc_sim *s) {
   if (!s) return;
   if (s->csr) {
@@ -297,6 +412,10 @@ void orc_destroy(orc_sim *s) {
       free(s->csr[t].vals);
     }
     free(s->csr);
+  }
+  if (s->dip) {
+    for (int t = 0; t < s->nt; ++t) free(s->dip[t].e);
+    free(s->dip);
   }
   free(s->terms);
   free(s->mus); free(s->gyro); free(s->alpha); free(s->sigma);
@@ -322,6 +441,7 @@ int orc_create(const orc_model *m, orc_sim **out) {
   s->terms = calloc((size_t)(s->nt > 0 ? s->nt : 1), sizeof(orc_term));
   memcpy(s->terms, m->terms, sizeof(orc_term) * (size_t)s->nt);
   s->csr = calloc((size_t)(s->nt > 0 ? s->nt : 1), sizeof(csr_t));
+  s->dip = calloc((size_t)(s->nt > 0 ? s->nt : 1), sizeof(dip_t));
   const int64_t n = s->n, n3 = 3 * n;
   s->mus = malloc(sizeof(double) * n);
   s->gyro = malloc(sizeof(double) * n);
@@ -354,6 +474,11 @@ int orc_create(const orc_model *m, orc_sim **out) {
       if (!(tm->order == 1 || tm->order == 2)) {
         orc_destroy(s);
         return fail("cubic order must be 1 or 2");
+      }
+    } else if (tm->kind == ORC_TERM_DIPOLE) {
+      if (build_dipole(s, tm, &s->dip[t]) != 0) {
+        orc_destroy(s);
+        return -1;
       }
     } else if (tm->kind != ORC_TERM_APPLIED_FIELD) {
       orc_destroy(s);
@@ -436,6 +561,34 @@ static void term_field(const orc_sim *s, int t, const double *spins, int64_t i,
         }
         f[j] = fj;
       }
+      break;
+    }
+    case ORC_TERM_DIPOLE: {
+      /* h_i = mu_i sum_j mu_j w_ij . s_j (dipole_bruteforce.cc:96-116) */
+      const dip_t *dp = &s->dip[t];
+      const int64_t ci = i / s->m.nb;
+      int c[3];
+      c[2] = (int)(ci % s->m.L[2]);
+      c[1] = (int)((ci / s->m.L[2]) % s->m.L[1]);
+      c[0] = (int)(ci / ((int64_t)s->m.L[2] * s->m.L[1]));
+      double acc[3] = {0.0, 0.0, 0.0};
+      for (int64_t k = dp->start[b]; k < dp->start[b + 1]; ++k) {
+        const dip_entry_t *e = &dp->e[k];
+        int cj[3], ok = 1;
+        for (int l = 0; l < 3; ++l) {
+          cj[l] = c[l] + e->d[l];
+          if (s->m.periodic[l]) cj[l] = ((cj[l] % s->m.L[l]) + s->m.L[l]) % s->m.L[l];
+          else if (cj[l] < 0 || cj[l] >= s->m.L[l]) ok = 0;
+        }
+        if (!ok) continue;
+        const int64_t j = site_index(s, cj[0], cj[1], cj[2], e->bj);
+        const double *sj = spins + 3 * j;
+        const double muj = s->mus[j];
+        acc[0] += muj * (e->w[0] * sj[0] + e->w[1] * sj[1] + e->w[2] * sj[2]);
+        acc[1] += muj * (e->w[1] * sj[0] + e->w[3] * sj[1] + e->w[4] * sj[2]);
+        acc[2] += muj * (e->w[2] * sj[0] + e->w[4] * sj[1] + e->w[5] * sj[2]);
+      }
+      for (int l = 0; l < 3; ++l) f[l] = s->mus[i] * acc[l];
       break;
     }
     default: { /* ORC_TERM_APPLIED_FIELD: src/jams/hamiltonian/applied_field.cc:146-148 */
@@ -653,6 +806,11 @@ int orc_energies(orc_sim *s, const double *spins, double t, double *e_terms) {
           else e += -tm->K[b] * (Su2 * Sv2 * Sw2);
           break;
         }
+        case ORC_TERM_DIPOLE:
+          /* -1/2 sum s.h (cuda_dipole_fft.cu:156-167) */
+          term_field(s, tt, spins, i, f);
+          e += -(sp[0] * f[0] + sp[1] * f[1] + sp[2] * f[2]);
+          break;
         default:
           /* applied_field.cc:150-155 */
           term_field(s, tt, spins, i, f);
@@ -660,7 +818,7 @@ int orc_energies(orc_sim *s, const double *spins, double t, double *e_terms) {
           break;
       }
     }
-    if (tm->kind == ORC_TERM_EXCHANGE) e = 0.5 * e;
+    if (tm->kind == ORC_TERM_EXCHANGE || tm->kind == ORC_TERM_DIPOLE) e = 0.5 * e;
     e_terms[tt] = e;
   }
   return 0;

@@ -26,6 +26,11 @@
  *                src/jams/cuda/cuda_spin_ops.cu:4-27
  *   - thermal noise amplitude: src/jams/solvers/cpu_llg_heun.cc:36-43,
  *                src/jams/thermostats/cuda_thermostat_classical.cc:33-45
+ *   - dipole field and energy, as the sum the FFT term convolves:
+ *       src/jams/hamiltonian/dipole_fft.cc:205-265 (tensor within
+ *       r_cutoff + distance_tolerance, self term excluded),
+ *       src/jams/hamiltonian/dipole_bruteforce.cc:80-119 (field formula),
+ *       src/jams/core/lattice.cc:1155-1200 (cutoff <= supercell inradius)
  *   - magnetisation / energies: src/jams/monitors/magnetisation.cc:77-104,
  *                src/jams/hamiltonian/sparse_interaction.cc:86-100
  *
@@ -51,7 +56,8 @@ enum {
   ORC_TERM_EXCHANGE = 0,
   ORC_TERM_UNIAXIAL = 1,
   ORC_TERM_CUBIC = 2,
-  ORC_TERM_APPLIED_FIELD = 3
+  ORC_TERM_APPLIED_FIELD = 3,
+  ORC_TERM_DIPOLE = 4
 };
 
 enum { ORC_HEUN = 0, ORC_RK4 = 1 };
@@ -72,6 +78,14 @@ typedef struct {
   const double *axis;
   /* applied field in tesla */
   double B[3];
+  /* dipole: cutoff and tolerance in lattice parameters, lattice parameter in
+     metres, lattice vectors (rows, lattice parameters), fractional basis
+     positions (3 nb) */
+  double r_cutoff;
+  double distance_tolerance;
+  double lattice_parameter;
+  const double *lattice_vectors;
+  const double *positions;
 } orc_term;
 
 typedef struct {

@@ -32,6 +32,11 @@ class OrcTerm(ctypes.Structure):
         ("K", ctypes.POINTER(ctypes.c_double)),
         ("axis", ctypes.POINTER(ctypes.c_double)),
         ("B", ctypes.c_double * 3),
+        ("r_cutoff", ctypes.c_double),
+        ("distance_tolerance", ctypes.c_double),
+        ("lattice_parameter", ctypes.c_double),
+        ("lattice_vectors", ctypes.POINTER(ctypes.c_double)),
+        ("positions", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -141,6 +146,13 @@ class _Packed:
                 B = rep.B
             for j in range(3):
                 ot.B[j] = float(B[j])
+            if t.kind == 4:   # dipole
+                vec = np.ascontiguousarray(t.lattice_vectors, dtype=np.float64).reshape(-1)
+                pos = np.ascontiguousarray(t.positions, dtype=np.float64).reshape(-1)
+                self.keep += [vec, pos]
+                ot.r_cutoff, ot.distance_tolerance = float(t.r_cutoff), float(t.distance_tolerance)
+                ot.lattice_parameter = float(t.lattice_parameter)
+                ot.lattice_vectors, ot.positions = _dp(vec), _dp(pos)
         self.terms = terms
         mus = np.ascontiguousarray(m.mus, dtype=np.float64)
         gyro = np.ascontiguousarray(m.gyro, dtype=np.float64)

@@ -93,7 +93,7 @@ def test_parser_comments_and_syntax(llg):
 
 @pytest.mark.parametrize("bad,msg", [
     ("lattice : { size = [4, 4, 4] ", "missing '}'"),
-    ('hamiltonians = ( { module = "dipole-fft"; } );', "not on the LLG hot path"),
+    ('hamiltonians = ( { module = "crystal-field"; } );', "not on the LLG hot path"),
     ('solver : { module = "monte-carlo-metropolis-cpu"; t_step = 1e-15; t_max = 1e-12; };', "unknown solver"),
 ])
 def test_config_errors_are_reported(llg, bad, msg):

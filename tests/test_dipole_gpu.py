@@ -1,0 +1,100 @@
+"""The dipole-dipole term on the GPU (FFT convolution, cuFFT transforms,
+this library's k-space product) against the oracle's direct sum: fields,
+energies and trajectories, periodic and open boundaries, Heun and RK4, both
+precisions, the tiled and the gather FP32 kernels."""
+import numpy as np
+import pytest
+
+from jams_gb300 import configs as C
+from jams_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+FP64_FIELD_TOL = 1e-12       # relative to the largest field component
+FP32C_FIELD_TOL = 2e-6
+FP64_RUN_TOL = 1e-10         # max |dS| after 100 T = 0 steps (FFT rounding, not bit-exact)
+FP32C_RUN_TOL = 1e-5         # max |dS| after 1000 T = 0 steps
+
+
+def cases():
+    return {
+        "bcc3_periodic": W.bcc_three_shell(L=(6, 5, 7), T=0.0, start="random", dipole_cutoff=2.4),
+        "sc_film_open_z": W.sc_ferromagnet(L=(8, 6, 3), periodic=(1, 1, 0), dipole_cutoff=2.2, B=(0, 0, 0.3)),
+        "triangular_rk4": W.triangular_dmi_field_sweep(L=(10, 12, 1), n_fields=2, T=0.0, dipole_cutoff=3.1),
+    }
+
+
+def start(w, r=0):
+    return W.initial_state(w, r)
+
+
+@pytest.mark.parametrize("name", sorted(cases()))
+@pytest.mark.parametrize("prec", ["FP64", "FP32C"])
+def test_dipole_fields_and_energies_match_oracle(llg, oracle, name, prec):
+    w = cases()[name]
+    s = llg.Solver(w, precision=getattr(llg, prec))
+    s0 = start(w)
+    s.set_state(s0, 0)
+    ref = oracle.OracleSim(w, 0)
+    want = ref.fields(s0)
+    got = s.fields(0)
+    tol = FP64_FIELD_TOL if prec == "FP64" else FP32C_FIELD_TOL
+    assert np.abs(got - want).max() <= tol * np.abs(want).max()
+    e_want = ref.energies(s0)
+    _, e_got = s.observables(0)
+    k = [t.kind for t in w.model.terms].index(W.TERM_DIPOLE)
+    np.testing.assert_allclose(e_got[k], e_want[k], rtol=1e-10 if prec == "FP64" else 1e-5)
+
+
+@pytest.mark.parametrize("name", sorted(cases()))
+def test_fp64_dipole_run_matches_oracle(llg, oracle, name):
+    w = cases()[name]
+    s = llg.Solver(w, precision=llg.FP64, steps_per_graph=16)
+    s0 = start(w)
+    s.set_state(s0, 0)
+    s.step(100)
+    ref = oracle.OracleSim(w, 0).run(s0, 100)
+    assert np.abs(s.get_state(0) - ref).max() <= FP64_RUN_TOL
+
+
+@pytest.mark.parametrize("name", sorted(cases()))
+def test_fp32c_dipole_run_within_bound(llg, oracle, name):
+    w = cases()[name]
+    s = llg.Solver(w, precision=llg.FP32C)
+    s0 = start(w)
+    s.set_state(s0, 0)
+    s.step(1000)
+    ref = oracle.OracleSim(w, 0).run(s0, 1000)
+    assert np.abs(s.get_state(0) - ref).max() <= FP32C_RUN_TOL
+
+
+def test_dipole_tilings_agree(llg):
+    """The tiled kernels add the FFT field like the other local terms: every
+    tiling gives the same state."""
+    w = W.bcc_three_shell(L=(6, 8, 10), T=300.0, start="random", dipole_cutoff=2.9)
+    outs = []
+    for tx, store, occ in [(2, False, 2), (4, True, 4), (10, True, 3)]:
+        s = llg.Solver(w, precision=llg.FP32C, steps_per_graph=4)
+        assert s.kernel_info()["family"] == "bcc3"
+        s.set_tuning(tx, store, occ)
+        s.set_state(start(w), 0)
+        s.step(9)
+        outs.append(s.get_state(0))
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+
+
+def test_dipole_from_config_equals_oracle(llg, oracle):
+    text = C.bcc_three_shell(L=5, T=0.0, spin='"random"', dipole_cutoff=2.4)
+    s = llg.Solver.from_config(text, precision=llg.FP64)
+    w = W.bcc_three_shell(L=5, T=0.0, dipole_cutoff=2.4)
+    s0 = s.get_state(0)
+    s.step(20)
+    ref = oracle.OracleSim(w, 0).run(s0, 20)
+    assert np.abs(s.get_state(0) - ref).max() <= FP64_RUN_TOL
+
+
+def test_dipole_cutoff_beyond_inradius_is_an_error(llg):
+    w = W.sc_ferromagnet(L=6, dipole_cutoff=3.5)
+    with pytest.raises(llg.LLGError, match="inradius"):
+        llg.Solver(w, precision=llg.FP32C)
