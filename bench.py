@@ -70,6 +70,10 @@ WORKLOADS = {
     "sc_sweep256": lambda: W.sc_temperature_sweep(),
     # triangular 2048^2 x 16 fields, tensor exchange + DMI, RK4, 5 K
     "tri2048_dmi_x16": lambda: W.triangular_dmi_field_sweep(),
+    # the headline and the 256^3 3-shell workloads with the dipole-dipole term
+    # (FFT convolution, r_c = 8 lattice parameters)
+    "bcc64_3shell_dipole": lambda: W.bcc_three_shell(L=64, T=300.0, start="+z", dipole_cutoff=8.0),
+    "bcc256_3shell_dipole": lambda: W.bcc_three_shell(L=256, T=500.0, steps=2000, dipole_cutoff=8.0),
     # profiling cases: state larger than L2 (129 MB) but a few GB on the device
     "bcc192_nn": lambda: W.bcc_nearest_neighbour(L=192, T=500.0),
     "bcc192_3shell": lambda: W.bcc_three_shell(L=192, T=500.0),
@@ -382,10 +386,14 @@ def main():
     # ---- per-stage kernel durations (same flush between steps)
     ns = len(STAGE_BYTES[(integ, args.precision)])
     stage_ms = np.zeros(ns)
+    dip_ms = np.zeros(ns)
     for _ in range(args.profile_steps):
         flush.fill_(1.0)
-        stage_ms += sol.profile_stages(1)[:ns]
+        k_ms, d_ms = sol.profile_stages(1, dipole=True)
+        stage_ms += k_ms
+        dip_ms += d_ms
     stage_ms /= args.profile_steps
+    dip_ms /= args.profile_steps
     dom = int(np.argmax(stage_ms))
     bytes_per_launch = STAGE_BYTES[(integ, args.precision)][dom] * n_spins
     achieved = bytes_per_launch / (stage_ms[dom] * 1e-3) / 1e9
@@ -405,6 +413,14 @@ def main():
                 "algorithmic_bytes_per_spin_step": int(sum(STAGE_BYTES[(integ, args.precision)])),
                 "step_frac": (sum(STAGE_BYTES[(integ, args.precision)]) * n_spins / (ms_per_step * 1e-3) / 1e9)
                 / peak}
+
+    # ---- dipole term: FFT convolution before every stage (cuFFT transforms
+    # and this library's scatter / k-space product / gather kernels)
+    dipole = None
+    if any(t.kind == W.TERM_DIPOLE for t in w.model.terms):
+        dipole = {"ms_per_evaluation": float(dip_ms.mean()), "evaluations_per_step": ns,
+                  "share_of_stage_time": float(dip_ms.sum() / (dip_ms.sum() + stage_ms.sum())),
+                  "r_cutoff": next(t.r_cutoff for t in w.model.terms if t.kind == W.TERM_DIPOLE)}
 
     # ---- steady state without flush: blocks of 100 steps as CUDA graphs
     blk = 100
@@ -468,6 +484,7 @@ def main():
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         "steady_state_graph": steady, "wall_s_timed_region": t_wall,
         "final_abs_m": {"mean": float(np.mean([m for r in mags for m in r])), "ranks": len(mags)},
+        "dipole": dipole,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -217,9 +217,11 @@ int llg_set_stream(llg_handle *h, void *cuda_stream);
    llg_profile_stages call. */
 int64_t llg_last_launch_count(const llg_handle *h);
 
-/* Advances nsteps steps like llg_step, without graphs, with a CUDA event
-   pair around every stage kernel; ms[k] = mean duration (ms) of stage k
-   (Heun: predictor, corrector; RK4: stages 1-4).  Synchronous. */
+/* Advances nsteps steps like llg_step, without graphs, with CUDA events
+   around every stage; ms holds 2 x stages values: ms[k] = mean duration (ms)
+   of the kernel of stage k (Heun: predictor, corrector; RK4: stages 1-4),
+   ms[stages + k] = the dipole-field evaluation (FFT convolution) before it,
+   0 without a dipole term.  Synchronous. */
 int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
 
 /* Kernel selection of the handle: info[0] stencil family of the tiled FP32

@@ -822,7 +822,7 @@ int num_stages(const llg_handle* h) { return h->integrator == LLG_HEUN ? 2 : 4; 
 
 // launches stage `stage` of step `ks` of a block; `cur` is the buffer that
 // holds the state at the start of the step (FP32 Heun alternates 0 and 2)
-void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur) {
+void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t after_dipole = nullptr) {
   // the stage's input state (whose dipole field the stage needs)
   const void* input;
   if (h->integrator == LLG_HEUN)
@@ -830,6 +830,7 @@ void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur) {
   else
     input = stage == 0 ? h->state[0].p : (stage == 2 ? h->state[2].p : h->state[1].p);
   const Params P = launch_params(h, input, (h->integrator == LLG_HEUN && stage == 1) ? 1 : 0);
+  if (after_dipole) cudaEventRecord(after_dipole, h->stream);
   const unsigned grid = (unsigned)P.ntiles;
   cudaStream_t st = h->stream;
   if (h->tiled) {
@@ -1309,7 +1310,8 @@ int llg_profile_stages(llg_handle* h, int32_t nsteps, double* ms) {
   int rc = sync_replicas(h);
   if (rc) return rc;
   const int ns = num_stages(h);
-  std::vector<cudaEvent_t> ev((size_t)nsteps * ns * 2);
+  // per stage: start, after the dipole field evaluation, end
+  std::vector<cudaEvent_t> ev((size_t)nsteps * ns * 3);
   for (auto& e : ev) {
     cudaError_t ce = cudaEventCreate(&e);
     if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaEventCreate");
@@ -1317,9 +1319,10 @@ int llg_profile_stages(llg_handle* h, int32_t nsteps, double* ms) {
   int cur = h->cur;
   for (int k = 0; k < nsteps; ++k) {
     for (int stg = 0; stg < ns; ++stg) {
-      cudaEventRecord(ev[((size_t)k * ns + stg) * 2], h->stream);
-      launch_stage(h, stg, (uint32_t)k, cur);
-      cudaEventRecord(ev[((size_t)k * ns + stg) * 2 + 1], h->stream);
+      cudaEvent_t* e = &ev[((size_t)k * ns + stg) * 3];
+      cudaEventRecord(e[0], h->stream);
+      launch_stage(h, stg, (uint32_t)k, cur, e[1]);
+      cudaEventRecord(e[2], h->stream);
     }
     cur = next_buffer(h, cur);
   }
@@ -1329,14 +1332,22 @@ int llg_profile_stages(llg_handle* h, int32_t nsteps, double* ms) {
   h->last_launches = (int64_t)nsteps * ns + 1;
   cudaError_t ce = cudaStreamSynchronize(h->stream);
   if (ce != cudaSuccess) return h->cuda_fail(ce, "profiling stages");
-  for (int stg = 0; stg < ns; ++stg) ms[stg] = 0.0;
+  for (int stg = 0; stg < 2 * ns; ++stg) ms[stg] = 0.0;
   for (int k = 0; k < nsteps; ++k)
     for (int stg = 0; stg < ns; ++stg) {
+      const cudaEvent_t* e = &ev[((size_t)k * ns + stg) * 3];
       float t = 0.f;
-      cudaEventElapsedTime(&t, ev[((size_t)k * ns + stg) * 2], ev[((size_t)k * ns + stg) * 2 + 1]);
+      cudaEventElapsedTime(&t, e[1], e[2]);
       ms[stg] += t / nsteps;
+      cudaEventElapsedTime(&t, e[0], e[1]);
+      ms[ns + stg] += t / nsteps;
     }
   for (auto& e : ev) cudaEventDestroy(e);
+  if (!h->async_err.empty()) {
+    const std::string e = h->async_err;
+    h->async_err.clear();
+    return h->fail(LLG_ERR_CUDA, "%s", e.c_str());
+  }
   return 0;
 }
 

@@ -365,12 +365,14 @@ class Solver:
     def set_stream(self, stream_ptr: int) -> None:
         self._check(self.L.llg_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
 
-    def profile_stages(self, nsteps: int) -> np.ndarray:
-        """Mean duration (ms) of each stage kernel over nsteps steps."""
-        ms = np.zeros(4)
+    def profile_stages(self, nsteps: int, dipole: bool = False):
+        """Mean duration (ms) of each stage kernel over nsteps steps; with
+        dipole=True also the dipole-field evaluation before each stage."""
+        ms = np.zeros(8)
         self._check(self.L.llg_profile_stages(self.h, int(nsteps), _dp(ms)))
         integ = self.workload.model.integrator if self.workload is not None else self._integrator
-        return ms[: 2 if integ == W.HEUN else 4]
+        ns = 2 if integ == W.HEUN else 4
+        return (ms[:ns], ms[ns:2 * ns]) if dipole else ms[:ns]
 
     def kernel_info(self) -> dict:
         info = (ctypes.c_int32 * 8)()
