@@ -8,7 +8,9 @@
 // src/jams/core/solver.cc, src/jams/hamiltonian/sparse_interaction.cc,
 // src/jams/hamiltonian/uniaxial_anisotropy.cc,
 // src/jams/hamiltonian/cubic_anisotropy.cc,
-// src/jams/hamiltonian/applied_field.cc, src/jams/core/physics.cc,
+// src/jams/hamiltonian/applied_field.cc,
+// src/jams/hamiltonian/dipole_bruteforce.cc, src/jams/lattice/minimum_image.cc,
+// src/jams/containers/cell.cc, src/jams/core/physics.cc,
 // src/jams/core/base.cc, src/jams/common.cc, and the header-only CSR builder
 // and Xcsrmv_general (src/jams/containers/sparse_matrix*.h,
 // src/jams/interface/sparse_blas.h).
@@ -16,7 +18,11 @@
 // Supplied here because their own translation units pull in spglib, HDF5,
 // FFTW or the whole plugin factory set:
 //   - globals storage (src/jams/core/globals.h with GLOBALORIGIN),
-//   - the handful of Lattice accessors the anisotropy terms call,
+//   - the handful of Lattice accessors the anisotropy and dipole terms call
+//     (lattice parameter, supercell, cartesian site positions, and the
+//     supercell inradius of jams::maximum_interaction_length,
+//     src/jams/core/lattice.cc:1155-1200, restated),
+//   - LAPACK's dgetrf_/dgetri_ for the Mat3 inverse (mat3.h:232-257),
 //   - the Hamiltonian base constructor (energy-unit lookup and name only,
 //     src/jams/core/hamiltonian.cc:116-165),
 //   - an exchange term that inserts 3x3 blocks for the neighbour list of an
@@ -41,7 +47,9 @@
 #include <jams/core/lattice.h>
 #include <jams/core/units.h>
 #include <jams/hamiltonian/applied_field.h>
+#include <jams/containers/cell.h>
 #include <jams/hamiltonian/cubic_anisotropy.h>
+#include <jams/hamiltonian/dipole_bruteforce.h>
 #include <jams/hamiltonian/sparse_interaction.h>
 #include <jams/hamiltonian/uniaxial_anisotropy.h>
 #include <jams/physics/empty.h>
@@ -55,12 +63,85 @@ extern "C" void cblas_daxpy(int n, double a, const double* x, int incx, double* 
   for (int i = 0; i < n; ++i) y[i * incy] += a * x[i * incx];
 }
 
+// LU factorisation with partial pivoting and the inverse from it, column-major
+// (the LAPACK routines the reference's Mat3 inverse calls)
+extern "C" void dgetrf_(const int* m, const int* n, double* a, const int* lda, int* ipiv, int* info) {
+  const int M = *m, N = *n, LD = *lda;
+  auto A = [&](int i, int j) -> double& { return a[i + j * LD]; };
+  *info = 0;
+  for (int k = 0; k < std::min(M, N); ++k) {
+    int p = k;
+    for (int i = k + 1; i < M; ++i)
+      if (std::fabs(A(i, k)) > std::fabs(A(p, k))) p = i;
+    ipiv[k] = p + 1;
+    if (A(p, k) == 0.0) {
+      if (!*info) *info = k + 1;
+      continue;
+    }
+    if (p != k)
+      for (int j = 0; j < N; ++j) std::swap(A(k, j), A(p, j));
+    for (int i = k + 1; i < M; ++i) A(i, k) /= A(k, k);
+    for (int j = k + 1; j < N; ++j)
+      for (int i = k + 1; i < M; ++i) A(i, j) -= A(i, k) * A(k, j);
+  }
+}
+
+extern "C" void dgetri_(const int* n, double* a, const int* lda, const int* ipiv, double* work, const int* lwork,
+                        int* info) {
+  const int N = *n, LD = *lda;
+  *info = 0;
+  if (*lwork == -1) {
+    work[0] = N;
+    return;
+  }
+  std::vector<double> inv((size_t)N * N);
+  for (int c = 0; c < N; ++c) {
+    std::vector<double> x(N, 0.0);
+    x[c] = 1.0;
+    for (int k = 0; k < N; ++k)
+      if (ipiv[k] - 1 != k) std::swap(x[k], x[ipiv[k] - 1]);
+    for (int i = 0; i < N; ++i)
+      for (int k = 0; k < i; ++k) x[i] -= a[i + k * LD] * x[k];
+    for (int i = N - 1; i >= 0; --i) {
+      for (int k = i + 1; k < N; ++k) x[i] -= a[i + k * LD] * x[k];
+      x[i] /= a[i + i * LD];
+    }
+    for (int i = 0; i < N; ++i) inv[i + (size_t)c * N] = x[i];
+  }
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i < N; ++i) a[i + j * LD] = inv[i + (size_t)j * N];
+}
+
 namespace {
 struct HarnessLattice {
   int L[3] = {1, 1, 1};
   int periodic[3] = {1, 1, 1};
   int nb = 1;
+  double a = 3e-10;                                  // lattice parameter (m)
+  double A[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};         // lattice vectors (rows)
+  std::vector<double> frac;                          // basis positions, 3 nb
+  Cell supercell;
+  std::vector<Vec3> pos;                             // cartesian site positions
 } g_lat;
+
+void build_geometry() {
+  Mat3 m;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) m[r][c] = g_lat.L[c] * g_lat.A[3 * c + r];
+  g_lat.supercell = Cell(m, Vec3b{g_lat.periodic[0] != 0, g_lat.periodic[1] != 0, g_lat.periodic[2] != 0});
+  g_lat.pos.clear();
+  for (int i = 0; i < g_lat.L[0]; ++i)
+    for (int j = 0; j < g_lat.L[1]; ++j)
+      for (int k = 0; k < g_lat.L[2]; ++k)
+        for (int b = 0; b < g_lat.nb; ++b) {
+          const double f[3] = {i + (g_lat.frac.empty() ? 0.0 : g_lat.frac[3 * b]),
+                               j + (g_lat.frac.empty() ? 0.0 : g_lat.frac[3 * b + 1]),
+                               k + (g_lat.frac.empty() ? 0.0 : g_lat.frac[3 * b + 2])};
+          Vec3 r;
+          for (int c = 0; c < 3; ++c) r[c] = f[0] * g_lat.A[c] + f[1] * g_lat.A[3 + c] + f[2] * g_lat.A[6 + c];
+          g_lat.pos.push_back(r);
+        }
+}
 
 std::string g_err;
 
@@ -70,7 +151,25 @@ std::string material_name_of_basis(int b) { return "M" + std::to_string(b); }
 // --- Lattice accessors used by the anisotropy terms (each basis site is its
 // own material "M<b>") ---
 Lattice::~Lattice() {}
-double Lattice::parameter() const { return 3e-10; }
+double Lattice::parameter() const { return g_lat.a; }
+const Cell& Lattice::get_supercell() { return g_lat.supercell; }
+double Lattice::max_interaction_radius() const {
+  const Vec3 v[3] = {g_lat.supercell.a1(), g_lat.supercell.a2(), g_lat.supercell.a3()};
+  auto cross_norm = [](const Vec3& x, const Vec3& y) { return norm(cross(x, y)); };
+  const int np = (g_lat.periodic[0] != 0) + (g_lat.periodic[1] != 0) + (g_lat.periodic[2] != 0);
+  if (np == 3) {
+    const double vol = std::fabs(dot(v[0], cross(v[1], v[2])));
+    return 0.5 * std::min(vol / cross_norm(v[1], v[2]), std::min(vol / cross_norm(v[2], v[0]), vol / cross_norm(v[0], v[1])));
+  }
+  if (np == 2) {
+    const Vec3& x = g_lat.periodic[0] ? v[0] : v[1];
+    const Vec3& y = g_lat.periodic[2] ? v[2] : v[1];
+    const double area = cross_norm(x, y);
+    return 0.5 * std::min(area / norm(x), area / norm(y));
+  }
+  if (np == 1) return 0.5 * norm(g_lat.periodic[0] ? v[0] : (g_lat.periodic[1] ? v[1] : v[2]));
+  return norm(v[0] + v[1] + v[2]);
+}
 int Lattice::num_basis_sites() const { return g_lat.nb; }
 int Lattice::num_materials() const { return g_lat.nb; }
 int Lattice::material_index(const std::string& name) const {
@@ -86,7 +185,7 @@ bool Lattice::material_exists(const std::string& name) const {
 int Lattice::lattice_site_material_id(int i) const { return i % g_lat.nb; }
 unsigned Lattice::lattice_site_basis_index(int i) const { return (unsigned)(i % g_lat.nb); }
 // reached only by Physics' "initial_state" option, which the harness never sets
-const Vec3& Lattice::lattice_site_position_cart(int) const { throw std::runtime_error("not available"); }
+const Vec3& Lattice::lattice_site_position_cart(int i) const { return g_lat.pos.at((size_t)i); }
 Vec3 Lattice::displacement(const Vec3&, const Vec3&) const { throw std::runtime_error("not available"); }
 
 // --- Hamiltonian base constructor: unit lookup and name ---
@@ -168,6 +267,16 @@ __attribute__((visibility("default"))) int ref_create(const orc_model* m, double
     g_lat.L[2] = m->L[2];
     g_lat.nb = m->nb;
     for (int l = 0; l < 3; ++l) g_lat.periodic[l] = m->periodic[l];
+    g_lat.a = 3e-10;
+    for (int c = 0; c < 9; ++c) g_lat.A[c] = c % 4 == 0 ? 1.0 : 0.0;
+    g_lat.frac.assign((size_t)3 * m->nb, 0.0);
+    for (int t = 0; t < m->n_terms; ++t)
+      if (m->terms[t].kind == ORC_TERM_DIPOLE) {
+        g_lat.a = m->terms[t].lattice_parameter;
+        for (int c = 0; c < 9; ++c) g_lat.A[c] = m->terms[t].lattice_vectors[c];
+        for (int c = 0; c < 3 * m->nb; ++c) g_lat.frac[c] = m->terms[t].positions[c];
+      }
+    build_geometry();
     globals::lattice = new Lattice();
     const int n = m->L[0] * m->L[1] * m->L[2] * m->nb;
     globals::num_spins = n;
@@ -235,6 +344,10 @@ __attribute__((visibility("default"))) int ref_create(const orc_model* m, double
         hs.add("module", Setting::string("applied-field"));
         hs.add("field", vec3(tm.B));
         g_solver->register_hamiltonian(new AppliedFieldHamiltonian(hs, n));
+      } else if (tm.kind == ORC_TERM_DIPOLE) {
+        hs.add("module", Setting::string("dipole-bruteforce"));
+        hs.add("r_cutoff", Setting::number(tm.r_cutoff));
+        g_solver->register_hamiltonian(new DipoleBruteforceHamiltonian(hs, n));
       } else {
         throw std::runtime_error("unknown term kind");
       }

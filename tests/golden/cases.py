@@ -1,4 +1,9 @@
-"""The small seeded workloads behind the golden fixtures (all T = 0, Heun)."""
+"""The small seeded workloads behind the golden fixtures (all T = 0, Heun).
+
+cases(): the reference's exchange, anisotropy and field terms; the FP64 form
+equals these bit for bit.  dipole_cases(): with the dipole-dipole term (the
+reference's dipole-bruteforce Hamiltonian); the FFT evaluation equals these
+within rounding, not bit for bit."""
 from jams_gb300 import workloads as W
 
 
@@ -22,4 +27,11 @@ def cases():
         "bcc4_nn_uniaxial_field": W.bcc_nearest_neighbour(L=4, T=0.0, start="random"),
         "tri8_dmi_tensor": _tri(),
         "sc6x5x4_open_x": _open_sc(),
+    }
+
+
+def dipole_cases():
+    return {
+        "bcc5x6x7_3shell_dipole": W.bcc_three_shell(L=(5, 6, 7), T=0.0, start="random", dipole_cutoff=2.4),
+        "sc6x5x3_film_dipole": W.sc_ferromagnet(L=(6, 5, 3), periodic=(1, 1, 0), dipole_cutoff=2.2),
     }

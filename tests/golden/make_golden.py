@@ -9,6 +9,9 @@ reference sources are present (the development container):
     make -f oracle/Makefile.ref REF=/root/reference
     python tests/golden/make_golden.py
 
+The dipole cases run the reference's dipole-bruteforce Hamiltonian
+(src/jams/hamiltonian/dipole_bruteforce.cc) compiled the same way.
+
 Each fixture holds, for a small seeded case at T = 0: the initial spins, the
 total field and per-term energies of the reference at those spins, and the
 reference's spins after 1, 10 and 100 Heun steps.  The reference's thermal
@@ -27,7 +30,7 @@ sys.path.insert(0, ROOT)
 
 from jams_gb300 import workloads as W  # noqa: E402
 from oracle import oracle as O  # noqa: E402
-from tests.golden.cases import cases  # noqa: E402
+from tests.golden.cases import cases, dipole_cases  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -35,7 +38,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 def main():
     if not O.reference_available():
         raise SystemExit("oracle/_ref/libjams_ref.so is missing: build it with oracle/Makefile.ref first")
-    for name, w in cases().items():
+    for name, w in {**cases(), **dipole_cases()}.items():
         s0 = W.initial_state(w, 0)
         ref = O.ReferenceSim(w)
         out = {"s0": s0, "fields": ref.fields(s0), "energies": ref.energies(s0)}

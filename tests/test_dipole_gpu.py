@@ -5,8 +5,13 @@ precisions, the tiled and the gather FP32 kernels."""
 import numpy as np
 import pytest
 
+import os
+
 from jams_gb300 import configs as C
 from jams_gb300 import workloads as W
+from tests.golden.cases import dipole_cases
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 pytestmark = pytest.mark.gpu
 
@@ -98,3 +103,21 @@ def test_dipole_cutoff_beyond_inradius_is_an_error(llg):
     w = W.sc_ferromagnet(L=6, dipole_cutoff=3.5)
     with pytest.raises(llg.LLGError, match="inradius"):
         llg.Solver(w, precision=llg.FP32C)
+
+
+@pytest.mark.parametrize("name", sorted(dipole_cases().keys()))
+@pytest.mark.parametrize("prec", ["FP64", "FP32C"])
+def test_dipole_against_reference_golden_vectors(llg, name, prec):
+    """Fixtures from the reference's dipole-bruteforce Hamiltonian and CPU
+    Heun solver compiled from its sources: fields and 100 Heun steps."""
+    w = dipole_cases()[name]
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    s = llg.Solver(w, precision=getattr(llg, prec), steps_per_graph=16)
+    s.set_state(g["s0"], 0)
+    h = s.fields(0)
+    tol = FP64_FIELD_TOL if prec == "FP64" else FP32C_FIELD_TOL
+    assert np.abs(h - g["fields"]).max() <= tol * np.abs(g["fields"]).max()
+    s.step(100)
+    run_tol = FP64_RUN_TOL if prec == "FP64" else FP32C_RUN_TOL
+    assert np.abs(s.get_state(0) - g["s100"]).max() <= run_tol
+

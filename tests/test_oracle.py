@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from jams_gb300 import workloads as W
-from tests.golden.cases import cases
+from tests.golden.cases import cases, dipole_cases
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -206,3 +206,23 @@ def test_topological_charge_of_uniform_and_skyrmion(oracle):
             s[i * L + j] = [math.sin(th) * math.cos(ph), math.sin(th) * math.sin(ph), math.cos(th)]
     q = oracle.topological_charge_triangular(s, L, L)
     assert abs(abs(q) - 1.0) < 0.05
+
+
+@pytest.mark.parametrize("name", sorted(dipole_cases().keys()))
+def test_oracle_dipole_matches_reference_golden_vectors(oracle, name):
+    """The dipole fixtures come from the reference's dipole-bruteforce
+    Hamiltonian (dipole_bruteforce.cc) compiled from its sources; the oracle's
+    direct sum differs from it only in summation order."""
+    w = dipole_cases()[name]
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    sim = oracle.OracleSim(w)
+    h = sim.fields(g["s0"])
+    assert np.abs(h - g["fields"]).max() <= 1e-14 * np.abs(g["fields"]).max()
+    np.testing.assert_allclose(sim.energies(g["s0"]), g["energies"], rtol=1e-13, atol=1e-16)
+    s = g["s0"]
+    done = 0
+    for k in (1, 10, 100):
+        s = sim.run(s, k - done, first_step=done)
+        done = k
+        assert np.abs(s - g["s%d" % k]).max() <= 1e-13, k
+
