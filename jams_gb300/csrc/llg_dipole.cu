@@ -9,7 +9,7 @@
 // M = L cells along periodic axes and 2L along open ones (zero padding turns
 // the circular convolution into the open-boundary sum; an open axis of one
 // cell needs none) and transformed once (D2Z).  A field evaluation is then
-//   scatter the spins onto the grid -> R2C -> h_i(q) = sum_j mu_j G_ij(q) S_j(q)
+//   scatter the spins onto the grid -> R2C -> h_i(q) = sum_j mu_j W_ij(q) S_j(q)
 //   -> C2R -> h_i = mu_i h_i(r) / prod(M) back into SoA planes,
 // the reference's sequence (cuda_dipole_fft.cu:184-209) with the tensor
 // normalised by the grid size as there.  cuFFT does the transforms; the
@@ -86,37 +86,78 @@ __global__ void __launch_bounds__(kDipBlock) dip_scatter(const Real* __restrict_
       grid[(int64_t)(c * nb + b) * Mtot + n] = in ? s[c * npad + offset + i0 + b] : Real(0);
 }
 
+// h_i(q) = sum_j mu_j W_ij(q) S_j(q) for every k-space point q.  W_ij is the
+// transform of a real tensor, so W_ji = conj(W_ij); W_ii is the transform of
+// a tensor even in the offset, so it is real.  Stored: wd, the six real
+// components (xx, xy, xz, yy, yz, zz) of every W_ii; wo, the six complex
+// components of every W_ij with i < j (pair index p in row order).
 template <class C>
-__device__ __forceinline__ C cmad(C acc, C a, C b) {
-  acc.x += a.x * b.x - a.y * b.y;
-  acc.y += a.x * b.y + a.y * b.x;
-  return acc;
+__device__ __forceinline__ void cmac_sym(C h[3], const C g[6], const C s[3], bool conj) {
+  // h += g s with g the symmetric 3x3 of six complex components (conj: of g*)
+  const int idx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+#pragma unroll
+  for (int m = 0; m < 3; ++m)
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      const C a = g[idx[m][n]];
+      const auto ai = conj ? -a.y : a.y;
+      h[m].x += a.x * s[n].x - ai * s[n].y;
+      h[m].y += a.x * s[n].y + ai * s[n].x;
+    }
 }
 
-// h_i(q) = sum_j mu_j G_ij(q) S_j(q) for every k-space point q; G holds the
-// six independent components xx, xy, xz, yy, yz, zz
-template <class C>
-__global__ void __launch_bounds__(kDipBlock) dip_convolve(const C* __restrict__ ks, const C* __restrict__ w,
-                                                          C* __restrict__ kh, int nb, int64_t Mq, MusArr mus) {
+template <class C, class Real, int NB>
+__global__ void __launch_bounds__(kDipBlock) dip_convolve(const C* __restrict__ ks, const Real* __restrict__ wd,
+                                                          const C* __restrict__ wo, C* __restrict__ kh, int64_t Mq,
+                                                          MusArr mus) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= Mq) return;
-  for (int i = 0; i < nb; ++i) {
-    C h[3];
-    for (int m = 0; m < 3; ++m) h[m].x = h[m].y = 0;
-    for (int j = 0; j < nb; ++j) {
-      C sj[3];
-      for (int m = 0; m < 3; ++m) {
-        sj[m] = ks[(int64_t)(m * nb + j) * Mq + q];
-        sj[m].x *= mus.v[j];
-        sj[m].y *= mus.v[j];
-      }
-      const C* g = w + (int64_t)((i * nb + j) * 6) * Mq + q;
-      const C gxx = g[0], gxy = g[Mq], gxz = g[2 * Mq], gyy = g[3 * Mq], gyz = g[4 * Mq], gzz = g[5 * Mq];
-      h[0] = cmad(cmad(cmad(h[0], gxx, sj[0]), gxy, sj[1]), gxz, sj[2]);
-      h[1] = cmad(cmad(cmad(h[1], gxy, sj[0]), gyy, sj[1]), gyz, sj[2]);
-      h[2] = cmad(cmad(cmad(h[2], gxz, sj[0]), gyz, sj[1]), gzz, sj[2]);
+  C s[NB][3], h[NB][3];
+#pragma unroll
+  for (int j = 0; j < NB; ++j)
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const C v = ks[(int64_t)(m * NB + j) * Mq + q];
+      s[j][m].x = v.x * (Real)mus.v[j];
+      s[j][m].y = v.y * (Real)mus.v[j];
+      h[j][m].x = h[j][m].y = 0;
     }
-    for (int m = 0; m < 3; ++m) kh[(int64_t)(m * nb + i) * Mq + q] = h[m];
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    C g[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      g[c].x = wd[(int64_t)(i * 6 + c) * Mq + q];
+      g[c].y = 0;
+    }
+    cmac_sym(h[i], g, s[i], false);
+  }
+  int p = 0;
+#pragma unroll
+  for (int i = 0; i < NB; ++i)
+#pragma unroll
+    for (int j = i + 1; j < NB; ++j, ++p) {
+      C g[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) g[c] = wo[(int64_t)(p * 6 + c) * Mq + q];
+      cmac_sym(h[i], g, s[j], false);
+      cmac_sym(h[j], g, s[i], true);
+    }
+#pragma unroll
+  for (int i = 0; i < NB; ++i)
+#pragma unroll
+    for (int m = 0; m < 3; ++m) kh[(int64_t)(m * NB + i) * Mq + q] = h[i][m];
+}
+
+template <class C, class Real>
+void launch_convolve(int nb, const C* ks, const Real* wd, const C* wo, C* kh, int64_t Mq, const MusArr& mus,
+                     cudaStream_t st) {
+  const unsigned g = (unsigned)((Mq + kDipBlock - 1) / kDipBlock);
+  switch (nb) {
+    case 1: dip_convolve<C, Real, 1><<<g, kDipBlock, 0, st>>>(ks, wd, wo, kh, Mq, mus); break;
+    case 2: dip_convolve<C, Real, 2><<<g, kDipBlock, 0, st>>>(ks, wd, wo, kh, Mq, mus); break;
+    case 3: dip_convolve<C, Real, 3><<<g, kDipBlock, 0, st>>>(ks, wd, wo, kh, Mq, mus); break;
+    default: dip_convolve<C, Real, 4><<<g, kDipBlock, 0, st>>>(ks, wd, wo, kh, Mq, mus); break;
   }
 }
 
@@ -144,9 +185,21 @@ __global__ void dip_tensor_scatter(const int64_t* __restrict__ idx, const double
   for (int c = 0; c < 6; ++c) grid[c * Mtot + idx[e]] = vals[6 * e + c];
 }
 
-__global__ void dip_to_float(const double2* __restrict__ a, float2* __restrict__ b, int64_t n) {
+// k-space tensor of one basis pair into its stored form: real parts (a
+// diagonal pair) or the complex values, in the replica's precision
+template <class C, class Real>
+__global__ void dip_store_tensor(const double2* __restrict__ a, Real* __restrict__ real_out, C* __restrict__ cplx_out,
+                                 int64_t n) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < n) b[e] = make_float2((float)a[e].x, (float)a[e].y);
+  if (e >= n) return;
+  if (real_out) {
+    real_out[e] = (Real)a[e].x;
+  } else {
+    C v;
+    v.x = (Real)a[e].x;
+    v.y = (Real)a[e].y;
+    cplx_out[e] = v;
+  }
 }
 
 unsigned blocks(int64_t n) { return (unsigned)((n + kDipBlock - 1) / kDipBlock); }
@@ -201,7 +254,7 @@ struct DipoleReplica {
   int64_t Mtot = 0, Mq = 0;
   cufftHandle fwd = 0, inv = 0;
   bool have_fwd = false, have_inv = false;
-  Dev<unsigned char> grid, ks, kh, w;
+  Dev<unsigned char> grid, ks, kh, wd, wo;   // wd: diagonal tensors (real), wo: i < j (complex)
   size_t work = 0;
   ~DipoleReplica() {
     if (have_fwd) cufftDestroy(fwd);
@@ -354,7 +407,8 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
     cudaError_t ce = R->grid.alloc((size_t)3 * nb * R->Mtot * real);
     if (ce == cudaSuccess) ce = R->ks.alloc((size_t)3 * nb * R->Mq * cplx);
     if (ce == cudaSuccess) ce = R->kh.alloc((size_t)3 * nb * R->Mq * cplx);
-    if (ce == cudaSuccess) ce = R->w.alloc((size_t)nb * nb * 6 * R->Mq * cplx);
+    if (ce == cudaSuccess) ce = R->wd.alloc((size_t)nb * 6 * R->Mq * real);
+    if (ce == cudaSuccess) ce = R->wo.alloc((size_t)std::max(nb * (nb - 1) / 2, 1) * 6 * R->Mq * cplx);
     if (ce != cudaSuccess) {
       err = cuda_msg(ce, "dipole: allocating grids");
       delete D;
@@ -375,8 +429,9 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
     Dev<double> dval;
     ce = tgrid.alloc((size_t)6 * R->Mtot);
     if (ce == cudaSuccess) ce = tk.alloc((size_t)6 * R->Mq);
+    int pair = 0;
     for (int bi = 0; bi < nb && ce == cudaSuccess && err.empty(); ++bi)
-      for (int bj = 0; bj < nb && ce == cudaSuccess && err.empty(); ++bj) {
+      for (int bj = bi; bj < nb && ce == cudaSuccess && err.empty(); ++bj) {
         std::vector<int64_t> idx;
         std::vector<double> vals;
         if (!tensor_entries(g, periodic, *R, bi, bj, idx, vals, err)) break;
@@ -399,13 +454,15 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
           break;
         }
         const int64_t n = 6 * R->Mq;
-        unsigned char* dst = R->w.p + (size_t)(bi * nb + bj) * 6 * R->Mq * cplx;
-        if (fp64) {
-          ce = cudaMemcpy(dst, tk.p, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice);
-        } else {
-          dip_to_float<<<blocks(n), kDipBlock>>>(tk.p, reinterpret_cast<float2*>(dst), n);
-          ce = cudaGetLastError();
-        }
+        unsigned char* rdst = bi == bj ? R->wd.p + (size_t)bi * 6 * R->Mq * real : nullptr;
+        unsigned char* cdst = bi == bj ? nullptr : R->wo.p + (size_t)(pair++) * 6 * R->Mq * cplx;
+        if (fp64)
+          dip_store_tensor<double2, double><<<blocks(n), kDipBlock>>>(
+              tk.p, reinterpret_cast<double*>(rdst), reinterpret_cast<double2*>(cdst), n);
+        else
+          dip_store_tensor<float2, float><<<blocks(n), kDipBlock>>>(
+              tk.p, reinterpret_cast<float*>(rdst), reinterpret_cast<float2*>(cdst), n);
+        ce = cudaGetLastError();
       }
     cufftDestroy(tplan);
     if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
@@ -422,7 +479,7 @@ void dipole_destroy(DipoleField* d) { delete d; }
 
 size_t dipole_device_bytes(const DipoleField* d) {
   size_t b = 0;
-  for (const auto* R : d->reps) b += R->grid.n + R->ks.n + R->kh.n + R->w.n + R->work;
+  for (const auto* R : d->reps) b += R->grid.n + R->ks.n + R->kh.n + R->wd.n + R->wo.n + R->work;
   return b;
 }
 
@@ -442,8 +499,8 @@ std::string dipole_compute(DipoleField* D, const void* s, void* h, int64_t npad,
                                                                 R->Mtot, grid);
       fr = cufftExecD2Z(R->fwd, grid, ks);
       if (fr != CUFFT_SUCCESS) return std::string("dipole: D2Z: ") + cufft_name(fr);
-      dip_convolve<double2><<<blocks(R->Mq), kDipBlock, 0, st>>>(ks, reinterpret_cast<const double2*>(R->w.p), kh,
-                                                                nb, R->Mq, D->mus);
+      launch_convolve<double2, double>(nb, ks, reinterpret_cast<const double*>(R->wd.p),
+                                       reinterpret_cast<const double2*>(R->wo.p), kh, R->Mq, D->mus, st);
       fr = cufftExecZ2D(R->inv, kh, grid);
       if (fr != CUFFT_SUCCESS) return std::string("dipole: Z2D: ") + cufft_name(fr);
       dip_gather<double><<<blocks(nspins), kDipBlock, 0, st>>>(grid, R->Mtot, R->L[1], R->L[2], nb, R->M[1],
@@ -458,8 +515,8 @@ std::string dipole_compute(DipoleField* D, const void* s, void* h, int64_t npad,
                                                                R->Mtot, grid);
       fr = cufftExecR2C(R->fwd, grid, ks);
       if (fr != CUFFT_SUCCESS) return std::string("dipole: R2C: ") + cufft_name(fr);
-      dip_convolve<float2><<<blocks(R->Mq), kDipBlock, 0, st>>>(ks, reinterpret_cast<const float2*>(R->w.p), kh, nb,
-                                                               R->Mq, D->mus);
+      launch_convolve<float2, float>(nb, ks, reinterpret_cast<const float*>(R->wd.p),
+                                     reinterpret_cast<const float2*>(R->wo.p), kh, R->Mq, D->mus, st);
       fr = cufftExecC2R(R->inv, kh, grid);
       if (fr != CUFFT_SUCCESS) return std::string("dipole: C2R: ") + cufft_name(fr);
       dip_gather<float><<<blocks(nspins), kDipBlock, 0, st>>>(grid, R->Mtot, R->L[1], R->L[2], nb, R->M[1],
