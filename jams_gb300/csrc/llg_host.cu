@@ -961,6 +961,20 @@ int64_t llg_num_spins(const llg_handle* h, int32_t replica) {
 
 int32_t llg_num_replicas(const llg_handle* h) { return h ? (int32_t)h->reps.size() : -1; }
 
+// the device address of a pinned, mapped host buffer (the unpack kernel then
+// reads it in place over the host link, in one pass with the layout
+// conversion), or null for pageable memory (copied by the DMA engines through
+// the device scratch buffer).  Results go back through the DMA engines: a
+// kernel's strided stores to host memory measured 2.6x slower.
+static void* mapped_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 static int transfer_state(llg_handle* h, int32_t replica, const double* src, double* dst, bool device_ptr) {
   if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
   if (replica >= (int32_t)h->reps.size()) return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
@@ -978,6 +992,8 @@ static int transfer_state(llg_handle* h, int32_t replica, const double* src, dou
       const double* s = src + 3 * host_off;
       if (device_ptr) {
         dev_aos = const_cast<double*>(s);
+      } else if (void* m = mapped_host(s)) {
+        dev_aos = static_cast<double*>(m);
       } else {
         ce = cudaMemcpyAsync(dev_aos, s, bytes, cudaMemcpyHostToDevice, h->stream);
         if (ce != cudaSuccess) return h->cuda_fail(ce, "copying spins to the device");
@@ -1031,16 +1047,21 @@ int llg_step(llg_handle* h, int32_t nsteps) {
   h->last_launches = 0;
   const bool alternates = next_buffer(h, 0) != 0;
   int K = h->steps_per_graph;
-  if (alternates && (K & 1)) K += 1;  // graphs must return the state to the buffer they found it in
+  if (alternates && (K & 1)) K += 1;  // full blocks return the state to the buffer they found it in
   int remaining = nsteps;
-  while (remaining >= K && K > 1) {
-    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX, K};
+  // blocks of K steps, then the remainder, each as one CUDA-graph launch
+  // (graphs cached per buffer parity, tiling and step count; remainders are
+  // cached while fewer than kMaxGraphs graphs exist, else launched directly)
+  constexpr size_t kMaxGraphs = 64;
+  while (remaining > 0) {
+    const int n = remaining >= K && K > 1 ? K : remaining;
+    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX, n};
     auto it = h->graphs.find(key);
-    if (it == h->graphs.end()) {
+    if (it == h->graphs.end() && (n == K || h->graphs.size() < kMaxGraphs)) {
       cudaGraph_t g;
       cudaError_t ce = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
       if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamBeginCapture");
-      enqueue_steps(h, K, h->cur);
+      enqueue_steps(h, n, h->cur);
       ce = cudaStreamEndCapture(h->stream, &g);
       if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamEndCapture");
       cudaGraphExec_t ge;
@@ -1049,16 +1070,16 @@ int llg_step(llg_handle* h, int32_t nsteps) {
       if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaGraphInstantiate");
       it = h->graphs.emplace(key, ge).first;
     }
-    cudaError_t ce = cudaGraphLaunch(it->second, h->stream);
-    if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaGraphLaunch");
-    h->last_launches += (int64_t)K * (h->integrator == LLG_HEUN ? 2 : 4) + 1;
-    remaining -= K;
-    h->iteration += K;
-  }
-  if (remaining > 0) {
-    h->last_launches += enqueue_steps(h, remaining, h->cur);
-    if (remaining & 1) h->cur = next_buffer(h, h->cur);
-    h->iteration += remaining;
+    if (it != h->graphs.end()) {
+      cudaError_t ce = cudaGraphLaunch(it->second, h->stream);
+      if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaGraphLaunch");
+      h->last_launches += (int64_t)n * (h->integrator == LLG_HEUN ? 2 : 4) + 1;
+    } else {
+      h->last_launches += enqueue_steps(h, n, h->cur);
+    }
+    if (n & 1) h->cur = next_buffer(h, h->cur);
+    remaining -= n;
+    h->iteration += n;
   }
   if (!h->async_err.empty()) {
     const std::string e = h->async_err;

@@ -90,3 +90,33 @@ def test_checkpoint_rejects_other_models_and_corruption(llg, tmp_path):
         other.load_checkpoint(str(bad))
     assert np.array_equal(other.get_state(-1), before)
     assert other.iteration == 0
+
+
+def test_pinned_host_buffers_go_through_the_mapped_path(llg):
+    """Pinned host buffers are read and written in place by the pack/unpack
+    kernels; the result equals the pageable (copied) path bit for bit,
+    including a replica's rows in the middle of a pinned buffer."""
+    torch = pytest.importorskip("torch")
+    w = W.sc_temperature_sweep(n_replicas=3, L_min=5, L_max=8)
+    sizes = [int(np.prod(r.L)) for r in w.replicas]
+    n = sum(sizes)
+    s = fresh(llg, w, llg.FP32C)
+    s.step(3)
+    want = s.get_state(-1)
+    pinned = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    got = pinned.numpy()
+    s.get_state(-1, out=got)
+    assert np.array_equal(got, want)
+    new = W.random_sphere(n, seed=11)
+    got[:] = new
+    s.set_state(got)
+    assert np.array_equal(s.get_state(-1), new.astype(np.float32).astype(np.float64))
+    # replica 1 into / from the interior rows of the pinned buffer
+    lo, hi = sizes[0], sizes[0] + sizes[1]
+    got[:] = 0.0
+    s.get_state(1, out=got[lo:hi])
+    assert np.array_equal(got[lo:hi], s.get_state(1))
+    assert not got[:lo].any() and not got[hi:].any()
+    got[lo:hi] = W.random_sphere(sizes[1], seed=12)
+    s.set_state(got[lo:hi], 1)
+    assert np.array_equal(s.get_state(1), got[lo:hi].astype(np.float32).astype(np.float64))
