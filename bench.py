@@ -450,15 +450,38 @@ def main():
             sol.get_state(-1, out=host_np)
         torch.cuda.synchronize()
         barrier(world)
+        t_set = t_step = t_get = 0.0
         t0 = time.perf_counter()
         for _ in range(ke):
+            a = time.perf_counter()
             sol.set_state(host_np, -1)
+            b = time.perf_counter()
             sol.step(1)
+            sol.synchronize()
+            c = time.perf_counter()
             sol.get_state(-1, out=host_np)
+            t_set += b - a
+            t_step += c - b
+            t_get += time.perf_counter() - c
         dt = time.perf_counter() - t0
         dt = max_over_ranks(dt, world, torch.device("cuda", local))
+        # the host link: pinned copies of the state's size, each direction
+        dev = torch.empty_like(host, device="cuda")
+        link = {}
+        for name, dst, src in (("h2d", dev, host), ("d2h", host, dev)):
+            dst.copy_(src)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            for _ in range(20):
+                dst.copy_(src)
+            torch.cuda.synchronize()
+            link[name] = n_spins * 24 * 20 / (time.perf_counter() - t1) / 1e9
+        floor_s = n_spins * 24 * (1.0 / link["h2d"] + 1.0 / link["d2h"]) / 1e9 + ms_per_step * 1e-3
         e2e = {"value": job_rate(n_spins, world, ke, dt), "unit": "spin-steps/s", "h2d_bytes_per_step": n_spins * 24,
-               "d2h_bytes_per_step": n_spins * 24, "steps": ke}
+               "d2h_bytes_per_step": n_spins * 24, "steps": ke,
+               "us_per_step": {"set_state": 1e6 * t_set / ke, "step": 1e6 * t_step / ke, "get_state": 1e6 * t_get / ke},
+               "host_link_gbs": link,
+               "link_floor_value": job_rate(n_spins, world, 1, floor_s)}
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
