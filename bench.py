@@ -81,7 +81,7 @@ WORKLOADS = {
 }
 
 
-def kernel_name(info: dict, integ: str, stage: int, precision: str) -> str:
+def kernel_name(info: dict, integ: str, stage: int, precision: str, dipole: bool = False) -> str:
     """Name of the kernel that runs stage `stage` of a step, as ncu prints it."""
     if info.get("family", "generic") != "generic" and precision == "fp32c":
         fam = {"sc": "FamSC", "bcc": "FamBCC", "bcc3": "FamBCC3", "triangular": "FamTRI"}[info["family"]]
@@ -89,7 +89,8 @@ def kernel_name(info: dict, integ: str, stage: int, precision: str) -> str:
             st = 0 if stage == 0 else (2 if info["store_rhs"] else 1)
         else:
             st = 3 + stage
-        return "tiled_stage<%s, %d, %d, %d, %d>" % (fam, info["tile_z"], info["tile_y"], st, info["occupancy"])
+        return "tiled_stage<%s, %d, %d, %d, %d, %s>" % (fam, info["tile_z"], info["tile_y"], st, info["occupancy"],
+                                                      "true" if dipole else "false")
     suffix = "_f32" if precision == "fp32c" else "_f64"
     if integ == "heun":
         return ("heun_predict" if stage == 0 else "heun_correct") + suffix
@@ -310,9 +311,10 @@ def traffic_from_profiles(workload: str, kernel: str, precision: str):
         d = json.load(open(path)).get(workload, {}).get(precision, {})
         e = d.get(kernel)
         if e is None and kernel.startswith("tiled_stage<"):
-            # the same stage compiled for another occupancy moves the same bytes
-            stem = kernel.rsplit(",", 1)[0]
-            e = next((v for k, v in d.items() if k.rsplit(",", 1)[0] == stem), None)
+            # the same family, tile and stage compiled for another occupancy
+            # moves the same bytes
+            stem = lambda k: ",".join(k.split(",")[:4])
+            e = next((v for k, v in d.items() if stem(k) == stem(kernel)), None)
         return None if e is None else float(e["dram_bytes_per_launch"])
     except (ValueError, OSError, KeyError, TypeError):
         return None
@@ -405,7 +407,8 @@ def main():
     peak = peaks.get("hbm_gbs")
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
-    kname = kernel_name(tuning, integ, dom, args.precision)
+    has_dipole = any(t.kind == W.TERM_DIPOLE for t in w.model.terms)
+    kname = kernel_name(tuning, integ, dom, args.precision, has_dipole)
     traffic = traffic_from_profiles(args.workload, kname, args.precision)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": kname, "stage": STAGE_NAMES[integ][dom], "peak_source": peak_src,

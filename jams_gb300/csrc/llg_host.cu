@@ -840,18 +840,18 @@ void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
       float* s0 = buf<float>(h, cur);
       float* sp = buf<float>(h, 1);
       if (stage == 0)
-        launch_tiled(h->family, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks);
+        launch_tiled(h->family, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, h->dipole != nullptr);
       else if (h->store_mode)
-        launch_tiled(h->family, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks);
+        launch_tiled(h->family, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks, h->dipole != nullptr);
       else
-        launch_tiled(h->family, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks);
+        launch_tiled(h->family, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, h->dipole != nullptr);
     } else {
       float* s0 = buf<float>(h, 0);
       float* a = buf<float>(h, 1);
       float* b = buf<float>(h, 2);
       float* in = stage == 0 ? s0 : (stage == 2 ? b : a);
       float* out = stage == 0 ? a : (stage == 1 ? b : (stage == 2 ? a : s0));
-      launch_tiled(h->family, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks);
+      launch_tiled(h->family, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, h->dipole != nullptr);
     }
     return;
   }

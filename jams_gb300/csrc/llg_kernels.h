@@ -46,7 +46,11 @@ void launch_pack(bool fp64, cudaStream_t st, const void* soa, double* aos, int64
 void tiled_geometry(int family, int* tz, int* ty);
 cudaError_t launch_tiled(int family, int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
                          const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux,
-                         uint32_t k);
+                         uint32_t k, bool dipole);
+template <bool DIP>
+cudaError_t launch_tiled_t(int family, int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
+                           const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux,
+                           uint32_t k);
 
 // observables (llg_observe.cu): ordered per-tile partial sums copied to
 // h_partials [ntiles][nq] = (sum mu_s Sx, Sy, Sz, sum mu_s, E_term...)

@@ -1,0 +1,702 @@
+// Tiled FP32 stage kernels for lattices that match a compile-time stencil
+// family (llg_families.h).  Implementation header: llg_tiled.cu compiles the
+// kernels of models without a dipole term, llg_tiled_dipole.cu those with one
+// (DIP: the dipole field planes are read and added), in parallel.
+//
+// 2.5-D streaming: a CTA owns a TY x TZ patch of cells (all basis sites) and
+// walks TX planes along the slowest axis X.  The spins of planes x-1, x, x+1
+// sit in a four-plane ring of float4 in shared memory (halo rows/columns
+// included, periodic wrap or open-boundary zeros applied once at load time);
+// the plane x+2 is fetched into registers while plane x is computed and
+// stored into the free ring slot before the CTA barrier.  Every neighbour is
+// then one 16-byte shared-memory load at a compile-time offset plus three
+// adds, and global memory sees each spin once per stage (plus the halo).
+//
+// Warps are laid out along Z (32 consecutive cells) with the basis site
+// uniform per warp, so the per-basis stencil never diverges.
+#pragma once
+#include <cstdint>
+#include <utility>
+
+#include "llg_families.h"
+#include "llg_kernels.h"
+
+// neighbour sums with packed f32x2 adds for x and y (1) or scalar adds (0);
+// both give the same sums bit for bit
+#ifndef JAMS_TILED_PACKED_GATHER
+#define JAMS_TILED_PACKED_GATHER 0
+#endif
+#include "llg_noise.cuh"
+
+namespace jams_llg {
+
+namespace {
+
+// every FP32 operation below is an explicit intrinsic: the result does not
+// depend on how the compiler would contract a given kernel, so all tiling
+// choices (stored or recomputed rhs, planes per CTA) agree bit for bit
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float ff(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+
+// packed pairs of FP32 (Blackwell f32x2 instructions, round to nearest):
+// the x and y components of a spin or field travel as one 64-bit register
+// (the 64-bit pairs are formed and split inside the PTX, so no C++ type
+// punning is involved)
+#define JAMS_F32X2_BINARY(NAME, OP)                                                              \
+  __device__ __forceinline__ float2 NAME(float2 a, float2 b) {                                    \
+    float2 d;                                                                                     \
+    asm("{.reg .b64 ra, rb, rd;\n\t"                                                              \
+        "mov.b64 ra, {%2, %3};\n\t"                                                               \
+        "mov.b64 rb, {%4, %5};\n\t" OP " rd, ra, rb;\n\t"                                       \
+        "mov.b64 {%0, %1}, rd;}"                                                                  \
+        : "=f"(d.x), "=f"(d.y)                                                                    \
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                                \
+    return d;                                                                                     \
+  }
+JAMS_F32X2_BINARY(add2, "add.rn.f32x2")
+JAMS_F32X2_BINARY(sub2, "sub.rn.f32x2")
+JAMS_F32X2_BINARY(mul2, "mul.rn.f32x2")
+#undef JAMS_F32X2_BINARY
+
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\t"
+      "mov.b64 rb, {%4, %5};\n\t"
+      "mov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\t"
+      "mov.b64 {%0, %1}, rd;}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+
+// (hi, lo) += (jhi + jlo) a for a packed pair, with TwoProd (p = jhi a,
+// pe = jhi a - p exactly) and TwoSum (hi + p = s + e exactly); jn = -jhi
+// lets the negated product feed both without extra sign flips
+__device__ __forceinline__ void acc_mad2(float2& hi, float2& lo, float jhi, float jn, float jlo, float2 a) {
+  const float2 J = make_float2(jhi, jhi), JN = make_float2(jn, jn), JL = make_float2(jlo, jlo);
+  const float2 pn = mul2(JN, a);         // -p
+  const float2 pe = fma2(J, a, pn);      // jhi a - p
+  const float2 s = sub2(hi, pn);         // hi + p
+  const float2 bb = sub2(s, hi);
+  const float2 e = sub2(sub2(hi, sub2(s, bb)), add2(pn, bb));
+  hi = s;
+  lo = add2(lo, add2(e, fma2(JL, a, pe)));
+}
+
+__device__ __forceinline__ void two_sum_t(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void acc_add_t(float& hi, float& lo, float c) {
+  float s, e;
+  two_sum_t(hi, c, s, e);
+  hi = s;
+  lo = __fadd_rn(lo, e);
+}
+
+__device__ __forceinline__ void acc_mad_t(float& hi, float& lo, float jhi, float jlo, float a) {
+  const float p = __fmul_rn(jhi, a);
+  const float pe = __fmaf_rn(jhi, a, -p);
+  float s, e;
+  two_sum_t(hi, p, s, e);
+  hi = s;
+  lo = __fadd_rn(lo, __fadd_rn(e, __fmaf_rn(jlo, a, pe)));
+}
+
+// thermal field for the FP32 form, Box-Muller with the special-function
+// unit (log2, sin, cos, rsqrt): two spins (planes x and x + 1 of one column,
+// x even) from one Philox4x32-10 call keyed by the even spin's index; six
+// 21-bit uniforms (the four words' top 21 bits, and their low bits
+// recombined) make three Box-Muller pairs.  The largest normal is
+// sqrt(-2 ln 2^-21) = 5.4.
+__device__ __forceinline__ float bm_radius(uint32_t k) {
+  const float u = (float)(k + 1u) * 0x1.0p-21f;  // (0, 1]
+  const float x = fmaxf(-1.3862943611198906f * __log2f(u), 1e-30f);  // -2 ln u
+  return x * rsqrtf(x);
+}
+
+__device__ __forceinline__ void noise_pair(const uint32_t* keys, uint32_t replica, uint64_t step, uint32_t spin,
+                                           float amp, float wa[3], float wb[3]) {
+  uint32_t c[4] = {spin, replica, (uint32_t)step, (uint32_t)(step >> 32)};
+  philox4x32_10_keyed(c, keys);
+  const uint32_t k4 = ((c[0] & 0x7FFu) << 10) | (c[1] & 0x3FFu);
+  const uint32_t k5 = ((c[2] & 0x7FFu) << 10) | (c[3] & 0x3FFu);
+  const float r0 = fm(amp, bm_radius(c[0] >> 11)), r1 = fm(amp, bm_radius(c[2] >> 11)), r2 = fm(amp, bm_radius(k4));
+  float s0, c0, s1, c1, s2, c2;
+  __sincosf(6.283185307179586f * (float)(c[1] >> 11) * 0x1.0p-21f, &s0, &c0);
+  __sincosf(6.283185307179586f * (float)(c[3] >> 11) * 0x1.0p-21f, &s1, &c1);
+  __sincosf(6.283185307179586f * (float)k5 * 0x1.0p-21f, &s2, &c2);
+  wa[0] = fm(r0, c0);
+  wa[1] = fm(r0, s0);
+  wa[2] = fm(r1, c1);
+  wb[0] = fm(r1, s1);
+  wb[1] = fm(r2, c2);
+  wb[2] = fm(r2, s2);
+}
+
+// Anisotropy and applied-field terms of one basis site, gathered once per
+// CTA into registers (at most one uniaxial, one cubic and one applied-field
+// term; the host sends other term lists to the gather kernels).  They are
+// summed in plain FP32 and added to the low word of the compensated
+// exchange sum.
+struct LocalField {
+  float uk;       // K * p of the uniaxial term (0: none)
+  int upow;
+  float ua[3];
+  float ck;       // 2 K of the cubic term (0: none)
+  int corder;
+  float cu[9];
+  float hb[3];    // mu_s B
+  float inv_mus, mg, alpha;
+};
+
+__device__ __forceinline__ LocalField local_field(const Params& P, const ReplicaDev& R, int b, int skip) {
+  LocalField L;
+  L.uk = 0.f;
+  L.upow = 2;
+  L.ck = 0.f;
+  L.corder = 1;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    L.ua[m] = 0.f;
+    L.hb[m] = 0.f;
+  }
+#pragma unroll
+  for (int m = 0; m < 9; ++m) L.cu[m] = 0.f;
+  for (int t = 0; t < P.nterms; ++t) {
+    if (t == skip) continue;
+    const TermDev& T = P.term[t];
+    if (T.kind == kUniaxial) {
+      L.uk = fm(T.Kf[b], (float)T.order);
+      L.upow = T.order;
+      for (int m = 0; m < 3; ++m) L.ua[m] = T.axisf[b][m];
+    } else if (T.kind == kCubic) {
+      L.ck = fm(2.0f, T.Kf[b]);
+      L.corder = T.order;
+      for (int m = 0; m < 9; ++m) L.cu[m] = T.axisf[b][m];
+    } else if (T.kind == kAppliedField) {
+      for (int m = 0; m < 3; ++m) L.hb[m] = fm(P.mus32[b], R.Bf[m]);
+    }
+  }
+  L.inv_mus = P.inv_mus32[b];
+  L.mg = -P.gyro32[b];
+  L.alpha = P.alpha32[b];
+  return L;
+}
+
+__device__ __forceinline__ void local_terms(const LocalField& L, const float s[3], float hi[3], float lo[3]) {
+  float l[3] = {L.hb[0], L.hb[1], L.hb[2]};
+  if (L.uk != 0.f) {
+    const float d = ff(L.ua[2], s[2], ff(L.ua[1], s[1], fm(L.ua[0], s[0])));
+    float pw = d;
+    if (L.upow >= 4) pw = fm(fm(d, d), d);
+    if (L.upow >= 6) pw = fm(fm(pw, d), d);
+    const float pre = fm(L.uk, pw);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) l[m] = ff(pre, L.ua[m], l[m]);
+  }
+  if (L.ck != 0.f) {
+    const float* u = L.cu;
+    const float Su = ff(u[2], s[2], ff(u[1], s[1], fm(u[0], s[0])));
+    const float Sv = ff(u[5], s[2], ff(u[4], s[1], fm(u[3], s[0])));
+    const float Sw = ff(u[8], s[2], ff(u[7], s[1], fm(u[6], s[0])));
+    const float Su2 = fm(Su, Su), Sv2 = fm(Sv, Sv), Sw2 = fm(Sw, Sw);
+    float cu, cv, cw;
+    if (L.corder == 1) {
+      cu = fm(Su, fa(Sv2, Sw2));
+      cv = fm(Sv, fa(Sw2, Su2));
+      cw = fm(Sw, fa(Su2, Sv2));
+    } else {
+      cu = fm(fm(Su, Sv2), Sw2);
+      cv = fm(fm(Sv, Sw2), Su2);
+      cw = fm(fm(Sw, Su2), Sv2);
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) l[m] = ff(L.ck, ff(u[6 + m], cw, ff(u[3 + m], cv, fm(u[m], cu))), l[m]);
+  }
+  // these terms are small next to the exchange field: added to the low
+  // word, their rounding stays at their own magnitude
+#pragma unroll
+  for (int m = 0; m < 3; ++m) lo[m] = fa(lo[m], l[m]);
+}
+
+__device__ __forceinline__ void llg_rhs_t(const LocalField& L, const float s[3], const float h[3], const float w[3],
+                                          float rhs[3]) {
+  const float im = L.inv_mus;
+  const float hh[3] = {ff(h[0], im, w[0]), ff(h[1], im, w[1]), ff(h[2], im, w[2])};
+  const float c1[3] = {ff(s[1], hh[2], -fm(s[2], hh[1])), ff(s[2], hh[0], -fm(s[0], hh[2])),
+                       ff(s[0], hh[1], -fm(s[1], hh[0]))};
+  const float c2[3] = {ff(s[1], c1[2], -fm(s[2], c1[1])), ff(s[2], c1[0], -fm(s[0], c1[2])),
+                       ff(s[0], c1[1], -fm(s[1], c1[0]))};
+  const float mg = L.mg, a = L.alpha;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) rhs[m] = fm(mg, ff(a, c2[m], c1[m]));
+}
+
+__device__ __forceinline__ void normalise_t(float v[3]) {
+  const float r = rsqrtf(ff(v[2], v[2], ff(v[1], v[1], fm(v[0], v[0]))));
+  v[0] = fm(v[0], r);
+  v[1] = fm(v[1], r);
+  v[2] = fm(v[2], r);
+}
+
+template <class F, int TZ, int TY>
+struct Geo {
+  static constexpr int NB = F::NB;
+  static constexpr int PY = TY + 2 * F::RY;
+  static constexpr int PZ = TZ + 2 * F::RZ;
+  static constexpr int PLANE = NB * PY * PZ;   // float4 per ring slot
+  static constexpr int NT = TZ * TY * NB;
+  static constexpr int PER_THREAD = (PLANE + NT - 1) / NT;
+};
+
+template <class F>
+__host__ __device__ constexpr int shell_of(int b, int k) {
+  int g = 0;
+  while (g + 1 < F::NSHELL && k >= F::shell_end(b, g)) ++g;
+  return g;
+}
+
+// one neighbour slot: every offset is a compile-time constant
+template <class F, int TZ, int TY, int B, int K>
+__device__ __forceinline__ void gather_slot(const float4* bm, const float4* b0, const float4* bp,
+                                            float2 (&axy)[F::NSHELL], float (&az)[F::NSHELL], float (&r)[3],
+                                            const TiledParams& TP) {
+  using G = Geo<F, TZ, TY>;
+  constexpr Slot sl = F::slot(B, K);
+  constexpr int off = (sl.bj * G::PY + sl.dy) * G::PZ + sl.dz;
+  constexpr int g = shell_of<F>(B, K);
+  const float4* p = sl.dx < 0 ? bm : (sl.dx == 0 ? b0 : bp);
+  const float4 v = p[off];
+#if JAMS_TILED_PACKED_GATHER
+  axy[g] = add2(axy[g], make_float2(v.x, v.y));
+#else
+  axy[g].x = fa(axy[g].x, v.x);
+  axy[g].y = fa(axy[g].y, v.y);
+#endif
+  az[g] = fa(az[g], v.z);
+  if constexpr (F::REST != 0) {
+    const float* J = TP.rest[B][K];
+    r[0] = ff(J[0], v.x, ff(J[1], v.y, ff(J[2], v.z, r[0])));
+    r[1] = ff(J[3], v.x, ff(J[4], v.y, ff(J[5], v.z, r[1])));
+    r[2] = ff(J[6], v.x, ff(J[7], v.y, ff(J[8], v.z, r[2])));
+  }
+}
+
+template <class F, int TZ, int TY, int B, int... K>
+__device__ __forceinline__ void gather_all(std::integer_sequence<int, K...>, const float4* bm, const float4* b0,
+                                           const float4* bp, float2 (&axy)[F::NSHELL], float (&az)[F::NSHELL],
+                                           float (&r)[3], const TiledParams& TP) {
+  (gather_slot<F, TZ, TY, B, K>(bm, b0, bp, axy, az, r, TP), ...);
+}
+
+// exchange field of basis site B at the thread's cell from one ring: plain
+// FP32 sum of the neighbour spins of each shell (x and y packed), then
+// h += J_shell * sum with TwoProd/TwoSum compensation; 3x3 remainders (REST
+// families) per slot
+template <class F, int TZ, int TY, int B>
+__device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const float4* ring, int xs, int own,
+                                               float hi[3], float lo[3]) {
+  using G = Geo<F, TZ, TY>;
+  const float4* bm = ring + ((xs + 3) & 3) * G::PLANE + own;
+  const float4* b0 = ring + (xs & 3) * G::PLANE + own;
+  const float4* bp = ring + ((xs + 1) & 3) * G::PLANE + own;
+  float2 axy[F::NSHELL];
+  float az[F::NSHELL];
+  float r[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int g = 0; g < F::NSHELL; ++g) {
+    axy[g] = make_float2(0.f, 0.f);
+    az[g] = 0.f;
+  }
+  gather_all<F, TZ, TY, B>(std::make_integer_sequence<int, F::Z>{}, bm, b0, bp, axy, az, r, TP);
+  // first shell: (hi, lo) is the exact product J a (TwoProd) plus the J
+  // low word, no TwoSum needed; the other shells are added with TwoSum
+  float2 hxy, lxy;
+  {
+    const float2 J = make_float2(TP.shell_hi[B][0], TP.shell_hi[B][0]);
+    const float2 JN = make_float2(-TP.shell_hi[B][0], -TP.shell_hi[B][0]);
+    const float2 JL = make_float2(TP.shell_lo[B][0], TP.shell_lo[B][0]);
+    const float2 pn = mul2(JN, axy[0]);
+    hxy = make_float2(-pn.x, -pn.y);
+    lxy = fma2(JL, axy[0], fma2(J, axy[0], pn));
+    const float p = fm(TP.shell_hi[B][0], az[0]);
+    hi[2] = p;
+    lo[2] = ff(TP.shell_lo[B][0], az[0], ff(TP.shell_hi[B][0], az[0], -p));
+  }
+#pragma unroll
+  for (int g = 1; g < F::NSHELL; ++g) {
+    acc_mad2(hxy, lxy, TP.shell_hi[B][g], -TP.shell_hi[B][g], TP.shell_lo[B][g], axy[g]);
+    acc_mad_t(hi[2], lo[2], TP.shell_hi[B][g], TP.shell_lo[B][g], az[g]);
+  }
+  hi[0] = hxy.x;
+  hi[1] = hxy.y;
+  lo[0] = lxy.x;
+  lo[1] = lxy.y;
+  if constexpr (F::REST != 0) {
+    acc_add_t(hi[0], lo[0], r[0]);
+    acc_add_t(hi[1], lo[1], r[1]);
+    acc_add_t(hi[2], lo[2], r[2]);
+  }
+}
+
+template <class F, int TZ, int TY>
+__device__ __forceinline__ void exchange_dispatch(int b, const TiledParams& TP, const float4* ring, int xs, int own,
+                                                  float hi[3], float lo[3]) {
+  if (F::NB == 1 || b == 0) {
+    exchange_tiled<F, TZ, TY, 0>(TP, ring, xs, own, hi, lo);
+  } else if (F::NB > 1) {
+    exchange_tiled<F, TZ, TY, (F::NB > 1 ? 1 : 0)>(TP, ring, xs, own, hi, lo);
+  }
+}
+
+// total field (meV) of the thread's spin from ring `ring`
+template <class F, int TZ, int TY>
+__device__ __forceinline__ void field_tiled(const LocalField& L, const TiledParams& TP, int b, const float4* ring,
+                                           int xs, int own, float h[3], float s[3], bool has_dip,
+                                           const float dip[3]) {
+  using G = Geo<F, TZ, TY>;
+  const float4 c = ring[(xs & 3) * G::PLANE + own + b * G::PY * G::PZ];
+  s[0] = c.x;
+  s[1] = c.y;
+  s[2] = c.z;
+  float hi[3], lo[3];
+  exchange_dispatch<F, TZ, TY>(b, TP, ring, xs, own, hi, lo);
+  local_terms(L, s, hi, lo);
+  if (has_dip) {   // the dipole field of this spin, precomputed by FFT convolution
+#pragma unroll
+    for (int m = 0; m < 3; ++m) lo[m] = fa(lo[m], dip[m]);
+  }
+#pragma unroll
+  for (int m = 0; m < 3; ++m) h[m] = hi[m] + lo[m];
+}
+
+// one ring slot worth of spins for plane x: registers, then shared memory
+template <class F, int TZ, int TY>
+struct PlaneRegs {
+  float v[Geo<F, TZ, TY>::PER_THREAD][3];
+};
+
+// the replica's tile view, held in registers for the whole CTA
+struct View {
+  int L[3];
+  int st[3];      // spin-index strides (Z stride = basis count)
+  bool per[3];
+  int64_t offset;
+};
+
+__device__ __forceinline__ View load_view(const ReplicaDev& R) {
+  View v;
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    v.L[l] = R.vL[l];
+    v.st[l] = (int)R.vs[l];
+    v.per[l] = R.vper[l] != 0;
+  }
+  v.offset = R.offset;
+  return v;
+}
+
+// periodic wrap of a coordinate within one period of the lattice, without
+// branches; `valid` drops to false outside an open boundary or the lattice
+__device__ __forceinline__ int wrap_sel(int c, int L, bool per, bool& valid) {
+  const bool lo = c < 0, hi = c >= L;
+  valid = valid && (per || !(lo || hi));
+  const int w = c + (lo ? L : 0) - (hi ? L : 0);
+  valid = valid && w >= 0 && w < L;
+  return w;
+}
+
+// the part of a thread's halo loads that does not change from plane to
+// plane: which (row, column, basis site) it loads and where it stores it
+template <class F, int TZ, int TY>
+struct FetchPlan {
+  int idx[Geo<F, TZ, TY>::PER_THREAD];   // spin index in the plane (-1: zero / unused)
+  int dst[Geo<F, TZ, TY>::PER_THREAD];   // ring slot offset
+};
+
+template <class F, int TZ, int TY>
+__device__ __forceinline__ void plan_fetch(const View& V, int y0, int z0, int tid, FetchPlan<F, TZ, TY>& fp) {
+  using G = Geo<F, TZ, TY>;
+#pragma unroll
+  for (int q = 0; q < G::PER_THREAD; ++q) {
+    const int idx = tid + q * G::NT;
+    const int bb = idx % G::NB;
+    const int t = idx / G::NB;
+    const int zz = t % G::PZ;
+    const int yy = t / G::PZ;
+    bool valid = idx < G::PLANE;
+    const int gy = wrap_sel(y0 - F::RY + yy, V.L[1], V.per[1], valid);
+    const int gz = wrap_sel(z0 - F::RZ + zz, V.L[2], V.per[2], valid);
+    fp.idx[q] = valid ? gy * V.st[1] + gz * V.st[2] + bb : -1;
+    fp.dst[q] = idx < G::PLANE ? (bb * G::PY + yy) * G::PZ + zz : -1;
+  }
+}
+
+template <class F, int TZ, int TY>
+__device__ __forceinline__ void fetch_plane(const View& V, const float* __restrict__ s, int64_t npad, int x,
+                                            const FetchPlan<F, TZ, TY>& fp, PlaneRegs<F, TZ, TY>& pr) {
+  using G = Geo<F, TZ, TY>;
+  bool xvalid = true;
+  const int gx = wrap_sel(x, V.L[0], V.per[0], xvalid);
+  const float* sx = s + V.offset + gx * V.st[0];
+#pragma unroll
+  for (int q = 0; q < G::PER_THREAD; ++q) {
+    const bool valid = xvalid && fp.idx[q] >= 0;
+    const int i = fp.idx[q];
+    pr.v[q][0] = valid ? __ldg(sx + i) : 0.f;
+    pr.v[q][1] = valid ? __ldg(sx + npad + i) : 0.f;
+    pr.v[q][2] = valid ? __ldg(sx + 2 * npad + i) : 0.f;
+  }
+}
+
+template <class F, int TZ, int TY>
+__device__ __forceinline__ void store_plane(float4* ring, int x, const FetchPlan<F, TZ, TY>& fp,
+                                            const PlaneRegs<F, TZ, TY>& pr) {
+  using G = Geo<F, TZ, TY>;
+  float4* slot = ring + (x & 3) * G::PLANE;
+#pragma unroll
+  for (int q = 0; q < G::PER_THREAD; ++q)
+    if (fp.dst[q] >= 0) slot[fp.dst[q]] = make_float4(pr.v[q][0], pr.v[q][1], pr.v[q][2], 0.f);
+}
+
+}  // namespace
+
+// STAGE: 0 Heun predictor (writes sp; with aux != null also rhs0 into aux)
+//        1 Heun corrector recomputing rhs(s0) (rings of s0 and sp)
+//        2 Heun corrector from stored rhs0 (ring of sp; own s0 and aux)
+//        3..6 RK4 stages 1..4 (ring of sin; own s0, aux = k accumulator)
+template <class F, int TZ, int TY, int STAGE, int MINB, bool DIP>
+__global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __grid_constant__ Params P,
+                                                                  const __grid_constant__ TiledParams TP,
+                                                                  const float* s0, const float* sin, float* out,
+                                                                  float* aux, uint32_t kstep) {
+  using G = Geo<F, TZ, TY>;
+  constexpr int NR = STAGE == 1 ? 2 : 1;
+  extern __shared__ float4 smem[];
+  float4* ring0 = smem;                    // ring of the gathered state
+  float4* ring1 = smem + 4 * G::PLANE;     // second ring (s0) for STAGE 1
+  const int4 tile = TP.tiles[blockIdx.x];
+  const ReplicaDev& R = P.rep[tile.x];
+  const View V = load_view(R);
+  const int thermal = R.thermal;
+  const int x0 = tile.y, y0 = tile.z, z0 = tile.w;
+  const int tid = threadIdx.x + TZ * threadIdx.y;
+  const int tz = threadIdx.x;
+  const int ty = threadIdx.y % TY;
+  const int b = threadIdx.y / TY;
+  const float amp = R.amp32[b];
+  const int y = y0 + ty, z = z0 + tz;
+  const bool active_yz = y < V.L[1] && z < V.L[2];
+  const int own = (ty + F::RY) * G::PZ + (tz + F::RZ);
+  const uint64_t step = *P.step_base + kstep;
+  const float* gather_src = STAGE == 0 ? s0 : sin;
+  const LocalField L = local_field(P, R, b, TP.exch_term);
+  constexpr bool has_dip = DIP;   // the model has a dipole term (field planes in P.hdip32)
+  const float dt = P.dt32;
+  const int yz = y * V.st[1] + z * V.st[2] + b;
+  // planes of this replica (outputs, stored rhs / k sum, own start state)
+  float* ox = out + V.offset;
+  float* oy = ox + P.npad;
+  float* oz = oy + P.npad;
+  float* ax = aux ? aux + V.offset : nullptr;
+  float* ay = aux ? ax + P.npad : nullptr;
+  float* az = aux ? ay + P.npad : nullptr;
+  const float* s0x = s0 + V.offset;
+  const float* s0y = s0x + P.npad;
+  const float* s0z = s0y + P.npad;
+  const int xe = min(x0 + TP.TX, V.L[0]);
+  FetchPlan<F, TZ, TY> fp;
+  plan_fetch<F, TZ, TY>(V, y0, z0, tid, fp);
+
+  {
+    PlaneRegs<F, TZ, TY> pr;
+#pragma unroll
+    for (int d = -1; d <= 1; ++d) {
+      fetch_plane<F, TZ, TY>(V, gather_src, P.npad, x0 + d, fp, pr);
+      store_plane<F, TZ, TY>(ring0, x0 + d, fp, pr);
+      if (NR == 2) {
+        fetch_plane<F, TZ, TY>(V, s0, P.npad, x0 + d, fp, pr);
+        store_plane<F, TZ, TY>(ring1, x0 + d, fp, pr);
+      }
+    }
+  }
+  __syncthreads();
+
+  // noise of plane x + 1, drawn with plane x's when x is even (the host keeps
+  // planes per CTA even, so x0 is even)
+  float wn[3] = {0.f, 0.f, 0.f};
+  for (int x = x0; x < xe; ++x) {
+    const bool more = x + 1 < xe;
+    PlaneRegs<F, TZ, TY> pf0, pf1;
+    if (more) {
+      fetch_plane<F, TZ, TY>(V, gather_src, P.npad, x + 2, fp, pf0);
+      if (NR == 2) fetch_plane<F, TZ, TY>(V, s0, P.npad, x + 2, fp, pf1);
+    }
+    if (active_yz) {
+      const int i = x * V.st[0] + yz;   // spin index in the replica
+      float w[3] = {wn[0], wn[1], wn[2]};
+      if (thermal && (x & 1) == 0) noise_pair(P.philox_keys, (uint32_t)tile.x, step, (uint32_t)i, amp, w, wn);
+      // the spin's own start-of-step state and stored rhs / k sum: loaded
+      // before the exchange sum so that the sum covers their latency
+      float own_s0[3] = {0.f, 0.f, 0.f}, own_r[3] = {0.f, 0.f, 0.f};
+      if (STAGE >= 2) {
+        own_s0[0] = __ldg(s0x + i);
+        own_s0[1] = __ldg(s0y + i);
+        own_s0[2] = __ldg(s0z + i);
+      }
+      if (STAGE == 2 || STAGE >= 4) {
+        own_r[0] = ax[i];
+        own_r[1] = ay[i];
+        own_r[2] = az[i];
+      }
+      // dipole field of the spin (input state; s0 for the recomputed rhs)
+      float dip[3] = {0.f, 0.f, 0.f}, dip0[3] = {0.f, 0.f, 0.f};
+      if (has_dip) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) dip[m] = __ldg(P.hdip32 + m * P.npad + V.offset + i);
+        if (STAGE == 1) {
+#pragma unroll
+          for (int m = 0; m < 3; ++m) dip0[m] = __ldg(P.hdip32_s0 + m * P.npad + V.offset + i);
+        }
+      }
+      float h[3], s[3], k[3];
+      field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own, h, s, has_dip, dip);
+      llg_rhs_t(L, s, h, w, k);
+      if (STAGE == 0) {
+        float v[3] = {ff(dt, k[0], s[0]), ff(dt, k[1], s[1]), ff(dt, k[2], s[2])};
+        normalise_t(v);
+        ox[i] = v[0];
+        oy[i] = v[1];
+        oz[i] = v[2];
+        if (ax) {
+          ax[i] = k[0];
+          ay[i] = k[1];
+          az[i] = k[2];
+        }
+      } else if (STAGE == 1 || STAGE == 2) {
+        float a[3], r0[3];
+        if (STAGE == 1) {
+          float h0[3];
+          field_tiled<F, TZ, TY>(L, TP, b, ring1, x, own, h0, a, has_dip, dip0);
+          llg_rhs_t(L, a, h0, w, r0);
+        } else {
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            a[m] = own_s0[m];
+            r0[m] = own_r[m];
+          }
+        }
+        const float hdt = fm(0.5f, dt);
+        float v[3] = {ff(hdt, fa(r0[0], k[0]), a[0]), ff(hdt, fa(r0[1], k[1]), a[1]),
+                      ff(hdt, fa(r0[2], k[2]), a[2])};
+        normalise_t(v);
+        if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
+        ox[i] = v[0];
+        oy[i] = v[1];
+        oz[i] = v[2];
+      } else {
+        const float* a = own_s0;
+        float* acc[3] = {ax, ay, az};
+        float v[3];
+        if (STAGE == 6) {
+          const float c = fm(dt, 1.0f / 6.0f);
+#pragma unroll
+          for (int m = 0; m < 3; ++m) v[m] = ff(c, fa(own_r[m], k[m]), a[m]);
+          normalise_t(v);
+          if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
+        } else {
+          const float c = STAGE == 5 ? dt : fm(0.5f, dt);
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            const float an = STAGE == 3 ? k[m] : ff(2.0f, k[m], own_r[m]);
+            acc[m][i] = an;
+            v[m] = ff(c, k[m], a[m]);
+          }
+          if (P.rk4_normalise_stages) normalise_t(v);
+        }
+        ox[i] = v[0];
+        oy[i] = v[1];
+        oz[i] = v[2];
+      }
+    }
+    if (more) {
+      store_plane<F, TZ, TY>(ring0, x + 2, fp, pf0);
+      if (NR == 2) store_plane<F, TZ, TY>(ring1, x + 2, fp, pf1);
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ launchers --
+
+namespace {
+
+template <class F, int TZ, int TY>
+size_t smem_bytes(int stage) {
+  return (size_t)(stage == 1 ? 2 : 1) * 4 * Geo<F, TZ, TY>::PLANE * sizeof(float4);
+}
+
+template <class F, int TZ, int TY, int STAGE, int MINB, bool DIP>
+cudaError_t launch_one(unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP, const float* s0,
+                       const float* sin, float* out, float* aux, uint32_t k) {
+  const size_t sm = smem_bytes<F, TZ, TY>(STAGE);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tiled_stage<F, TZ, TY, STAGE, MINB, DIP>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const dim3 block(TZ, TY * F::NB);
+  tiled_stage<F, TZ, TY, STAGE, MINB, DIP><<<grid, block, sm, st>>>(P, TP, s0, sin, out, aux, k);
+  return cudaSuccess;
+}
+
+template <class F, int TZ, int TY, int MINB, bool DIP>
+cudaError_t launch_family(int stage, unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP,
+                          const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
+  switch (stage) {
+    case 0: return launch_one<F, TZ, TY, 0, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 1: return launch_one<F, TZ, TY, 1, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 2: return launch_one<F, TZ, TY, 2, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 3: return launch_one<F, TZ, TY, 3, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 4: return launch_one<F, TZ, TY, 4, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 5: return launch_one<F, TZ, TY, 5, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    default: return launch_one<F, TZ, TY, 6, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+  }
+}
+
+template <class F, int TZ, int TY, bool DIP>
+cudaError_t launch_occ(int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
+                       const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
+  // occupancy variant: at least 2 (up to 128 registers), 3 (up to 80) or 4
+  // (up to 64) CTAs per SM
+  if (occupancy >= 4) return launch_family<F, TZ, TY, 4, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  if (occupancy == 3) return launch_family<F, TZ, TY, 3, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  return launch_family<F, TZ, TY, 2, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+}
+
+}  // namespace
+
+// the tiled stage kernels with (DIP) or without the dipole field planes;
+// llg_tiled.cu instantiates DIP = false, llg_tiled_dipole.cu DIP = true
+template <bool DIP>
+cudaError_t launch_tiled_t(int family, int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
+                         const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux,
+                         uint32_t k) {
+  switch (family) {
+    case kFamSC: return launch_occ<FamSC, 32, 8, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    case kFamBCC: return launch_occ<FamBCC, 32, 4, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    case kFamBCC3: return launch_occ<FamBCC3, 32, 4, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    case kFamTRI: return launch_occ<FamTRI, 256, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace jams_llg
