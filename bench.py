@@ -110,7 +110,7 @@ def parse(argv=None):
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-steps", type=int, default=50)
     p.add_argument("--no-tune", action="store_true")
-    p.add_argument("--tuning", default="", help="planes_per_cta,store_rhs,occupancy instead of autotuning")
+    p.add_argument("--tuning", default="", help="planes_per_cta,flags,occupancy instead of autotuning (flags: 1 stored rhs, 2 narrow tile)")
     return p.parse_args(argv)
 
 
@@ -348,8 +348,8 @@ def main():
     n_spins = sol.num_spins(-1)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if args.tuning:
-        tx, st, oc = (int(v) for v in args.tuning.split(","))
-        sol.set_tuning(tx, bool(st), oc)
+        tx, fl, oc = (int(v) for v in args.tuning.split(","))
+        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2))
         tuning = sol.kernel_info()
     else:
         # the choice is cached per lattice shape ($JAMS_LLG_TUNE_CACHE), so a

@@ -234,10 +234,11 @@ int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
 int llg_kernel_info(const llg_handle *h, int32_t *info);
 
 /* Tiling choice of the tiled FP32 kernels (no effect on other kernels):
-   planes streamed per CTA (rounded up to even: a thread computes two
-   consecutive planes per iteration); flags bit 0: the Heun predictor stores rhs(s0);
-   flags >> 4: occupancy variant, 2 (<= 128 registers), 3 (<= 80) or 4
-   (<= 64). */
+   planes streamed per CTA (rounded up to even: the thermal noise of planes
+   x and x + 1, x even, comes from one draw); flags bit 0: the Heun
+   predictor stores rhs(s0); bit 1: the narrow tile (half the rows, twice
+   the CTAs, for lattices too small to fill the GPU); flags >> 4: occupancy
+   variant, 2 (<= 128 registers), 3 (<= 80) or 4 (<= 64). */
 int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t flags);
 
 /* Times every tiling candidate (planes per CTA 2..64, stored or recomputed

@@ -840,18 +840,18 @@ void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
       float* s0 = buf<float>(h, cur);
       float* sp = buf<float>(h, 1);
       if (stage == 0)
-        launch_tiled(h->family, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, h->dipole != nullptr);
       else if (h->store_mode)
-        launch_tiled(h->family, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks, h->dipole != nullptr);
       else
-        launch_tiled(h->family, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, h->dipole != nullptr);
     } else {
       float* s0 = buf<float>(h, 0);
       float* a = buf<float>(h, 1);
       float* b = buf<float>(h, 2);
       float* in = stage == 0 ? s0 : (stage == 2 ? b : a);
       float* out = stage == 0 ? a : (stage == 1 ? b : (stage == 2 ? a : s0));
-      launch_tiled(h->family, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, h->dipole != nullptr);
+      launch_tiled(h->family, h->ty, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, h->dipole != nullptr);
     }
     return;
   }
@@ -1055,7 +1055,7 @@ int llg_step(llg_handle* h, int32_t nsteps) {
   constexpr size_t kMaxGraphs = 64;
   while (remaining > 0) {
     const int n = remaining >= K && K > 1 ? K : remaining;
-    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX, n};
+    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX + 8192 * h->ty, n};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end() && (n == K || h->graphs.size() < kMaxGraphs)) {
       cudaGraph_t g;
@@ -1316,7 +1316,13 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
   h->store_mode = (store_rhs & 1) != 0 && h->integrator == LLG_HEUN;
   const int occ = store_rhs >> 4;
   h->occupancy = occ >= 4 ? 4 : (occ == 3 ? 3 : 2);
-  if (planes_per_cta != h->TP.TX) {
+  // bit 1: the narrow tile (half the rows, twice the CTAs)
+  int wide_tz = 0, wide_ty = 0;
+  tiled_geometry(h->family, &wide_tz, &wide_ty);
+  const int ty = (store_rhs & 2) ? narrow_tile_rows(h->family) : wide_ty;
+  const bool retile = ty != h->ty;
+  h->ty = ty;
+  if (planes_per_cta != h->TP.TX || retile) {
     h->TP.TX = planes_per_cta;
     int rc = build_tiles4(h);
     if (rc) return rc;
@@ -1397,15 +1403,22 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   std::vector<std::pair<int, int>> cands;   // (planes per CTA, store flag | occupancy << 4)
   for (int t : {2, 4, 8, 16, 32, 64})
     if (t <= std::max(2, maxL))
-      for (int occ : {2, 3, 4}) {
-        cands.push_back({t, occ << 4});
-        if (h->integrator == LLG_HEUN) cands.push_back({t, 1 | (occ << 4)});
-      }
+      for (int occ : {2, 3, 4})
+        for (int narrow : {0, 2}) {   // the family's wide tile, or the narrow one where it differs
+          int wide_tz = 0, wide_ty = 0;
+          tiled_geometry(h->family, &wide_tz, &wide_ty);
+          if (narrow && narrow_tile_rows(h->family) == wide_ty) continue;
+          cands.push_back({t, narrow | (occ << 4)});
+          if (h->integrator == LLG_HEUN) cands.push_back({t, 1 | narrow | (occ << 4)});
+        }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  std::pair<int, int> choice = {h->TP.TX, (h->store_mode ? 1 : 0) | (h->occupancy << 4)};
+  int wide_tz0 = 0, wide_ty0 = 0;
+  tiled_geometry(h->family, &wide_tz0, &wide_ty0);
+  std::pair<int, int> choice = {h->TP.TX, (h->store_mode ? 1 : 0) | (h->ty != wide_ty0 ? 2 : 0) |
+                                              (h->occupancy << 4)};
   // each trial runs as llg_step runs steps: one CUDA graph of trial_steps
   // steps (captured and run once untimed, then timed)
   const int spg0 = h->steps_per_graph;

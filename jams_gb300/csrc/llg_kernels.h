@@ -44,13 +44,16 @@ void launch_pack(bool fp64, cudaStream_t st, const void* soa, double* aos, int64
 
 // tiled FP32 kernels (llg_tiled.cu); family ids in llg_families.h
 void tiled_geometry(int family, int* tz, int* ty);
-cudaError_t launch_tiled(int family, int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
-                         const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux,
-                         uint32_t k, bool dipole);
+// ty: tile rows (the family's wide tile from tiled_geometry or the narrow
+// one from narrow_tile_rows)
+int narrow_tile_rows(int family);
+cudaError_t launch_tiled(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
+                         const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
+                         float* aux, uint32_t k, bool dipole);
 template <bool DIP>
-cudaError_t launch_tiled_t(int family, int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
-                           const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux,
-                           uint32_t k);
+cudaError_t launch_tiled_t(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
+                           const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
+                           float* aux, uint32_t k);
 
 // observables (llg_observe.cu): ordered per-tile partial sums copied to
 // h_partials [ntiles][nq] = (sum mu_s Sx, Sy, Sz, sum mu_s, E_term...)

@@ -4,9 +4,9 @@
 
 namespace jams_llg {
 
-template cudaError_t launch_tiled_t<false>(int, int, int, unsigned, cudaStream_t, const Params&, const TiledParams&,
-                                           const float*, const float*, float*, float*, uint32_t);
-extern template cudaError_t launch_tiled_t<true>(int, int, int, unsigned, cudaStream_t, const Params&,
+template cudaError_t launch_tiled_t<false>(int, int, int, int, unsigned, cudaStream_t, const Params&,
+                                           const TiledParams&, const float*, const float*, float*, float*, uint32_t);
+extern template cudaError_t launch_tiled_t<true>(int, int, int, int, unsigned, cudaStream_t, const Params&,
                                                  const TiledParams&, const float*, const float*, float*, float*,
                                                  uint32_t);
 
@@ -20,11 +20,19 @@ void tiled_geometry(int family, int* tz, int* ty) {
   }
 }
 
-cudaError_t launch_tiled(int family, int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
-                         const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux,
-                         uint32_t k, bool dipole) {
-  return dipole ? launch_tiled_t<true>(family, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k)
-                : launch_tiled_t<false>(family, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+// rows of the narrow tile variant of a family (the wide one when it has none)
+int narrow_tile_rows(int family) {
+  if (family == kFamSC) return 4;
+  int tz, ty;
+  tiled_geometry(family, &tz, &ty);
+  return ty;
+}
+
+cudaError_t launch_tiled(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
+                         const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
+                         float* aux, uint32_t k, bool dipole) {
+  return dipole ? launch_tiled_t<true>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k)
+                : launch_tiled_t<false>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
 }
 
 }  // namespace jams_llg

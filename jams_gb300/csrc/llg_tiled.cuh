@@ -675,23 +675,31 @@ cudaError_t launch_family(int stage, unsigned grid, cudaStream_t st, const Param
 template <class F, int TZ, int TY, bool DIP>
 cudaError_t launch_occ(int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
                        const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
-  // occupancy variant: at least 2 (up to 128 registers), 3 (up to 80) or 4
-  // (up to 64) CTAs per SM
-  if (occupancy >= 4) return launch_family<F, TZ, TY, 4, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
-  if (occupancy == 3) return launch_family<F, TZ, TY, 3, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
-  return launch_family<F, TZ, TY, 2, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  // occupancy variant, as the resident threads of 2, 3 or 4 CTAs of 256
+  // threads (up to 128, 80 or 64 registers per thread); narrow tiles of 128
+  // threads run twice as many CTAs per SM with the same register budget
+  constexpr int S = 256 / Geo<F, TZ, TY>::NT > 1 ? 256 / Geo<F, TZ, TY>::NT : 1;
+  if (occupancy >= 4) return launch_family<F, TZ, TY, 4 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  if (occupancy == 3) return launch_family<F, TZ, TY, 3 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  return launch_family<F, TZ, TY, 2 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
 }
 
 }  // namespace
 
 // the tiled stage kernels with (DIP) or without the dipole field planes;
 // llg_tiled.cu instantiates DIP = false, llg_tiled_dipole.cu DIP = true
+// ty: rows of the CTA tile, the family's wide tile or, for simple cubic,
+// the narrow one (half the rows: twice the CTAs, for small lattices; the
+// bcc narrow tile measured slower at 64^3 and 256^3, its halo rows cost more
+// than the extra CTAs gain)
 template <bool DIP>
-cudaError_t launch_tiled_t(int family, int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
-                         const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux,
-                         uint32_t k) {
+cudaError_t launch_tiled_t(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
+                           const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
+                           float* aux, uint32_t k) {
   switch (family) {
-    case kFamSC: return launch_occ<FamSC, 32, 8, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    case kFamSC:
+      return ty == 4 ? launch_occ<FamSC, 32, 4, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k)
+                     : launch_occ<FamSC, 32, 8, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
     case kFamBCC: return launch_occ<FamBCC, 32, 4, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
     case kFamBCC3: return launch_occ<FamBCC3, 32, 4, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
     case kFamTRI: return launch_occ<FamTRI, 256, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);

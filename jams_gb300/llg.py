@@ -385,8 +385,10 @@ class Solver:
         self._check(self.L.llg_autotune(self.h, int(trial_steps), int(bool(use_cache))))
         return self.kernel_info()
 
-    def set_tuning(self, planes_per_cta: int, store_rhs: bool, occupancy: int = 2) -> None:
-        flags = int(bool(store_rhs)) | (int(occupancy) << 4)
+    def set_tuning(self, planes_per_cta: int, store_rhs: bool, occupancy: int = 2, narrow: bool = False) -> None:
+        """Tiling of the tiled FP32 kernels: planes per CTA, stored rhs(s0)
+        (Heun), occupancy variant 2/3/4, narrow tile (half the rows)."""
+        flags = int(bool(store_rhs)) | (int(bool(narrow)) << 1) | (int(occupancy) << 4)
         self._check(self.L.llg_set_tuning(self.h, int(planes_per_cta), flags))
 
     @property

@@ -256,16 +256,19 @@ def test_fp32c_gather_kernels_within_bound(llg, oracle):
 def test_tiling_choices_give_identical_results(llg, name):
     """Planes per CTA and stored vs recomputed rhs(s0) change the schedule,
     not the arithmetic: states are bit-identical.  Odd plane counts are
-    rounded up to even (a thread computes two planes)."""
+    rounded up to even (the noise of two planes comes from one draw); the
+    narrow tile exists for simple cubic (elsewhere the flag is ignored)."""
     w = {"bcc3": W.bcc_three_shell(L=10, T=300.0, start="random"),
          "sc": W.sc_ferromagnet(L=(9, 12, 40), T=100.0),
          "tri": W.triangular_dmi_field_sweep(L=(20, 300, 1), n_fields=2, T=5.0)}[name]
     if name == "tri":
         w.model.integrator = W.HEUN
     outs = []
-    for tx, store, occ in [(1, False, 2), (1, True, 4), (3, False, 4), (4, True, 3), (8, True, 2), (64, False, 2)]:
+    for tx, store, occ, narrow in [(1, False, 2, False), (1, True, 4, False), (3, False, 4, False),
+                                   (4, True, 3, False), (8, True, 2, False), (64, False, 2, False),
+                                   (2, True, 4, True), (6, False, 3, True), (64, True, 2, True)]:
         s = solver(llg, w, llg.FP32C, steps_per_graph=4)
-        s.set_tuning(tx, store, occ)
+        s.set_tuning(tx, store, occ, narrow)
         for r in range(len(w.replicas)):
             s.set_state(W.initial_state(w, r), r)
         s.step(11)
