@@ -161,21 +161,24 @@ void launch_convolve(int nb, const C* ks, const Real* wd, const C* wo, C* kh, in
   }
 }
 
-// grid -> SoA field planes of the replica, times mu_i
+// grid -> SoA field planes of the replica, times mu_i; one thread per
+// lattice cell (coalesced reads of every grid row; the basis sites of a cell
+// are adjacent in the planes)
 template <class Real>
 __global__ void __launch_bounds__(kDipBlock) dip_gather(const Real* __restrict__ grid, int64_t Mtot, int L1, int L2,
-                                                        int nb, int M1, int M2, int64_t nspins, int64_t offset,
+                                                        int nb, int M1, int M2, int64_t ncells, int64_t offset,
                                                         int64_t npad, MusArr mus, Real* __restrict__ h) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nspins) return;
-  const int b = (int)(i % nb);
-  const int64_t cell = i / nb;
+  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncells) return;
   const int z = (int)(cell % L2);
   const int y = (int)((cell / L2) % L1);
   const int x = (int)(cell / ((int64_t)L1 * L2));
   const int64_t n = ((int64_t)x * M1 + y) * M2 + z;
-  const Real mu = (Real)mus.v[b];
-  for (int c = 0; c < 3; ++c) h[c * npad + offset + i] = mu * grid[(int64_t)(c * nb + b) * Mtot + n];
+  for (int b = 0; b < nb; ++b) {
+    const Real mu = (Real)mus.v[b];
+    for (int c = 0; c < 3; ++c)
+      h[c * npad + offset + cell * nb + b] = mu * grid[(int64_t)(c * nb + b) * Mtot + n];
+  }
 }
 
 __global__ void dip_tensor_scatter(const int64_t* __restrict__ idx, const double* __restrict__ vals, int64_t n,
@@ -486,7 +489,7 @@ size_t dipole_device_bytes(const DipoleField* d) {
 std::string dipole_compute(DipoleField* D, const void* s, void* h, int64_t npad, cudaStream_t st) {
   const int nb = D->nb;
   for (DipoleReplica* R : D->reps) {
-    const int64_t nspins = (int64_t)R->L[0] * R->L[1] * R->L[2] * nb;
+    const int64_t ncells = (int64_t)R->L[0] * R->L[1] * R->L[2];
     cufftResult fr = cufftSetStream(R->fwd, st);
     if (fr == CUFFT_SUCCESS) fr = cufftSetStream(R->inv, st);
     if (fr != CUFFT_SUCCESS) return std::string("dipole: cufftSetStream: ") + cufft_name(fr);
@@ -503,8 +506,8 @@ std::string dipole_compute(DipoleField* D, const void* s, void* h, int64_t npad,
                                        reinterpret_cast<const double2*>(R->wo.p), kh, R->Mq, D->mus, st);
       fr = cufftExecZ2D(R->inv, kh, grid);
       if (fr != CUFFT_SUCCESS) return std::string("dipole: Z2D: ") + cufft_name(fr);
-      dip_gather<double><<<blocks(nspins), kDipBlock, 0, st>>>(grid, R->Mtot, R->L[1], R->L[2], nb, R->M[1],
-                                                               R->M[2], nspins, R->offset, npad, D->mus,
+      dip_gather<double><<<blocks(ncells), kDipBlock, 0, st>>>(grid, R->Mtot, R->L[1], R->L[2], nb, R->M[1],
+                                                               R->M[2], ncells, R->offset, npad, D->mus,
                                                                static_cast<double*>(h));
     } else {
       float* grid = reinterpret_cast<float*>(R->grid.p);
@@ -519,8 +522,8 @@ std::string dipole_compute(DipoleField* D, const void* s, void* h, int64_t npad,
                                      reinterpret_cast<const float2*>(R->wo.p), kh, R->Mq, D->mus, st);
       fr = cufftExecC2R(R->inv, kh, grid);
       if (fr != CUFFT_SUCCESS) return std::string("dipole: C2R: ") + cufft_name(fr);
-      dip_gather<float><<<blocks(nspins), kDipBlock, 0, st>>>(grid, R->Mtot, R->L[1], R->L[2], nb, R->M[1],
-                                                              R->M[2], nspins, R->offset, npad, D->mus,
+      dip_gather<float><<<blocks(ncells), kDipBlock, 0, st>>>(grid, R->Mtot, R->L[1], R->L[2], nb, R->M[1],
+                                                              R->M[2], ncells, R->offset, npad, D->mus,
                                                               static_cast<float*>(h));
     }
     const cudaError_t ce = cudaGetLastError();
