@@ -70,6 +70,8 @@ WORKLOADS = {
     "sc_sweep256": lambda: W.sc_temperature_sweep(),
     # triangular 2048^2 x 16 fields, tensor exchange + DMI, RK4, 5 K
     "tri2048_dmi_x16": lambda: W.triangular_dmi_field_sweep(),
+    # fcc (4-site conventional cell), 12 + 6 neighbours, 300 K: 128^3 x 4 = 8.4 M spins
+    "fcc128_2shell": lambda: W.fcc_ferromagnet(L=128, T=300.0, J2=0.2),
     # the headline and the 256^3 3-shell workloads with the dipole-dipole term
     # (FFT convolution, r_c = 8 lattice parameters)
     "bcc64_3shell_dipole": lambda: W.bcc_three_shell(L=64, T=300.0, start="+z", dipole_cutoff=8.0),
@@ -84,7 +86,8 @@ WORKLOADS = {
 def kernel_name(info: dict, integ: str, stage: int, precision: str, dipole: bool = False) -> str:
     """Name of the kernel that runs stage `stage` of a step, as ncu prints it."""
     if info.get("family", "generic") != "generic" and precision == "fp32c":
-        fam = {"sc": "FamSC", "bcc": "FamBCC", "bcc3": "FamBCC3", "triangular": "FamTRI"}[info["family"]]
+        fam = {"sc": "FamSC", "bcc": "FamBCC", "bcc3": "FamBCC3", "triangular": "FamTRI", "fcc": "FamFCC",
+               "fcc2": "FamFCC2"}[info["family"]]
         if integ == "heun":
             st = 0 if stage == 0 else (2 if info["store_rhs"] else 1)
         else:

@@ -226,7 +226,8 @@ int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
 
 /* Kernel selection of the handle: info[0] stencil family of the tiled FP32
    kernels (0: generic gather kernels; 1 simple cubic, 2 bcc nearest
-   neighbours, 3 bcc three shells, 4 triangular monolayer), info[1] planes
+   neighbours, 3 bcc three shells, 4 triangular monolayer, 5 fcc nearest
+   neighbours, 6 fcc two shells), info[1] planes
    streamed per CTA, info[2] 1 when the Heun predictor stores rhs(s0) for
    the corrector (else the corrector recomputes it), info[3..4] CTA tile
    (cells along the contiguous axis, rows), info[5] 1 for FP64, info[6] the

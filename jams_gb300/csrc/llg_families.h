@@ -20,7 +20,7 @@ struct Slot {
   int dx, dy, dz, bj;
 };
 
-enum FamilyId { kFamNone = 0, kFamSC = 1, kFamBCC = 2, kFamBCC3 = 3, kFamTRI = 4 };
+enum FamilyId { kFamNone = 0, kFamSC = 1, kFamBCC = 2, kFamBCC3 = 3, kFamTRI = 4, kFamFCC = 5, kFamFCC2 = 6 };
 
 // simple cubic, 6 nearest neighbours, one shell
 struct FamSC {
@@ -68,6 +68,49 @@ struct FamBCC3 {
   __host__ __device__ static constexpr int shell_end(int /*b*/, int g) { return g == 0 ? 8 : g == 1 ? 14 : 26; }
   __host__ __device__ static constexpr Slot slot(int b, int k) {
     return k < 8 ? bcc_shell1(b, k) : k < 14 ? bcc_shell2(b, k - 8) : bcc_shell3(b, k - 14);
+  }
+};
+
+// fcc as a 4-site conventional cubic cell, sites at (0,0,0), (0,1/2,1/2),
+// (1/2,0,1/2), (1/2,1/2,0).  fcc_half: twice the fractional coordinate of
+// site b along axis.
+__host__ __device__ constexpr int fcc_half(int b, int axis) { return b == 0 ? 0 : (b - 1 == axis ? 0 : 1); }
+
+// shell 1: the 12 neighbours at a / sqrt(2), on the other three
+// sublattices, in (partner, dX, dY, dZ) lexicographic order
+__host__ __device__ constexpr Slot fcc_shell1(int b, int k) {
+  int n = 0;
+  for (int bj = 0; bj < 4; ++bj)
+    for (int tx = -1; tx <= 1; ++tx)
+      for (int ty = -1; ty <= 1; ++ty)
+        for (int tz = -1; tz <= 1; ++tz) {
+          const int dx = 2 * tx + fcc_half(bj, 0) - fcc_half(b, 0);
+          const int dy = 2 * ty + fcc_half(bj, 1) - fcc_half(b, 1);
+          const int dz = 2 * tz + fcc_half(bj, 2) - fcc_half(b, 2);
+          if (bj != b && dx * dx + dy * dy + dz * dz == 2) {
+            if (n == k) return Slot{tx, ty, tz, bj};
+            ++n;
+          }
+        }
+  return Slot{0, 0, 0, -1};
+}
+
+struct FamFCC {
+  static constexpr int id = kFamFCC;
+  static constexpr int NB = 4, RX = 1, RY = 1, RZ = 1, TWO_D = 0;
+  static constexpr int NSHELL = 1, Z = 12, REST = 0;
+  __host__ __device__ static constexpr int shell_end(int /*b*/, int /*g*/) { return 12; }
+  __host__ __device__ static constexpr Slot slot(int b, int k) { return fcc_shell1(b, k); }
+};
+
+// fcc with the second shell: the 6 same-sublattice neighbours at a
+struct FamFCC2 {
+  static constexpr int id = kFamFCC2;
+  static constexpr int NB = 4, RX = 1, RY = 1, RZ = 1, TWO_D = 0;
+  static constexpr int NSHELL = 2, Z = 18, REST = 0;
+  __host__ __device__ static constexpr int shell_end(int /*b*/, int g) { return g == 0 ? 12 : 18; }
+  __host__ __device__ static constexpr Slot slot(int b, int k) {
+    return k < 12 ? fcc_shell1(b, k) : bcc_shell2(b, k - 12);
   }
 };
 

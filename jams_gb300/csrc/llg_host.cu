@@ -333,6 +333,8 @@ int find_family(const llg_desc* d, const llg_term& t, TiledParams& TP) {
   if (match_family<FamBCC>(d, t, TP)) return kFamBCC;
   if (match_family<FamBCC3>(d, t, TP)) return kFamBCC3;
   if (match_family<FamTRI>(d, t, TP)) return kFamTRI;
+  if (match_family<FamFCC>(d, t, TP)) return kFamFCC;
+  if (match_family<FamFCC2>(d, t, TP)) return kFamFCC2;
   return kFamNone;
 }
 

@@ -16,6 +16,8 @@ void tiled_geometry(int family, int* tz, int* ty) {
     case kFamBCC:
     case kFamBCC3: *tz = 32; *ty = 4; break;
     case kFamTRI: *tz = 256; *ty = 1; break;
+    case kFamFCC:
+    case kFamFCC2: *tz = 32; *ty = 2; break;
     default: *tz = 0; *ty = 0; break;
   }
 }

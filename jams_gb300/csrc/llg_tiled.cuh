@@ -348,11 +348,17 @@ __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const floa
 template <class F, int TZ, int TY>
 __device__ __forceinline__ void exchange_dispatch(int b, const TiledParams& TP, const float4* ring, int xs, int own,
                                                   float hi[3], float lo[3]) {
+  // the basis site is uniform per warp; one compile-time stencil per site
   if (F::NB == 1 || b == 0) {
     exchange_tiled<F, TZ, TY, 0>(TP, ring, xs, own, hi, lo);
-  } else if (F::NB > 1) {
+  } else if (b == 1) {
     exchange_tiled<F, TZ, TY, (F::NB > 1 ? 1 : 0)>(TP, ring, xs, own, hi, lo);
+  } else if (b == 2) {
+    exchange_tiled<F, TZ, TY, (F::NB > 2 ? 2 : 0)>(TP, ring, xs, own, hi, lo);
+  } else {
+    exchange_tiled<F, TZ, TY, (F::NB > 3 ? 3 : 0)>(TP, ring, xs, own, hi, lo);
   }
+  static_assert(F::NB <= 4, "at most four basis sites per family");
 }
 
 // total field (meV) of the thread's spin from ring `ring`
@@ -703,6 +709,8 @@ cudaError_t launch_tiled_t(int family, int ty, int occupancy, int stage, unsigne
     case kFamBCC: return launch_occ<FamBCC, 32, 4, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
     case kFamBCC3: return launch_occ<FamBCC3, 32, 4, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
     case kFamTRI: return launch_occ<FamTRI, 256, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    case kFamFCC: return launch_occ<FamFCC, 32, 2, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    case kFamFCC2: return launch_occ<FamFCC2, 32, 2, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -377,7 +377,7 @@ class Solver:
     def kernel_info(self) -> dict:
         info = (ctypes.c_int32 * 8)()
         self._check(self.L.llg_kernel_info(self.h, info))
-        fam = {0: "generic", 1: "sc", 2: "bcc", 3: "bcc3", 4: "triangular"}[info[0]]
+        fam = {0: "generic", 1: "sc", 2: "bcc", 3: "bcc3", 4: "triangular", 5: "fcc", 6: "fcc2"}[info[0]]
         return {"family": fam, "planes_per_cta": info[1], "store_rhs": bool(info[2]), "tile_z": info[3],
                 "tile_y": info[4], "fp64": bool(info[5]), "occupancy": info[6]}
 

@@ -20,6 +20,7 @@ Unit conventions follow the reference:
 from __future__ import annotations
 
 import dataclasses
+import itertools
 import math
 from typing import List, Optional, Sequence
 
@@ -281,6 +282,42 @@ def bcc_nearest_neighbour(L=256, steps=2000, T=500.0, seed=1, start="+z", t_step
     return Workload(name=f"bcc{Ls[0]}_nn", model=model,
                     replicas=[Replica(L=Ls, temperature=T)], steps=steps, seed=seed, start=start,
                     description="bcc 2-site basis, NN J=1 meV, K1=0.1 meV z, B=1 T z, Heun a=0.1 dt=0.5fs")
+
+
+def fcc_entries(J1: float, J2: Optional[float] = None):
+    """Exchange template of the 4-site conventional fcc cell (sites at
+    (0,0,0), (0,1/2,1/2), (1/2,0,1/2), (1/2,1/2,0)): the 12 nearest
+    neighbours at a/sqrt2 and, with J2, the 6 at a."""
+    f = np.array([[0, 0, 0], [0, 0.5, 0.5], [0.5, 0, 0.5], [0.5, 0.5, 0]])
+    out = []
+    for bi in range(4):
+        for bj in range(4):
+            for T in itertools.product((-1, 0, 1), repeat=3):
+                d = np.asarray(T) + f[bj] - f[bi]
+                r2 = float(d @ d)
+                if abs(r2 - 0.5) < 1e-9:
+                    out.append((bi, bj, T, isotropic(J1)))
+                elif J2 is not None and abs(r2 - 1.0) < 1e-9:
+                    out.append((bi, bj, T, isotropic(J2)))
+    return out
+
+
+def fcc_ferromagnet(L=64, steps=2000, T=300.0, seed=1, J1=1.5, J2=None, start="+z", t_step=0.5e-15) -> Workload:
+    """fcc, 4-site conventional basis, isotropic J1 (12 neighbours) and
+    optional J2 (6), mu_s = 1.7 muB, uniaxial K1 = 0.01 meV z, B = 0.5 T z,
+    Heun alpha = 0.05, dt = 0.5 fs (as the bcc configurations: the exchange
+    field is ~180 T)."""
+    mus, gyro, al = material(1.7, 1.0, 0.05)
+    basis = np.array([[0, 0, 0], [0, 0.5, 0.5], [0.5, 0, 0.5], [0.5, 0.5, 0]], dtype=np.float64)
+    terms = [exchange_term(fcc_entries(J1, J2)), uniaxial_term(4, 0.01), field_term((0.0, 0.0, 0.5))]
+    model = Model(nb=4, periodic=(1, 1, 1), mus=np.full(4, mus), gyro=np.full(4, gyro),
+                  alpha=np.full(4, al), terms=terms, t_step=t_step, integrator=HEUN,
+                  cell=np.eye(3), basis_frac=basis)
+    Ls = (L, L, L) if np.isscalar(L) else tuple(L)
+    shells = "J1=%g" % J1 + ("" if J2 is None else " J2=%g" % J2)
+    return Workload(name=f"fcc{Ls[0]}_" + ("2shell" if J2 is not None else "nn"), model=model,
+                    replicas=[Replica(L=Ls, temperature=T)], steps=steps, seed=seed, start=start,
+                    description="fcc 4-site basis, %s meV, K1=0.01 meV z, B=0.5 T z, Heun a=0.05 dt=0.5fs" % shells)
 
 
 def sc_temperature_sweep(n_replicas=256, L_min=16, L_max=64, T_max=1200.0, steps=10000, seed=1,

@@ -222,7 +222,8 @@ def test_tiled_families_selected(llg):
     """FP32C picks the tiled kernel of the matching lattice family; FP64 and
     templates outside the families use the gather kernels."""
     cases_ = [(W.sc_ferromagnet(L=8), "sc"), (W.bcc_nearest_neighbour(L=4), "bcc"),
-              (W.bcc_three_shell(L=4), "bcc3"), (W.triangular_dmi_field_sweep(L=8, n_fields=1), "triangular")]
+              (W.bcc_three_shell(L=4), "bcc3"), (W.triangular_dmi_field_sweep(L=8, n_fields=1), "triangular"),
+              (W.fcc_ferromagnet(L=4), "fcc"), (W.fcc_ferromagnet(L=4, J2=0.2), "fcc2")]
     for w, fam in cases_:
         assert solver(llg, w, llg.FP32C).kernel_info()["family"] == fam
         assert solver(llg, w, llg.FP64).kernel_info()["family"] == "generic"
@@ -252,7 +253,7 @@ def test_fp32c_gather_kernels_within_bound(llg, oracle):
     assert np.abs(s.get_state(0) - ref).max() <= FP32C_TOL
 
 
-@pytest.mark.parametrize("name", ["bcc3", "sc", "tri"])
+@pytest.mark.parametrize("name", ["bcc3", "sc", "tri", "fcc2"])
 def test_tiling_choices_give_identical_results(llg, name):
     """Planes per CTA and stored vs recomputed rhs(s0) change the schedule,
     not the arithmetic: states are bit-identical.  Odd plane counts are
@@ -260,7 +261,8 @@ def test_tiling_choices_give_identical_results(llg, name):
     narrow tile exists for simple cubic (elsewhere the flag is ignored)."""
     w = {"bcc3": W.bcc_three_shell(L=10, T=300.0, start="random"),
          "sc": W.sc_ferromagnet(L=(9, 12, 40), T=100.0),
-         "tri": W.triangular_dmi_field_sweep(L=(20, 300, 1), n_fields=2, T=5.0)}[name]
+         "tri": W.triangular_dmi_field_sweep(L=(20, 300, 1), n_fields=2, T=5.0),
+         "fcc2": W.fcc_ferromagnet(L=(6, 5, 66), T=300.0, J2=0.2, start="random")}[name]
     if name == "tri":
         w.model.integrator = W.HEUN
     outs = []
@@ -293,3 +295,22 @@ def test_autotune_keeps_state_and_iteration(llg):
     b.set_state(s0)
     b.step(12)
     assert np.array_equal(a.get_state(0), b.get_state(0))
+
+
+@pytest.mark.parametrize("J2", [None, 0.2])
+def test_fcc_families_match_oracle(llg, oracle, J2):
+    """fcc (4-site cell, 12 + 6 neighbours): FP64 bit for bit and FP32C within
+    bound against the oracle after 1000 T = 0 steps."""
+    w = W.fcc_ferromagnet(L=(5, 6, 7), T=0.0, J2=J2, start="random")
+    s0 = W.initial_state(w, 0)
+    ref = oracle.OracleSim(w).run(s0, 1000)
+    s = solver(llg, w, llg.FP32C)
+    assert s.kernel_info()["family"] == ("fcc" if J2 is None else "fcc2")
+    s.set_state(s0)
+    s.step(1000)
+    assert np.abs(s.get_state(0) - ref).max() <= FP32C_TOL
+    d = solver(llg, w, llg.FP64)
+    d.set_state(s0)
+    d.step(1000)
+    assert np.array_equal(d.get_state(0), ref)
+
