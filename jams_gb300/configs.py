@@ -114,3 +114,35 @@ solver : { module = "llg-rk4-gpu"; t_step = %r; t_max = %r; };
 physics : { temperature = %r; };
 sim : { seed = %d; };
 """ % (L, L, inter, Bz, t_step, t_step * steps, T, seed)
+
+
+def fcc_two_shell(L=32, T=300.0, t_step=0.5e-15, steps=2000, seed=1, J1=1.5, J2=0.2) -> str:
+    """fcc conventional cell (4 sites), one interaction vector per shell
+    expanded by the crystal's symmetry operations: 12 + 6 neighbours."""
+    return _header("Ni", 1.7, 0.05, "[0.0, 0.0, 1.0]") + """
+unitcell : {
+  parameter = 3.52e-10;
+  basis = ( [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0] );
+  positions = ( ("Ni", [0.0, 0.0, 0.0]), ("Ni", [0.0, 0.5, 0.5]),
+                ("Ni", [0.5, 0.0, 0.5]), ("Ni", [0.5, 0.5, 0.0]) );
+};
+
+lattice : { size = [%d, %d, %d]; periodic = [true, true, true]; };
+
+hamiltonians = (
+  {
+    module = "exchange";
+    energy_units = "meV";
+    interactions = (
+      ("Ni", "Ni", [0.5, 0.5, 0.0], %r),    // 12 at a<110>/2
+      ("Ni", "Ni", [1.0, 0.0, 0.0], %r)     // 6 at a<100>
+    );
+  },
+  { module = "uniaxial"; energy_units = "meV"; order = "K1"; anisotropies = ( ("Ni", [0.0, 0.0, 1.0], 0.01) ); },
+  { module = "applied-field"; field = [0.0, 0.0, 0.5]; }
+);
+
+solver : { module = "llg-heun-gpu"; t_step = %r; t_max = %r; };
+physics : { temperature = %r; };
+sim : { seed = %d; };
+""" % (L, L, L, J1, J2, t_step, t_step * steps, T, seed)

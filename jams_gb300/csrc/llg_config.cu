@@ -22,11 +22,18 @@
 // concatenation, '=' or ':' assignment, ';' or ',' separators).
 //
 // Symmetry operations: the reference asks spglib for the space group and
-// keeps the operations without translation that fix the basis site
-// (src/jams/core/lattice.cc:1127-1152).  Here those operations are found
+// keeps, per basis site, the rotations of the operations without
+// translation that fix the site modulo a lattice vector
+// (src/jams/core/lattice.cc:1127-1152).  Here the site point group is found
 // directly: integer matrices R (entries -1, 0, 1) in fractional coordinates
-// that preserve the lattice metric and map every basis site onto a basis
-// site of the same material with zero translation.
+// that preserve the lattice metric, for which x -> R x + (p - R p) maps every
+// basis site onto a basis site of the same material; the partner of an
+// expanded interaction is the site its rotated vector reaches.  On cells
+// whose site symmetries need no centring translation (simple cubic, bcc,
+// primitive cells, the triangular monolayer) this is the reference's set;
+// on centred conventional cells (the 4-site fcc cell) the reference drops
+// the operations with a centring translation and keeps the original partner,
+// which leaves sites with incomplete or inconsistent neighbour lists.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -444,8 +451,10 @@ int material_index(const Model& m, const std::string& name) {
   throw CfgError("material " + name + " is not defined");
 }
 
-// zero-translation point operations of the crystal (integer matrices in
-// fractional coordinates) that fix basis site `site`
+// point group of basis site `site`: the rotations R (integer matrices in
+// fractional coordinates) of the symmetry operations x -> R x + t of the
+// crystal that fix the site, as the reference takes them from spglib's
+// space group (src/jams/core/lattice.cc:1015-1060)
 std::vector<std::array<int, 9>> site_point_group(const Model& m, int site) {
   // metric G = A^T A
   M3 G{};
@@ -473,13 +482,20 @@ std::vector<std::array<int, 9>> site_point_group(const Model& m, int site) {
         if (std::fabs(v - G[i][j]) > kLatticeTolerance) metric = false;
       }
     if (!metric) continue;
-    auto apply = [&](const V3& p) {
+    auto rot = [&](const V3& p) {
       return V3{R[0] * p[0] + R[1] * p[1] + R[2] * p[2], R[3] * p[0] + R[4] * p[1] + R[5] * p[2],
                 R[6] * p[0] + R[7] * p[1] + R[8] * p[2]};
     };
+    // the operation x -> R x + t that fixes the site: t = p - R p (every
+    // symmetry fixing the site has this translation, modulo lattice vectors,
+    // including the centring translations of conventional cells)
+    const V3 ps = m.basis[site].frac;
+    const V3 rp = rot(ps);
+    const V3 t{ps[0] - rp[0], ps[1] - rp[1], ps[2] - rp[2]};
     bool maps = true;
     for (auto& b : m.basis) {
-      const V3 q = apply(b.frac);
+      const V3 r = rot(b.frac);
+      const V3 q{r[0] + t[0], r[1] + t[1], r[2] + t[2]};
       bool found = false;
       for (auto& b2 : m.basis)
         if (b2.mat == b.mat && same_site(q, b2.frac)) found = true;
@@ -489,7 +505,6 @@ std::vector<std::array<int, 9>> site_point_group(const Model& m, int site) {
       }
     }
     if (!maps) continue;
-    if (!same_site(apply(m.basis[site].frac), m.basis[site].frac)) continue;
     ops.push_back(R);
   }
   return ops;
@@ -593,6 +608,16 @@ void build_exchange(Model& m, const Node& h, Model::Term& out) {
       for (auto& q : pts) {
         Interaction J = I;
         J.r = q;
+        // the partner is the site the rotated vector reaches.  The reference
+        // keeps the original partner (apply_symops, interactions.cc:24-37),
+        // which is the same site whenever the point group maps the partner's
+        // sublattice onto itself (bcc, primitive cells) and, in cells where
+        // a rotation reaches another sublattice (the conventional fcc cell),
+        // gives a non-integer translation that only an assert checks.
+        const V3 qf = mul(m.cell_inv, q);
+        const V3 p{m.basis[I.bi].frac[0] + qf[0], m.basis[I.bi].frac[1] + qf[1], m.basis[I.bi].frac[2] + qf[2]};
+        for (int j = 0; j < (int)m.basis.size(); ++j)
+          if (same_site(p, m.basis[j].frac) && m.basis[j].material == I.tj) J.bj = j;
         sym.push_back(J);
       }
     }

@@ -613,8 +613,6 @@ int build(llg_handle* h, const llg_desc* d) {
     h->reps[r] = R;
   }
   // tile views (X, Y, Z) of every replica
-  const bool two_d_possible = true;
-  (void)two_d_possible;
   for (auto& R : h->reps) {
     const int64_t nbl = d->nb;
     R.vL[0] = R.L[0];

@@ -59,6 +59,15 @@ def test_bcc_symmetry_expansion_gives_26_neighbours(llg):
     assert d["max_steps"] == 20000
 
 
+def test_fcc_symmetry_expansion_gives_18_neighbours(llg):
+    """One vector per shell on the 4-site fcc cell expands to 12 + 6
+    neighbours per site (the fcc sites' point group is the full cubic one)."""
+    d = llg.describe_config(C.fcc_two_shell(L=6))
+    w = W.fcc_ferromagnet(L=6, J2=0.2)
+    check_model(d, w)
+    assert len(d["terms"][0]["bi"]) == 4 * 18
+
+
 def test_triangular_tensor_config(llg):
     d = llg.describe_config(C.triangular_dmi(L=16))
     w = W.triangular_dmi_field_sweep(L=16, n_fields=1)
