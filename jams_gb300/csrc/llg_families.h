@@ -23,8 +23,12 @@ struct Slot {
 enum FamilyId { kFamNone = 0, kFamSC = 1, kFamBCC = 2, kFamBCC3 = 3, kFamTRI = 4, kFamFCC = 5, kFamFCC2 = 6 };
 
 // simple cubic, 6 nearest neighbours, one shell
+// SEP: 0 plain slot gather; 1 bcc shell 1 as two carried 2x2 plane sums;
+// 2 also shells 2 and 3 from carried in-plane cross sums (llg_tiled.cuh).
+// bcc three shells use 2 (12 % faster at 256^3); bcc nearest neighbours
+// keep the plain gather.
 struct FamSC {
-  static constexpr int id = kFamSC;
+  static constexpr int id = kFamSC, SEP = 0;
   static constexpr int NB = 1, RX = 1, RY = 1, RZ = 1, TWO_D = 0;
   static constexpr int NSHELL = 1, Z = 6, REST = 0;
   __host__ __device__ static constexpr int shell_end(int /*b*/, int g) { return g == 0 ? 6 : 6; }
@@ -54,7 +58,7 @@ __host__ __device__ constexpr Slot bcc_shell3(int b, int k) {
 }
 
 struct FamBCC {
-  static constexpr int id = kFamBCC;
+  static constexpr int id = kFamBCC, SEP = 0;   // SEP = 1 measured 2 % slower: too little to save
   static constexpr int NB = 2, RX = 1, RY = 1, RZ = 1, TWO_D = 0;
   static constexpr int NSHELL = 1, Z = 8, REST = 0;
   __host__ __device__ static constexpr int shell_end(int /*b*/, int /*g*/) { return 8; }
@@ -62,7 +66,7 @@ struct FamBCC {
 };
 
 struct FamBCC3 {
-  static constexpr int id = kFamBCC3;
+  static constexpr int id = kFamBCC3, SEP = 2;
   static constexpr int NB = 2, RX = 1, RY = 1, RZ = 1, TWO_D = 0;
   static constexpr int NSHELL = 3, Z = 26, REST = 0;
   __host__ __device__ static constexpr int shell_end(int /*b*/, int g) { return g == 0 ? 8 : g == 1 ? 14 : 26; }
@@ -96,7 +100,7 @@ __host__ __device__ constexpr Slot fcc_shell1(int b, int k) {
 }
 
 struct FamFCC {
-  static constexpr int id = kFamFCC;
+  static constexpr int id = kFamFCC, SEP = 0;
   static constexpr int NB = 4, RX = 1, RY = 1, RZ = 1, TWO_D = 0;
   static constexpr int NSHELL = 1, Z = 12, REST = 0;
   __host__ __device__ static constexpr int shell_end(int /*b*/, int /*g*/) { return 12; }
@@ -105,7 +109,7 @@ struct FamFCC {
 
 // fcc with the second shell: the 6 same-sublattice neighbours at a
 struct FamFCC2 {
-  static constexpr int id = kFamFCC2;
+  static constexpr int id = kFamFCC2, SEP = 0;
   static constexpr int NB = 4, RX = 1, RY = 1, RZ = 1, TWO_D = 0;
   static constexpr int NSHELL = 2, Z = 18, REST = 0;
   __host__ __device__ static constexpr int shell_end(int /*b*/, int g) { return g == 0 ? 12 : 18; }
@@ -118,7 +122,7 @@ struct FamFCC2 {
 // as one shell plus a per-slot 3x3 remainder (DMI, anisotropic exchange).
 // Tile coordinates (X, Y, Z) = (a1, a3, a2).
 struct FamTRI {
-  static constexpr int id = kFamTRI;
+  static constexpr int id = kFamTRI, SEP = 0;
   static constexpr int NB = 1, RX = 1, RY = 0, RZ = 1, TWO_D = 1;
   static constexpr int NSHELL = 1, Z = 6, REST = 1;
   __host__ __device__ static constexpr int shell_end(int /*b*/, int /*g*/) { return 6; }

@@ -295,13 +295,90 @@ __device__ __forceinline__ void gather_all(std::integer_sequence<int, K...>, con
   (gather_slot<F, TZ, TY, B, K>(bm, b0, bp, axy, az, r, TP), ...);
 }
 
+// Separable bcc stencils.  Shell 1 of basis site 0 is the 2x2 block
+// (y-1..y, z-1..z) of sublattice 1 in planes x-1 and x; of site 1 the block
+// (y..y+1, z..z+1) of sublattice 0 in planes x and x+1.  Shells 2 and 3 (same
+// sublattice) are s(x-1) + s(x+1) + E(x) and E(x-1) + E(x+1) + D(x), with E
+// the in-plane cross (y +- 1, z +- 1) and D the in-plane diagonals.  Each
+// thread walks its column along x, so the block sum Q of the plane behind
+// and the cross sums E(x-1), E(x) are carried in registers from the previous
+// plane: per spin 4 (bcc) or 14 (3 shells) shared loads instead of 8 or 26.
+// The carried values are the same function of the plane data however the
+// planes are tiled, so all tilings still agree bit for bit.
+struct Carry {
+  float q[3];    // shell-1 block sum of the plane behind
+  float em[3];   // E(x - 1)
+  float e0[3];   // E(x)
+};
+
+template <class F, int TZ, int TY, int B>
+__device__ __forceinline__ void bcc_block(const float4* p, float q[3]) {
+  using G = Geo<F, TZ, TY>;
+  constexpr int bj = 1 - B;
+  constexpr int d = B == 0 ? -1 : 0;
+  const float4 a = p[(bj * G::PY + d) * G::PZ + d];
+  const float4 b = p[(bj * G::PY + d) * G::PZ + d + 1];
+  const float4 c = p[(bj * G::PY + d + 1) * G::PZ + d];
+  const float4 e = p[(bj * G::PY + d + 1) * G::PZ + d + 1];
+  q[0] = fa(fa(a.x, b.x), fa(c.x, e.x));
+  q[1] = fa(fa(a.y, b.y), fa(c.y, e.y));
+  q[2] = fa(fa(a.z, b.z), fa(c.z, e.z));
+}
+
+template <class F, int TZ, int TY, int B>
+__device__ __forceinline__ void bcc_cross(const float4* p, float e[3]) {
+  using G = Geo<F, TZ, TY>;
+  const float4 a = p[(B * G::PY + 1) * G::PZ];
+  const float4 b = p[(B * G::PY - 1) * G::PZ];
+  const float4 c = p[B * G::PY * G::PZ + 1];
+  const float4 d = p[B * G::PY * G::PZ - 1];
+  e[0] = fa(fa(a.x, b.x), fa(c.x, d.x));
+  e[1] = fa(fa(a.y, b.y), fa(c.y, d.y));
+  e[2] = fa(fa(a.z, b.z), fa(c.z, d.z));
+}
+
+template <class F, int TZ, int TY, int B>
+__device__ __forceinline__ void bcc_diag(const float4* p, float e[3]) {
+  using G = Geo<F, TZ, TY>;
+  const float4 a = p[(B * G::PY + 1) * G::PZ + 1];
+  const float4 b = p[(B * G::PY + 1) * G::PZ - 1];
+  const float4 c = p[(B * G::PY - 1) * G::PZ + 1];
+  const float4 d = p[(B * G::PY - 1) * G::PZ - 1];
+  e[0] = fa(fa(a.x, b.x), fa(c.x, d.x));
+  e[1] = fa(fa(a.y, b.y), fa(c.y, d.y));
+  e[2] = fa(fa(a.z, b.z), fa(c.z, d.z));
+}
+
+// the carried sums for the first plane x0 of a tile (ring holds x0-1..x0+1)
+template <class F, int TZ, int TY, int B>
+__device__ __forceinline__ void carry_init_b(const float4* ring, int xs, int own, Carry& c) {
+  using G = Geo<F, TZ, TY>;
+  if constexpr (F::SEP != 0) {
+    const float4* bm = ring + ((xs + 3) & 3) * G::PLANE + own;
+    const float4* b0 = ring + (xs & 3) * G::PLANE + own;
+    bcc_block<F, TZ, TY, B>(B == 0 ? bm : b0, c.q);
+    if constexpr (F::SEP == 2) {
+      bcc_cross<F, TZ, TY, B>(bm, c.em);
+      bcc_cross<F, TZ, TY, B>(b0, c.e0);
+    }
+  }
+}
+
+template <class F, int TZ, int TY>
+__device__ __forceinline__ void carry_init(int b, const float4* ring, int xs, int own, Carry& c) {
+  if constexpr (F::SEP != 0) {
+    if (b == 0) carry_init_b<F, TZ, TY, 0>(ring, xs, own, c);
+    else carry_init_b<F, TZ, TY, 1>(ring, xs, own, c);
+  }
+}
+
 // exchange field of basis site B at the thread's cell from one ring: plain
 // FP32 sum of the neighbour spins of each shell (x and y packed), then
 // h += J_shell * sum with TwoProd/TwoSum compensation; 3x3 remainders (REST
 // families) per slot
 template <class F, int TZ, int TY, int B>
 __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const float4* ring, int xs, int own,
-                                               float hi[3], float lo[3]) {
+                                               Carry& cy, float hi[3], float lo[3]) {
   using G = Geo<F, TZ, TY>;
   const float4* bm = ring + ((xs + 3) & 3) * G::PLANE + own;
   const float4* b0 = ring + (xs & 3) * G::PLANE + own;
@@ -314,7 +391,33 @@ __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const floa
     axy[g] = make_float2(0.f, 0.f);
     az[g] = 0.f;
   }
-  gather_all<F, TZ, TY, B>(std::make_integer_sequence<int, F::Z>{}, bm, b0, bp, axy, az, r, TP);
+  if constexpr (F::SEP != 0) {
+    // shell 1: carried block sum of the plane behind + this one's
+    float qn[3];
+    bcc_block<F, TZ, TY, B>(B == 0 ? b0 : bp, qn);
+    axy[0] = make_float2(fa(cy.q[0], qn[0]), fa(cy.q[1], qn[1]));
+    az[0] = fa(cy.q[2], qn[2]);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) cy.q[m] = qn[m];
+    if constexpr (F::SEP == 2) {
+      float en[3], d0[3];
+      bcc_cross<F, TZ, TY, B>(bp, en);
+      bcc_diag<F, TZ, TY, B>(b0, d0);
+      const float4 sm = bm[B * G::PY * G::PZ];
+      const float4 sp = bp[B * G::PY * G::PZ];
+      axy[1] = make_float2(fa(fa(sm.x, sp.x), cy.e0[0]), fa(fa(sm.y, sp.y), cy.e0[1]));
+      az[1] = fa(fa(sm.z, sp.z), cy.e0[2]);
+      axy[2] = make_float2(fa(fa(cy.em[0], en[0]), d0[0]), fa(fa(cy.em[1], en[1]), d0[1]));
+      az[2] = fa(fa(cy.em[2], en[2]), d0[2]);
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        cy.em[m] = cy.e0[m];
+        cy.e0[m] = en[m];
+      }
+    }
+  } else {
+    gather_all<F, TZ, TY, B>(std::make_integer_sequence<int, F::Z>{}, bm, b0, bp, axy, az, r, TP);
+  }
   // first shell: (hi, lo) is the exact product J a (TwoProd) plus the J
   // low word, no TwoSum needed; the other shells are added with TwoSum
   float2 hxy, lxy;
@@ -347,16 +450,16 @@ __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const floa
 
 template <class F, int TZ, int TY>
 __device__ __forceinline__ void exchange_dispatch(int b, const TiledParams& TP, const float4* ring, int xs, int own,
-                                                  float hi[3], float lo[3]) {
+                                                  Carry& cy, float hi[3], float lo[3]) {
   // the basis site is uniform per warp; one compile-time stencil per site
   if (F::NB == 1 || b == 0) {
-    exchange_tiled<F, TZ, TY, 0>(TP, ring, xs, own, hi, lo);
+    exchange_tiled<F, TZ, TY, 0>(TP, ring, xs, own, cy, hi, lo);
   } else if (b == 1) {
-    exchange_tiled<F, TZ, TY, (F::NB > 1 ? 1 : 0)>(TP, ring, xs, own, hi, lo);
+    exchange_tiled<F, TZ, TY, (F::NB > 1 ? 1 : 0)>(TP, ring, xs, own, cy, hi, lo);
   } else if (b == 2) {
-    exchange_tiled<F, TZ, TY, (F::NB > 2 ? 2 : 0)>(TP, ring, xs, own, hi, lo);
+    exchange_tiled<F, TZ, TY, (F::NB > 2 ? 2 : 0)>(TP, ring, xs, own, cy, hi, lo);
   } else {
-    exchange_tiled<F, TZ, TY, (F::NB > 3 ? 3 : 0)>(TP, ring, xs, own, hi, lo);
+    exchange_tiled<F, TZ, TY, (F::NB > 3 ? 3 : 0)>(TP, ring, xs, own, cy, hi, lo);
   }
   static_assert(F::NB <= 4, "at most four basis sites per family");
 }
@@ -364,7 +467,7 @@ __device__ __forceinline__ void exchange_dispatch(int b, const TiledParams& TP, 
 // total field (meV) of the thread's spin from ring `ring`
 template <class F, int TZ, int TY>
 __device__ __forceinline__ void field_tiled(const LocalField& L, const TiledParams& TP, int b, const float4* ring,
-                                           int xs, int own, float h[3], float s[3], bool has_dip,
+                                           int xs, int own, Carry& cy, float h[3], float s[3], bool has_dip,
                                            const float dip[3]) {
   using G = Geo<F, TZ, TY>;
   const float4 c = ring[(xs & 3) * G::PLANE + own + b * G::PY * G::PZ];
@@ -372,7 +475,7 @@ __device__ __forceinline__ void field_tiled(const LocalField& L, const TiledPara
   s[1] = c.y;
   s[2] = c.z;
   float hi[3], lo[3];
-  exchange_dispatch<F, TZ, TY>(b, TP, ring, xs, own, hi, lo);
+  exchange_dispatch<F, TZ, TY>(b, TP, ring, xs, own, cy, hi, lo);
   local_terms(L, s, hi, lo);
   if (has_dip) {   // the dipole field of this spin, precomputed by FFT convolution
 #pragma unroll
@@ -533,6 +636,10 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
     }
   }
   __syncthreads();
+  // carried partial sums of the separable stencils (ring1: s0 of STAGE 1)
+  Carry cy0, cy1;
+  carry_init<F, TZ, TY>(b, ring0, x0, own, cy0);
+  if (NR == 2) carry_init<F, TZ, TY>(b, ring1, x0, own, cy1);
 
   // noise of plane x + 1, drawn with plane x's when x is even (the host keeps
   // planes per CTA even, so x0 is even)
@@ -572,7 +679,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
         }
       }
       float h[3], s[3], k[3];
-      field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own, h, s, has_dip, dip);
+      field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own, cy0, h, s, has_dip, dip);
       llg_rhs_t(L, s, h, w, k);
       if (STAGE == 0) {
         float v[3] = {ff(dt, k[0], s[0]), ff(dt, k[1], s[1]), ff(dt, k[2], s[2])};
@@ -589,7 +696,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
         float a[3], r0[3];
         if (STAGE == 1) {
           float h0[3];
-          field_tiled<F, TZ, TY>(L, TP, b, ring1, x, own, h0, a, has_dip, dip0);
+          field_tiled<F, TZ, TY>(L, TP, b, ring1, x, own, cy1, h0, a, has_dip, dip0);
           llg_rhs_t(L, a, h0, w, r0);
         } else {
 #pragma unroll
