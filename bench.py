@@ -92,8 +92,12 @@ def kernel_name(info: dict, integ: str, stage: int, precision: str, dipole: bool
             st = 0 if stage == 0 else (2 if info["store_rhs"] else 1)
         else:
             st = 3 + stage
-        return "tiled_stage<%s, %d, %d, %d, %d, %s>" % (fam, info["tile_z"], info["tile_y"], st, info["occupancy"],
-                                                      "true" if dipole else "false")
+        rpt = info.get("rows_per_thread", 1) or 1
+        nt = info["tile_z"] * (info["tile_y"] // rpt) * {"fcc": 4, "fcc2": 4, "bcc": 2, "bcc3": 2}.get(
+            info["family"], 1)
+        minb = info["occupancy"] * max(1, 256 // nt)
+        return "tiled_stage<%s, %d, %d, %d, %d, %d, %s>" % (fam, info["tile_z"], info["tile_y"], rpt, st, minb,
+                                                          "true" if dipole else "false")
     suffix = "_f32" if precision == "fp32c" else "_f64"
     if integ == "heun":
         return ("heun_predict" if stage == 0 else "heun_correct") + suffix
@@ -113,7 +117,8 @@ def parse(argv=None):
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-steps", type=int, default=50)
     p.add_argument("--no-tune", action="store_true")
-    p.add_argument("--tuning", default="", help="planes_per_cta,flags,occupancy instead of autotuning (flags: 1 stored rhs, 2 narrow tile)")
+    p.add_argument("--tuning", default="", help="planes_per_cta,flags,occupancy instead of autotuning (flags: 1 stored rhs, 2 narrow tile, "
+                        "4 two rows per thread)")
     return p.parse_args(argv)
 
 
@@ -304,6 +309,14 @@ def run_reference(args, rank, world):
 
 # -------------------------------------------------------------------- GPU --
 
+def tiled_stem(name: str):
+    """(family, tile z, tile y, stage) of a tiled_stage kernel name: template
+    arguments <F, TZ, TY, RPT, STAGE, MINB, DIP>, or <F, TZ, TY, STAGE, MINB[,
+    DIP]> in captures of the kernels before rows per thread existed."""
+    args = [a.strip() for a in name[name.index("<") + 1:name.rindex(">")].split(",")]
+    return tuple(args[:3] + [args[4] if len(args) == 7 else args[3]])
+
+
 def traffic_from_profiles(workload: str, kernel: str, precision: str):
     """DRAM bytes (read + write) of one launch of `kernel` on `workload`, from
     the committed ncu summary profiles/dram_traffic.json, or None."""
@@ -315,9 +328,8 @@ def traffic_from_profiles(workload: str, kernel: str, precision: str):
         e = d.get(kernel)
         if e is None and kernel.startswith("tiled_stage<"):
             # the same family, tile and stage compiled for another occupancy
-            # moves the same bytes
-            stem = lambda k: ",".join(k.split(",")[:4])
-            e = next((v for k, v in d.items() if stem(k) == stem(kernel)), None)
+            # or rows per thread moves the same bytes
+            e = next((v for k, v in d.items() if tiled_stem(k) == tiled_stem(kernel)), None)
         return None if e is None else float(e["dram_bytes_per_launch"])
     except (ValueError, OSError, KeyError, TypeError):
         return None
@@ -352,7 +364,7 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if args.tuning:
         tx, fl, oc = (int(v) for v in args.tuning.split(","))
-        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2))
+        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2), bool(fl & 4))
         tuning = sol.kernel_info()
     else:
         # the choice is cached per lattice shape ($JAMS_LLG_TUNE_CACHE), so a

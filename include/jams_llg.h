@@ -231,15 +231,19 @@ int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
    streamed per CTA, info[2] 1 when the Heun predictor stores rhs(s0) for
    the corrector (else the corrector recomputes it), info[3..4] CTA tile
    (cells along the contiguous axis, rows), info[5] 1 for FP64, info[6] the
-   occupancy variant (CTAs per SM the tiled kernels were compiled for). */
+   occupancy variant (CTAs per SM the tiled kernels were compiled for),
+   info[7] rows computed per thread (1 or 2; 0 without tiled kernels).
+   info holds 8 values. */
 int llg_kernel_info(const llg_handle *h, int32_t *info);
 
 /* Tiling choice of the tiled FP32 kernels (no effect on other kernels):
    planes streamed per CTA (rounded up to even: the thermal noise of planes
    x and x + 1, x even, comes from one draw); flags bit 0: the Heun
    predictor stores rhs(s0); bit 1: the narrow tile (half the rows, twice
-   the CTAs, for lattices too small to fill the GPU); flags >> 4: occupancy
-   variant, 2 (<= 128 registers), 3 (<= 80) or 4 (<= 64). */
+   the CTAs, for lattices too small to fill the GPU); bit 2: two rows per
+   thread (wide tile of sc, bcc and fcc lattices, no dipole term; occupancy
+   2 only); flags >> 4: occupancy variant, 2 (<= 128 registers), 3
+   (<= 80) or 4 (<= 64). */
 int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t flags);
 
 /* Times every tiling candidate (planes per CTA 2..64, stored or recomputed

@@ -18,8 +18,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libjams_llg.so")
-SOURCES = ["llg_kernels.cu", "llg_tiled.cu", "llg_tiled_dipole.cu", "llg_observe.cu", "llg_host.cu", "llg_noalloc.cu", "llg_config.cu",
-           "llg_io.cu", "llg_dipole.cu"]
+SOURCES = ["llg_kernels.cu", "llg_tiled.cu", "llg_tiled_dipole.cu", "llg_tiled_pair.cu", "llg_observe.cu", "llg_host.cu",
+           "llg_noalloc.cu", "llg_config.cu", "llg_io.cu", "llg_dipole.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler",
               "-fPIC,-ffp-contract=off,-Wall", "-I" + os.path.join(HERE, "..", "include")]

@@ -141,6 +141,7 @@ struct llg_handle {
   bool store_mode = false;   // Heun: predictor stores rhs(s0) instead of the corrector recomputing it
   int occupancy = 2;         // tiled kernels compiled for >= 2, 3 or 4 CTAs per SM
   int tz = 0, ty = 0;
+  int rpt = 1;               // rows per thread of the tiled kernels (1 or 2)
   TiledParams TP{};
   DevBuf<int4> d_tiles4;
   // dipole-dipole term: FFT convolution state and the field planes of the
@@ -840,18 +841,18 @@ void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
       float* s0 = buf<float>(h, cur);
       float* sp = buf<float>(h, 1);
       if (stage == 0)
-        launch_tiled(h->family, h->ty, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, h->dipole != nullptr);
       else if (h->store_mode)
-        launch_tiled(h->family, h->ty, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks, h->dipole != nullptr);
       else
-        launch_tiled(h->family, h->ty, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, h->dipole != nullptr);
     } else {
       float* s0 = buf<float>(h, 0);
       float* a = buf<float>(h, 1);
       float* b = buf<float>(h, 2);
       float* in = stage == 0 ? s0 : (stage == 2 ? b : a);
       float* out = stage == 0 ? a : (stage == 1 ? b : (stage == 2 ? a : s0));
-      launch_tiled(h->family, h->ty, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, h->dipole != nullptr);
+      launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, h->dipole != nullptr);
     }
     return;
   }
@@ -1055,7 +1056,7 @@ int llg_step(llg_handle* h, int32_t nsteps) {
   constexpr size_t kMaxGraphs = 64;
   while (remaining > 0) {
     const int n = remaining >= K && K > 1 ? K : remaining;
-    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX + 8192 * h->ty, n};
+    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX + 8192 * h->ty + 131072 * h->rpt, n};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end() && (n == K || h->graphs.size() < kMaxGraphs)) {
       cudaGraph_t g;
@@ -1249,6 +1250,7 @@ int llg_kernel_info(const llg_handle* h, int32_t* info) {
   info[4] = h->ty;
   info[5] = h->fp64 ? 1 : 0;
   info[6] = h->occupancy;
+  info[7] = h->tiled ? h->rpt : 0;
   return 0;
 }
 
@@ -1256,7 +1258,7 @@ static std::string tuning_key(const llg_handle* h) {
   cudaDeviceProp prop;
   cudaGetDeviceProperties(&prop, h->device);
   std::string k = std::string(prop.name) + "|fam" + std::to_string(h->family) + "|int" +
-                  std::to_string(h->integrator) + "|nb" + std::to_string(h->nb) + "|nt" + std::to_string(h->nterms);
+                  std::to_string(h->integrator) + "|nb" + std::to_string(h->nb) + "|nt" + std::to_string(h->nterms) + "|k2";
   for (auto& R : h->reps)
     k += "|" + std::to_string(R.L[0]) + "x" + std::to_string(R.L[1]) + "x" + std::to_string(R.L[2]) +
          (R.thermal ? "T" : "0");
@@ -1313,9 +1315,16 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
   cudaError_t ce = cudaStreamSynchronize(h->stream);
   if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamSynchronize");
   drop_graphs(h);
+  // bit 2: two rows per thread (wide tile, no dipole term)
+  const bool pair = (store_rhs & 4) != 0;
+  if (pair && (!pair_rows_supported(h->family) || h->dipole || (store_rhs & 2)))
+    return h->fail(LLG_ERR_BAD_DESC, "two rows per thread: only for the wide tile of sc, bcc and fcc lattices "
+                                     "without a dipole term");
   h->store_mode = (store_rhs & 1) != 0 && h->integrator == LLG_HEUN;
   const int occ = store_rhs >> 4;
   h->occupancy = occ >= 4 ? 4 : (occ == 3 ? 3 : 2);
+  if (pair) h->occupancy = 2;   // two rows per thread need up to 128 registers
+  h->rpt = pair ? 2 : 1;
   // bit 1: the narrow tile (half the rows, twice the CTAs)
   int wide_tz = 0, wide_ty = 0;
   tiled_geometry(h->family, &wide_tz, &wide_ty);
@@ -1410,6 +1419,11 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
           if (narrow && narrow_tile_rows(h->family) == wide_ty) continue;
           cands.push_back({t, narrow | (occ << 4)});
           if (h->integrator == LLG_HEUN) cands.push_back({t, 1 | narrow | (occ << 4)});
+          // two rows per thread: wide tile, occupancy 2
+          if (!narrow && occ == 2 && pair_rows_supported(h->family) && !h->dipole) {
+            cands.push_back({t, 4 | (occ << 4)});
+            if (h->integrator == LLG_HEUN) cands.push_back({t, 5 | (occ << 4)});
+          }
         }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -1418,7 +1432,7 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   int wide_tz0 = 0, wide_ty0 = 0;
   tiled_geometry(h->family, &wide_tz0, &wide_ty0);
   std::pair<int, int> choice = {h->TP.TX, (h->store_mode ? 1 : 0) | (h->ty != wide_ty0 ? 2 : 0) |
-                                              (h->occupancy << 4)};
+                                              (h->rpt == 2 ? 4 : 0) | (h->occupancy << 4)};
   // each trial runs as llg_step runs steps: one CUDA graph of trial_steps
   // steps (captured and run once untimed, then timed)
   const int spg0 = h->steps_per_graph;

@@ -45,12 +45,14 @@ void launch_pack(bool fp64, cudaStream_t st, const void* soa, double* aos, int64
 // tiled FP32 kernels (llg_tiled.cu); family ids in llg_families.h
 void tiled_geometry(int family, int* tz, int* ty);
 // ty: tile rows (the family's wide tile from tiled_geometry or the narrow
-// one from narrow_tile_rows)
+// one from narrow_tile_rows); rpt: rows per thread, 1 or 2 (the wide tile of
+// a family that pair_rows_supported, without a dipole term)
 int narrow_tile_rows(int family);
-cudaError_t launch_tiled(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
+bool pair_rows_supported(int family);
+cudaError_t launch_tiled(int family, int ty, int rpt, int occupancy, int stage, unsigned grid, cudaStream_t st,
                          const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
                          float* aux, uint32_t k, bool dipole);
-template <bool DIP>
+template <bool DIP, int RPT>
 cudaError_t launch_tiled_t(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
                            const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
                            float* aux, uint32_t k);

@@ -4,11 +4,15 @@
 
 namespace jams_llg {
 
-template cudaError_t launch_tiled_t<false>(int, int, int, int, unsigned, cudaStream_t, const Params&,
-                                           const TiledParams&, const float*, const float*, float*, float*, uint32_t);
-extern template cudaError_t launch_tiled_t<true>(int, int, int, int, unsigned, cudaStream_t, const Params&,
-                                                 const TiledParams&, const float*, const float*, float*, float*,
-                                                 uint32_t);
+template cudaError_t launch_tiled_t<false, 1>(int, int, int, int, unsigned, cudaStream_t, const Params&,
+                                              const TiledParams&, const float*, const float*, float*, float*,
+                                              uint32_t);
+extern template cudaError_t launch_tiled_t<true, 1>(int, int, int, int, unsigned, cudaStream_t, const Params&,
+                                                    const TiledParams&, const float*, const float*, float*, float*,
+                                                    uint32_t);
+extern template cudaError_t launch_tiled_t<false, 2>(int, int, int, int, unsigned, cudaStream_t, const Params&,
+                                                     const TiledParams&, const float*, const float*, float*, float*,
+                                                     uint32_t);
 
 void tiled_geometry(int family, int* tz, int* ty) {
   switch (family) {
@@ -30,11 +34,19 @@ int narrow_tile_rows(int family) {
   return ty;
 }
 
-cudaError_t launch_tiled(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
+bool pair_rows_supported(int family) {
+  return family == kFamSC || family == kFamBCC || family == kFamBCC3 || family == kFamFCC || family == kFamFCC2;
+}
+
+cudaError_t launch_tiled(int family, int ty, int rpt, int occupancy, int stage, unsigned grid, cudaStream_t st,
                          const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
                          float* aux, uint32_t k, bool dipole) {
-  return dipole ? launch_tiled_t<true>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k)
-                : launch_tiled_t<false>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+  if (dipole) {
+    if (rpt != 1) return cudaErrorInvalidValue;
+    return launch_tiled_t<true, 1>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+  }
+  return rpt == 2 ? launch_tiled_t<false, 2>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k)
+                  : launch_tiled_t<false, 1>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
 }
 
 }  // namespace jams_llg

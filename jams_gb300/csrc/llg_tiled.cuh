@@ -245,13 +245,15 @@ __device__ __forceinline__ void normalise_t(float v[3]) {
   v[2] = fm(v[2], r);
 }
 
-template <class F, int TZ, int TY>
+// CTA tile of TZ x TY cells (all basis sites); each thread computes RPT
+// consecutive rows of one column (the ring layout does not depend on RPT)
+template <class F, int TZ, int TY, int RPT = 1>
 struct Geo {
   static constexpr int NB = F::NB;
   static constexpr int PY = TY + 2 * F::RY;
   static constexpr int PZ = TZ + 2 * F::RZ;
   static constexpr int PLANE = NB * PY * PZ;   // float4 per ring slot
-  static constexpr int NT = TZ * TY * NB;
+  static constexpr int NT = TZ * (TY / RPT) * NB;
   static constexpr int PER_THREAD = (PLANE + NT - 1) / NT;
 };
 
@@ -486,9 +488,9 @@ __device__ __forceinline__ void field_tiled(const LocalField& L, const TiledPara
 }
 
 // one ring slot worth of spins for plane x: registers, then shared memory
-template <class F, int TZ, int TY>
+template <class F, int TZ, int TY, int RPT>
 struct PlaneRegs {
-  float v[Geo<F, TZ, TY>::PER_THREAD][3];
+  float v[Geo<F, TZ, TY, RPT>::PER_THREAD][3];
 };
 
 // the replica's tile view, held in registers for the whole CTA
@@ -523,15 +525,15 @@ __device__ __forceinline__ int wrap_sel(int c, int L, bool per, bool& valid) {
 
 // the part of a thread's halo loads that does not change from plane to
 // plane: which (row, column, basis site) it loads and where it stores it
-template <class F, int TZ, int TY>
+template <class F, int TZ, int TY, int RPT>
 struct FetchPlan {
-  int idx[Geo<F, TZ, TY>::PER_THREAD];   // spin index in the plane (-1: zero / unused)
-  int dst[Geo<F, TZ, TY>::PER_THREAD];   // ring slot offset
+  int idx[Geo<F, TZ, TY, RPT>::PER_THREAD];   // spin index in the plane (-1: zero / unused)
+  int dst[Geo<F, TZ, TY, RPT>::PER_THREAD];   // ring slot offset
 };
 
-template <class F, int TZ, int TY>
-__device__ __forceinline__ void plan_fetch(const View& V, int y0, int z0, int tid, FetchPlan<F, TZ, TY>& fp) {
-  using G = Geo<F, TZ, TY>;
+template <class F, int TZ, int TY, int RPT>
+__device__ __forceinline__ void plan_fetch(const View& V, int y0, int z0, int tid, FetchPlan<F, TZ, TY, RPT>& fp) {
+  using G = Geo<F, TZ, TY, RPT>;
 #pragma unroll
   for (int q = 0; q < G::PER_THREAD; ++q) {
     const int idx = tid + q * G::NT;
@@ -547,10 +549,10 @@ __device__ __forceinline__ void plan_fetch(const View& V, int y0, int z0, int ti
   }
 }
 
-template <class F, int TZ, int TY>
+template <class F, int TZ, int TY, int RPT>
 __device__ __forceinline__ void fetch_plane(const View& V, const float* __restrict__ s, int64_t npad, int x,
-                                            const FetchPlan<F, TZ, TY>& fp, PlaneRegs<F, TZ, TY>& pr) {
-  using G = Geo<F, TZ, TY>;
+                                            const FetchPlan<F, TZ, TY, RPT>& fp, PlaneRegs<F, TZ, TY, RPT>& pr) {
+  using G = Geo<F, TZ, TY, RPT>;
   bool xvalid = true;
   const int gx = wrap_sel(x, V.L[0], V.per[0], xvalid);
   const float* sx = s + V.offset + gx * V.st[0];
@@ -564,10 +566,10 @@ __device__ __forceinline__ void fetch_plane(const View& V, const float* __restri
   }
 }
 
-template <class F, int TZ, int TY>
-__device__ __forceinline__ void store_plane(float4* ring, int x, const FetchPlan<F, TZ, TY>& fp,
-                                            const PlaneRegs<F, TZ, TY>& pr) {
-  using G = Geo<F, TZ, TY>;
+template <class F, int TZ, int TY, int RPT>
+__device__ __forceinline__ void store_plane(float4* ring, int x, const FetchPlan<F, TZ, TY, RPT>& fp,
+                                            const PlaneRegs<F, TZ, TY, RPT>& pr) {
+  using G = Geo<F, TZ, TY, RPT>;
   float4* slot = ring + (x & 3) * G::PLANE;
 #pragma unroll
   for (int q = 0; q < G::PER_THREAD; ++q)
@@ -580,13 +582,19 @@ __device__ __forceinline__ void store_plane(float4* ring, int x, const FetchPlan
 //        1 Heun corrector recomputing rhs(s0) (rings of s0 and sp)
 //        2 Heun corrector from stored rhs0 (ring of sp; own s0 and aux)
 //        3..6 RK4 stages 1..4 (ring of sin; own s0, aux = k accumulator)
-template <class F, int TZ, int TY, int STAGE, int MINB, bool DIP>
-__global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __grid_constant__ Params P,
-                                                                  const __grid_constant__ TiledParams TP,
-                                                                  const float* s0, const float* sin, float* out,
-                                                                  float* aux, uint32_t kstep) {
-  using G = Geo<F, TZ, TY>;
+// RPT: rows per thread.  With RPT = 2 a thread computes two neighbouring
+// rows of its column in every plane, so the per-plane work of a thread
+// (loop, addresses, fetch bookkeeping, barrier) is shared by two spins and
+// the two rows' neighbour loads overlap; each spin's arithmetic is the same
+// as with RPT = 1, so the results agree bit for bit.
+template <class F, int TZ, int TY, int RPT, int STAGE, int MINB, bool DIP>
+__global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
+    tiled_stage(const __grid_constant__ Params P, const __grid_constant__ TiledParams TP, const float* s0,
+                const float* sin, float* out, float* aux, uint32_t kstep) {
+  using G = Geo<F, TZ, TY, RPT>;
   constexpr int NR = STAGE == 1 ? 2 : 1;
+  constexpr int TYT = TY / RPT;   // thread rows per basis site
+  static_assert(TY % RPT == 0, "rows per thread must divide the tile rows");
   extern __shared__ float4 smem[];
   float4* ring0 = smem;                    // ring of the gathered state
   float4* ring1 = smem + 4 * G::PLANE;     // second ring (s0) for STAGE 1
@@ -597,18 +605,24 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
   const int x0 = tile.y, y0 = tile.z, z0 = tile.w;
   const int tid = threadIdx.x + TZ * threadIdx.y;
   const int tz = threadIdx.x;
-  const int ty = threadIdx.y % TY;
-  const int b = threadIdx.y / TY;
+  const int ty = (threadIdx.y % TYT) * RPT;   // the first of the thread's rows
+  const int b = threadIdx.y / TYT;
   const float amp = R.amp32[b];
-  const int y = y0 + ty, z = z0 + tz;
-  const bool active_yz = y < V.L[1] && z < V.L[2];
-  const int own = (ty + F::RY) * G::PZ + (tz + F::RZ);
+  const int z = z0 + tz;
+  bool active[RPT];   // the row's cell lies in the lattice
+  int own[RPT], yz[RPT];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    const int y = y0 + ty + r;
+    active[r] = y < V.L[1] && z < V.L[2];
+    own[r] = (ty + r + F::RY) * G::PZ + (tz + F::RZ);
+    yz[r] = y * V.st[1] + z * V.st[2] + b;
+  }
   const uint64_t step = *P.step_base + kstep;
   const float* gather_src = STAGE == 0 ? s0 : sin;
   const LocalField L = local_field(P, R, b, TP.exch_term);
   constexpr bool has_dip = DIP;   // the model has a dipole term (field planes in P.hdip32)
   const float dt = P.dt32;
-  const int yz = y * V.st[1] + z * V.st[2] + b;
   // planes of this replica (outputs, stored rhs / k sum, own start state)
   float* ox = out + V.offset;
   float* oy = ox + P.npad;
@@ -620,127 +634,160 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY>::NT, MINB) tiled_stage(const __
   const float* s0y = s0x + P.npad;
   const float* s0z = s0y + P.npad;
   const int xe = min(x0 + TP.TX, V.L[0]);
-  FetchPlan<F, TZ, TY> fp;
-  plan_fetch<F, TZ, TY>(V, y0, z0, tid, fp);
+  FetchPlan<F, TZ, TY, RPT> fp;
+  plan_fetch<F, TZ, TY, RPT>(V, y0, z0, tid, fp);
 
   {
-    PlaneRegs<F, TZ, TY> pr;
+    PlaneRegs<F, TZ, TY, RPT> pr;
 #pragma unroll
     for (int d = -1; d <= 1; ++d) {
-      fetch_plane<F, TZ, TY>(V, gather_src, P.npad, x0 + d, fp, pr);
-      store_plane<F, TZ, TY>(ring0, x0 + d, fp, pr);
+      fetch_plane<F, TZ, TY, RPT>(V, gather_src, P.npad, x0 + d, fp, pr);
+      store_plane<F, TZ, TY, RPT>(ring0, x0 + d, fp, pr);
       if (NR == 2) {
-        fetch_plane<F, TZ, TY>(V, s0, P.npad, x0 + d, fp, pr);
-        store_plane<F, TZ, TY>(ring1, x0 + d, fp, pr);
+        fetch_plane<F, TZ, TY, RPT>(V, s0, P.npad, x0 + d, fp, pr);
+        store_plane<F, TZ, TY, RPT>(ring1, x0 + d, fp, pr);
       }
     }
   }
   __syncthreads();
   // carried partial sums of the separable stencils (ring1: s0 of STAGE 1)
-  Carry cy0, cy1;
-  carry_init<F, TZ, TY>(b, ring0, x0, own, cy0);
-  if (NR == 2) carry_init<F, TZ, TY>(b, ring1, x0, own, cy1);
+  Carry cy0[RPT], cy1[RPT];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    carry_init<F, TZ, TY>(b, ring0, x0, own[r], cy0[r]);
+    if (NR == 2) carry_init<F, TZ, TY>(b, ring1, x0, own[r], cy1[r]);
+  }
 
   // noise of plane x + 1, drawn with plane x's when x is even (the host keeps
   // planes per CTA even, so x0 is even)
-  float wn[3] = {0.f, 0.f, 0.f};
+  float wn[RPT][3];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) wn[r][0] = wn[r][1] = wn[r][2] = 0.f;
   for (int x = x0; x < xe; ++x) {
     const bool more = x + 1 < xe;
-    PlaneRegs<F, TZ, TY> pf0, pf1;
+    PlaneRegs<F, TZ, TY, RPT> pf0, pf1;
     if (more) {
-      fetch_plane<F, TZ, TY>(V, gather_src, P.npad, x + 2, fp, pf0);
-      if (NR == 2) fetch_plane<F, TZ, TY>(V, s0, P.npad, x + 2, fp, pf1);
+      fetch_plane<F, TZ, TY, RPT>(V, gather_src, P.npad, x + 2, fp, pf0);
+      if (NR == 2) fetch_plane<F, TZ, TY, RPT>(V, s0, P.npad, x + 2, fp, pf1);
     }
-    if (active_yz) {
-      const int i = x * V.st[0] + yz;   // spin index in the replica
-      float w[3] = {wn[0], wn[1], wn[2]};
-      if (thermal && (x & 1) == 0) noise_pair(P.philox_keys, (uint32_t)tile.x, step, (uint32_t)i, amp, w, wn);
-      // the spin's own start-of-step state and stored rhs / k sum: loaded
-      // before the exchange sum so that the sum covers their latency
-      float own_s0[3] = {0.f, 0.f, 0.f}, own_r[3] = {0.f, 0.f, 0.f};
-      if (STAGE >= 2) {
-        own_s0[0] = __ldg(s0x + i);
-        own_s0[1] = __ldg(s0y + i);
-        own_s0[2] = __ldg(s0z + i);
-      }
-      if (STAGE == 2 || STAGE >= 4) {
-        own_r[0] = ax[i];
-        own_r[1] = ay[i];
-        own_r[2] = az[i];
-      }
-      // dipole field of the spin (input state; s0 for the recomputed rhs)
-      float dip[3] = {0.f, 0.f, 0.f}, dip0[3] = {0.f, 0.f, 0.f};
-      if (has_dip) {
+    // one row: skipped outside the lattice; two rows: both computed (rows
+    // outside the lattice see zeros in the ring), their loads and stores
+    // guarded, so that the two rows' work interleaves
+    if (RPT > 1 || active[0]) {
+      int ir[RPT];
+      float w[RPT][3];
+      // the spin's own start-of-step state, stored rhs / k sum and dipole
+      // field (input state; s0 for the recomputed rhs): loaded before the
+      // exchange sums so that the sums cover their latency
+      float own_s0[RPT][3], own_r[RPT][3], dip[RPT][3], dip0[RPT][3];
 #pragma unroll
-        for (int m = 0; m < 3; ++m) dip[m] = __ldg(P.hdip32 + m * P.npad + V.offset + i);
-        if (STAGE == 1) {
+      for (int r = 0; r < RPT; ++r) {
+        const int i = x * V.st[0] + yz[r];   // spin index in the replica
+        const bool ld = RPT == 1 || active[r];
+        ir[r] = i;
 #pragma unroll
-          for (int m = 0; m < 3; ++m) dip0[m] = __ldg(P.hdip32_s0 + m * P.npad + V.offset + i);
+        for (int m = 0; m < 3; ++m) {
+          w[r][m] = wn[r][m];
+          own_s0[r][m] = own_r[r][m] = dip[r][m] = dip0[r][m] = 0.f;
         }
-      }
-      float h[3], s[3], k[3];
-      field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own, cy0, h, s, has_dip, dip);
-      llg_rhs_t(L, s, h, w, k);
-      if (STAGE == 0) {
-        float v[3] = {ff(dt, k[0], s[0]), ff(dt, k[1], s[1]), ff(dt, k[2], s[2])};
-        normalise_t(v);
-        ox[i] = v[0];
-        oy[i] = v[1];
-        oz[i] = v[2];
-        if (ax) {
-          ax[i] = k[0];
-          ay[i] = k[1];
-          az[i] = k[2];
+        if (STAGE >= 2 && ld) {
+          own_s0[r][0] = __ldg(s0x + i);
+          own_s0[r][1] = __ldg(s0y + i);
+          own_s0[r][2] = __ldg(s0z + i);
         }
-      } else if (STAGE == 1 || STAGE == 2) {
-        float a[3], r0[3];
-        if (STAGE == 1) {
-          float h0[3];
-          field_tiled<F, TZ, TY>(L, TP, b, ring1, x, own, cy1, h0, a, has_dip, dip0);
-          llg_rhs_t(L, a, h0, w, r0);
-        } else {
+        if ((STAGE == 2 || STAGE >= 4) && ld) {
+          own_r[r][0] = ax[i];
+          own_r[r][1] = ay[i];
+          own_r[r][2] = az[i];
+        }
+        if (has_dip && ld) {
 #pragma unroll
-          for (int m = 0; m < 3; ++m) {
-            a[m] = own_s0[m];
-            r0[m] = own_r[m];
+          for (int m = 0; m < 3; ++m) dip[r][m] = __ldg(P.hdip32 + m * P.npad + V.offset + i);
+          if (STAGE == 1) {
+#pragma unroll
+            for (int m = 0; m < 3; ++m) dip0[r][m] = __ldg(P.hdip32_s0 + m * P.npad + V.offset + i);
           }
         }
-        const float hdt = fm(0.5f, dt);
-        float v[3] = {ff(hdt, fa(r0[0], k[0]), a[0]), ff(hdt, fa(r0[1], k[1]), a[1]),
-                      ff(hdt, fa(r0[2], k[2]), a[2])};
-        normalise_t(v);
-        if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
-        ox[i] = v[0];
-        oy[i] = v[1];
-        oz[i] = v[2];
-      } else {
-        const float* a = own_s0;
-        float* acc[3] = {ax, ay, az};
-        float v[3];
-        if (STAGE == 6) {
-          const float c = fm(dt, 1.0f / 6.0f);
+      }
+      if (thermal && (x & 1) == 0) {
 #pragma unroll
-          for (int m = 0; m < 3; ++m) v[m] = ff(c, fa(own_r[m], k[m]), a[m]);
+        for (int r = 0; r < RPT; ++r)
+          noise_pair(P.philox_keys, (uint32_t)tile.x, step, (uint32_t)ir[r], amp, w[r], wn[r]);
+      }
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) {
+        const int i = ir[r];
+        const bool st = RPT == 1 || active[r];
+        float h[3], s[3], k[3];
+        field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own[r], cy0[r], h, s, has_dip, dip[r]);
+        llg_rhs_t(L, s, h, w[r], k);
+        if (STAGE == 0) {
+          float v[3] = {ff(dt, k[0], s[0]), ff(dt, k[1], s[1]), ff(dt, k[2], s[2])};
           normalise_t(v);
-          if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
-        } else {
-          const float c = STAGE == 5 ? dt : fm(0.5f, dt);
-#pragma unroll
-          for (int m = 0; m < 3; ++m) {
-            const float an = STAGE == 3 ? k[m] : ff(2.0f, k[m], own_r[m]);
-            acc[m][i] = an;
-            v[m] = ff(c, k[m], a[m]);
+          if (st) {
+            ox[i] = v[0];
+            oy[i] = v[1];
+            oz[i] = v[2];
+            if (ax) {
+              ax[i] = k[0];
+              ay[i] = k[1];
+              az[i] = k[2];
+            }
           }
-          if (P.rk4_normalise_stages) normalise_t(v);
+        } else if (STAGE == 1 || STAGE == 2) {
+          float a[3], r0[3];
+          if (STAGE == 1) {
+            float h0[3];
+            field_tiled<F, TZ, TY>(L, TP, b, ring1, x, own[r], cy1[r], h0, a, has_dip, dip0[r]);
+            llg_rhs_t(L, a, h0, w[r], r0);
+          } else {
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+              a[m] = own_s0[r][m];
+              r0[m] = own_r[r][m];
+            }
+          }
+          const float hdt = fm(0.5f, dt);
+          float v[3] = {ff(hdt, fa(r0[0], k[0]), a[0]), ff(hdt, fa(r0[1], k[1]), a[1]),
+                        ff(hdt, fa(r0[2], k[2]), a[2])};
+          normalise_t(v);
+          if (st) {
+            if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
+            ox[i] = v[0];
+            oy[i] = v[1];
+            oz[i] = v[2];
+          }
+        } else {
+          const float* a = own_s0[r];
+          float* acc[3] = {ax, ay, az};
+          float v[3];
+          if (STAGE == 6) {
+            const float c = fm(dt, 1.0f / 6.0f);
+#pragma unroll
+            for (int m = 0; m < 3; ++m) v[m] = ff(c, fa(own_r[r][m], k[m]), a[m]);
+            normalise_t(v);
+            if (st && !(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
+          } else {
+            const float c = STAGE == 5 ? dt : fm(0.5f, dt);
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+              const float an = STAGE == 3 ? k[m] : ff(2.0f, k[m], own_r[r][m]);
+              if (st) acc[m][i] = an;
+              v[m] = ff(c, k[m], a[m]);
+            }
+            if (P.rk4_normalise_stages) normalise_t(v);
+          }
+          if (st) {
+            ox[i] = v[0];
+            oy[i] = v[1];
+            oz[i] = v[2];
+          }
         }
-        ox[i] = v[0];
-        oy[i] = v[1];
-        oz[i] = v[2];
       }
     }
     if (more) {
-      store_plane<F, TZ, TY>(ring0, x + 2, fp, pf0);
-      if (NR == 2) store_plane<F, TZ, TY>(ring1, x + 2, fp, pf1);
+      store_plane<F, TZ, TY, RPT>(ring0, x + 2, fp, pf0);
+      if (NR == 2) store_plane<F, TZ, TY, RPT>(ring1, x + 2, fp, pf1);
     }
     __syncthreads();
   }
@@ -755,70 +802,88 @@ size_t smem_bytes(int stage) {
   return (size_t)(stage == 1 ? 2 : 1) * 4 * Geo<F, TZ, TY>::PLANE * sizeof(float4);
 }
 
-template <class F, int TZ, int TY, int STAGE, int MINB, bool DIP>
+template <class F, int TZ, int TY, int RPT, int STAGE, int MINB, bool DIP>
 cudaError_t launch_one(unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP, const float* s0,
                        const float* sin, float* out, float* aux, uint32_t k) {
   const size_t sm = smem_bytes<F, TZ, TY>(STAGE);
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tiled_stage<F, TZ, TY, STAGE, MINB, DIP>,
+    cudaError_t e = cudaFuncSetAttribute(tiled_stage<F, TZ, TY, RPT, STAGE, MINB, DIP>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  const dim3 block(TZ, TY * F::NB);
-  tiled_stage<F, TZ, TY, STAGE, MINB, DIP><<<grid, block, sm, st>>>(P, TP, s0, sin, out, aux, k);
+  const dim3 block(TZ, (TY / RPT) * F::NB);
+  tiled_stage<F, TZ, TY, RPT, STAGE, MINB, DIP><<<grid, block, sm, st>>>(P, TP, s0, sin, out, aux, k);
   return cudaSuccess;
 }
 
-template <class F, int TZ, int TY, int MINB, bool DIP>
+template <class F, int TZ, int TY, int RPT, int MINB, bool DIP>
 cudaError_t launch_family(int stage, unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP,
                           const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
   switch (stage) {
-    case 0: return launch_one<F, TZ, TY, 0, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 1: return launch_one<F, TZ, TY, 1, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 2: return launch_one<F, TZ, TY, 2, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 3: return launch_one<F, TZ, TY, 3, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 4: return launch_one<F, TZ, TY, 4, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 5: return launch_one<F, TZ, TY, 5, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    default: return launch_one<F, TZ, TY, 6, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 0: return launch_one<F, TZ, TY, RPT, 0, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 1: return launch_one<F, TZ, TY, RPT, 1, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 2: return launch_one<F, TZ, TY, RPT, 2, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 3: return launch_one<F, TZ, TY, RPT, 3, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 4: return launch_one<F, TZ, TY, RPT, 4, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 5: return launch_one<F, TZ, TY, RPT, 5, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    default: return launch_one<F, TZ, TY, RPT, 6, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
   }
 }
 
-template <class F, int TZ, int TY, bool DIP>
+template <class F, int TZ, int TY, int RPT, bool DIP>
 cudaError_t launch_occ(int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
                        const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
   // occupancy variant, as the resident threads of 2, 3 or 4 CTAs of 256
-  // threads (up to 128, 80 or 64 registers per thread); narrow tiles of 128
-  // threads run twice as many CTAs per SM with the same register budget
-  constexpr int S = 256 / Geo<F, TZ, TY>::NT > 1 ? 256 / Geo<F, TZ, TY>::NT : 1;
-  if (occupancy >= 4) return launch_family<F, TZ, TY, 4 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
-  if (occupancy == 3) return launch_family<F, TZ, TY, 3 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
-  return launch_family<F, TZ, TY, 2 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  // threads (up to 128, 80 or 64 registers per thread); CTAs of 128 threads
+  // (narrow tiles, two rows per thread) run twice as many per SM with the
+  // same register budget.  Two rows per thread need up to 128 registers:
+  // they run at occupancy 2 only.
+  constexpr int S = 256 / Geo<F, TZ, TY, RPT>::NT > 1 ? 256 / Geo<F, TZ, TY, RPT>::NT : 1;
+  if constexpr (RPT == 1) {
+    if (occupancy >= 4) return launch_family<F, TZ, TY, 1, 4 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+    if (occupancy == 3) return launch_family<F, TZ, TY, 1, 3 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  }
+  return launch_family<F, TZ, TY, RPT, 2 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
 }
 
 }  // namespace
 
-// the tiled stage kernels with (DIP) or without the dipole field planes;
-// llg_tiled.cu instantiates DIP = false, llg_tiled_dipole.cu DIP = true
+// the tiled stage kernels with (DIP) or without the dipole field planes, one
+// (RPT = 1) or two rows per thread; llg_tiled.cu instantiates <false, 1>,
+// llg_tiled_dipole.cu <true, 1> and llg_tiled_pair.cu <false, 2>.
 // ty: rows of the CTA tile, the family's wide tile or, for simple cubic,
 // the narrow one (half the rows: twice the CTAs, for small lattices; the
 // bcc narrow tile measured slower at 64^3 and 256^3, its halo rows cost more
-// than the extra CTAs gain)
-template <bool DIP>
+// than the extra CTAs gain).  Two rows per thread: the wide tiles of the
+// families with at least two rows (not triangular).
+template <bool DIP, int RPT>
 cudaError_t launch_tiled_t(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
                            const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
                            float* aux, uint32_t k) {
-  switch (family) {
-    case kFamSC:
-      return ty == 4 ? launch_occ<FamSC, 32, 4, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k)
-                     : launch_occ<FamSC, 32, 8, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-    case kFamBCC: return launch_occ<FamBCC, 32, 4, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-    case kFamBCC3: return launch_occ<FamBCC3, 32, 4, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-    case kFamTRI: return launch_occ<FamTRI, 256, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-    case kFamFCC: return launch_occ<FamFCC, 32, 2, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-    case kFamFCC2: return launch_occ<FamFCC2, 32, 2, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-    default: return cudaErrorInvalidValue;
+  if constexpr (RPT == 1) {
+    switch (family) {
+      case kFamSC:
+        return ty == 4 ? launch_occ<FamSC, 32, 4, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k)
+                       : launch_occ<FamSC, 32, 8, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      case kFamBCC: return launch_occ<FamBCC, 32, 4, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      case kFamBCC3: return launch_occ<FamBCC3, 32, 4, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      case kFamTRI: return launch_occ<FamTRI, 256, 1, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      case kFamFCC: return launch_occ<FamFCC, 32, 2, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      case kFamFCC2: return launch_occ<FamFCC2, 32, 2, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      default: return cudaErrorInvalidValue;
+    }
+  } else {
+    if (ty != 8 && family == kFamSC) return cudaErrorInvalidValue;
+    switch (family) {
+      case kFamSC: return launch_occ<FamSC, 32, 8, RPT, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      case kFamBCC: return launch_occ<FamBCC, 32, 4, RPT, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      case kFamBCC3: return launch_occ<FamBCC3, 32, 4, RPT, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      case kFamFCC: return launch_occ<FamFCC, 32, 2, RPT, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      case kFamFCC2: return launch_occ<FamFCC2, 32, 2, RPT, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      default: return cudaErrorInvalidValue;
+    }
   }
 }
 

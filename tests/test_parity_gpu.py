@@ -258,25 +258,45 @@ def test_tiling_choices_give_identical_results(llg, name):
     """Planes per CTA and stored vs recomputed rhs(s0) change the schedule,
     not the arithmetic: states are bit-identical.  Odd plane counts are
     rounded up to even (the noise of two planes comes from one draw); the
-    narrow tile exists for simple cubic (elsewhere the flag is ignored)."""
+    narrow tile exists for simple cubic (elsewhere the flag is ignored); two
+    rows per thread exist for all but the triangular family (the odd row
+    counts leave one row of a pair outside the lattice)."""
     w = {"bcc3": W.bcc_three_shell(L=10, T=300.0, start="random"),
          "sc": W.sc_ferromagnet(L=(9, 12, 40), T=100.0),
          "tri": W.triangular_dmi_field_sweep(L=(20, 300, 1), n_fields=2, T=5.0),
          "fcc2": W.fcc_ferromagnet(L=(6, 5, 66), T=300.0, J2=0.2, start="random")}[name]
     if name == "tri":
         w.model.integrator = W.HEUN
+    if name == "sc":
+        w.replicas[0].L = (9, 13, 40)
     outs = []
-    for tx, store, occ, narrow in [(1, False, 2, False), (1, True, 4, False), (3, False, 4, False),
-                                   (4, True, 3, False), (8, True, 2, False), (64, False, 2, False),
-                                   (2, True, 4, True), (6, False, 3, True), (64, True, 2, True)]:
+    choices = [(1, False, 2, False, False), (1, True, 4, False, False), (3, False, 4, False, False),
+               (4, True, 3, False, False), (8, True, 2, False, False), (64, False, 2, False, False),
+               (2, True, 4, True, False), (6, False, 3, True, False), (64, True, 2, True, False)]
+    if name != "tri":
+        choices += [(2, False, 2, False, True), (4, True, 2, False, True), (64, True, 2, False, True)]
+    for tx, store, occ, narrow, pair in choices:
         s = solver(llg, w, llg.FP32C, steps_per_graph=4)
-        s.set_tuning(tx, store, occ, narrow)
+        s.set_tuning(tx, store, occ, narrow, pair)
+        assert s.kernel_info()["rows_per_thread"] == (2 if pair else 1)
         for r in range(len(w.replicas)):
             s.set_state(W.initial_state(w, r), r)
         s.step(11)
         outs.append(s.get_state(-1))
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
+
+
+def test_two_rows_per_thread_is_refused_where_unsupported(llg):
+    tri = W.triangular_dmi_field_sweep(L=(20, 30, 1), n_fields=1, T=5.0)
+    s = solver(llg, tri, llg.FP32C)
+    with pytest.raises(llg.LLGError, match="two rows per thread"):
+        s.set_tuning(4, False, 2, False, True)
+    sc = solver(llg, W.sc_ferromagnet(L=16), llg.FP32C)
+    with pytest.raises(llg.LLGError, match="two rows per thread"):
+        sc.set_tuning(4, False, 2, True, True)
+    sc.set_tuning(4, True, 4, False, True)   # occupancy 4 runs as 2
+    assert sc.kernel_info()["occupancy"] == 2
 
 
 def test_autotune_keeps_state_and_iteration(llg):
