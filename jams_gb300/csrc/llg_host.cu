@@ -124,6 +124,7 @@ struct llg_handle {
   DevBuf<uint16_t> d_mask[kMaxExchange];
   DevBuf<unsigned int> d_status;
   DevBuf<uint64_t> d_step_base;
+  DevBuf<unsigned int> d_ticket;
   DevBuf<double> d_scratch;        // N x 3 doubles for host transfers
   DevBuf<double> d_partials;
   std::vector<double> h_partials;
@@ -713,6 +714,7 @@ int build(llg_handle* h, const llg_desc* d) {
   if ((ce = h->d_cnt64.alloc(std::max<size_t>(cnt64.size(), 1))) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   if ((ce = h->d_status.alloc(1)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   if ((ce = h->d_step_base.alloc(1)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  if ((ce = h->d_ticket.alloc(1)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   ups.push_back({h->d_tiles.p, h->tiles.data(), h->tiles.size() * sizeof(int2)});
   if (!tab32.empty()) ups.push_back({h->d_tab32.p, tab32.data(), tab32.size() * sizeof(int32_t)});
   if (!tab64.empty()) ups.push_back({h->d_tab64.p, tab64.data(), tab64.size() * sizeof(int2)});
@@ -737,6 +739,7 @@ int build(llg_handle* h, const llg_desc* d) {
   }
   cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), h->stream);
   cudaMemsetAsync(h->d_step_base.p, 0, sizeof(uint64_t), h->stream);
+  cudaMemsetAsync(h->d_ticket.p, 0, sizeof(unsigned int), h->stream);
   P.tab32 = h->d_tab32.p;
   P.tab64 = h->d_tab64.p;
   P.cnt64 = h->d_cnt64.p;
@@ -744,6 +747,7 @@ int build(llg_handle* h, const llg_desc* d) {
   P.rep = h->d_rep.p;
   P.status = h->d_status.p;
   P.step_base = h->d_step_base.p;
+  P.ticket = h->d_ticket.p;
   size_t maxn = 0;
   for (auto& R : h->reps) maxn = std::max<size_t>(maxn, (size_t)R.n);
   if ((ce = h->d_scratch.alloc(3 * maxn)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
@@ -822,8 +826,12 @@ Real* buf(llg_handle* h, int k) {
 int num_stages(const llg_handle* h) { return h->integrator == LLG_HEUN ? 2 : 4; }
 
 // launches stage `stage` of step `ks` of a block; `cur` is the buffer that
-// holds the state at the start of the step (FP32 Heun alternates 0 and 2)
-void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t after_dipole = nullptr) {
+// holds the state at the start of the step (FP32 Heun alternates 0 and 2).
+// advance > 0: the tiled kernels advance the noise step counter by that
+// much at the end of the launch (returns true; other kernels leave it to
+// the caller)
+bool launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t after_dipole = nullptr,
+                  uint32_t advance = 0) {
   // the stage's input state (whose dipole field the stage needs)
   const void* input;
   if (h->integrator == LLG_HEUN)
@@ -841,20 +849,20 @@ void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
       float* s0 = buf<float>(h, cur);
       float* sp = buf<float>(h, 1);
       if (stage == 0)
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, advance, h->dipole != nullptr);
       else if (h->store_mode)
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks, advance, h->dipole != nullptr);
       else
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, advance, h->dipole != nullptr);
     } else {
       float* s0 = buf<float>(h, 0);
       float* a = buf<float>(h, 1);
       float* b = buf<float>(h, 2);
       float* in = stage == 0 ? s0 : (stage == 2 ? b : a);
       float* out = stage == 0 ? a : (stage == 1 ? b : (stage == 2 ? a : s0));
-      launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, h->dipole != nullptr);
+      launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, advance, h->dipole != nullptr);
     }
-    return;
+    return true;
   }
   if (h->integrator == LLG_HEUN) {
     if (h->fp64) {
@@ -890,6 +898,7 @@ void launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
       launch_rk4_f32(stage + 1, grid, st, P, (const float*)s0, (const float*)in, (float*)h->aux.p,
                      (float*)out, ks);
   }
+  return false;
 }
 
 int next_buffer(const llg_handle* h, int cur) {
@@ -897,13 +906,19 @@ int next_buffer(const llg_handle* h, int cur) {
 }
 
 // launches `nsteps` steps starting with the state in buffer `cur`; returns
-// the number of kernel launches
+// the number of kernel launches.  The last launch advances the noise step
+// counter (tiled kernels), else one more kernel does.
 int64_t enqueue_steps(llg_handle* h, int nsteps, int cur) {
   const int ns = num_stages(h);
+  bool advanced = false;
   for (int k = 0; k < nsteps; ++k) {
-    for (int stg = 0; stg < ns; ++stg) launch_stage(h, stg, (uint32_t)k, cur);
+    for (int stg = 0; stg < ns; ++stg) {
+      const bool last = k == nsteps - 1 && stg == ns - 1;
+      advanced = launch_stage(h, stg, (uint32_t)k, cur, nullptr, last ? (uint32_t)nsteps : 0u) && last;
+    }
     cur = next_buffer(h, cur);
   }
+  if (advanced) return (int64_t)nsteps * ns;
   advance_step_base<<<1, 1, 0, h->stream>>>(h->d_step_base.p, (uint32_t)nsteps);
   return (int64_t)nsteps * ns + 1;
 }
@@ -1074,7 +1089,7 @@ int llg_step(llg_handle* h, int32_t nsteps) {
     if (it != h->graphs.end()) {
       cudaError_t ce = cudaGraphLaunch(it->second, h->stream);
       if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaGraphLaunch");
-      h->last_launches += (int64_t)n * (h->integrator == LLG_HEUN ? 2 : 4) + 1;
+      h->last_launches += (int64_t)n * (h->integrator == LLG_HEUN ? 2 : 4) + (h->tiled ? 0 : 1);
     } else {
       h->last_launches += enqueue_steps(h, n, h->cur);
     }

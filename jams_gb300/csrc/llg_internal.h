@@ -119,7 +119,8 @@ struct Params {
   uint64_t seed;
   int rk4_normalise_stages;
   unsigned int* status;   // bit 0: non-finite spin
-  const uint64_t* step_base;  // iteration number of step 0 of a launch block
+  uint64_t* step_base;        // iteration number of step 0 of a launch block
+  unsigned int* ticket;       // CTAs finished in the launch that advances step_base
   uint32_t philox_keys[20];   // Philox4x32-10 round keys of the seed
   // dipole field planes (meV, three planes of npad) of the stage's input
   // state and of the start-of-step state; null without a dipole term

@@ -51,11 +51,11 @@ int narrow_tile_rows(int family);
 bool pair_rows_supported(int family);
 cudaError_t launch_tiled(int family, int ty, int rpt, int occupancy, int stage, unsigned grid, cudaStream_t st,
                          const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
-                         float* aux, uint32_t k, bool dipole);
+                         float* aux, uint32_t k, uint32_t advance, bool dipole);
 template <bool DIP, int RPT>
 cudaError_t launch_tiled_t(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
                            const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
-                           float* aux, uint32_t k);
+                           float* aux, uint32_t k, uint32_t adv);
 
 // observables (llg_observe.cu): ordered per-tile partial sums copied to
 // h_partials [ntiles][nq] = (sum mu_s Sx, Sy, Sz, sum mu_s, E_term...)

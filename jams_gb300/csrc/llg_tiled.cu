@@ -6,13 +6,13 @@ namespace jams_llg {
 
 template cudaError_t launch_tiled_t<false, 1>(int, int, int, int, unsigned, cudaStream_t, const Params&,
                                               const TiledParams&, const float*, const float*, float*, float*,
-                                              uint32_t);
+                                              uint32_t, uint32_t);
 extern template cudaError_t launch_tiled_t<true, 1>(int, int, int, int, unsigned, cudaStream_t, const Params&,
                                                     const TiledParams&, const float*, const float*, float*, float*,
-                                                    uint32_t);
+                                                    uint32_t, uint32_t);
 extern template cudaError_t launch_tiled_t<false, 2>(int, int, int, int, unsigned, cudaStream_t, const Params&,
                                                      const TiledParams&, const float*, const float*, float*, float*,
-                                                     uint32_t);
+                                                     uint32_t, uint32_t);
 
 void tiled_geometry(int family, int* tz, int* ty) {
   switch (family) {
@@ -40,13 +40,14 @@ bool pair_rows_supported(int family) {
 
 cudaError_t launch_tiled(int family, int ty, int rpt, int occupancy, int stage, unsigned grid, cudaStream_t st,
                          const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
-                         float* aux, uint32_t k, bool dipole) {
+                         float* aux, uint32_t k, uint32_t advance, bool dipole) {
   if (dipole) {
     if (rpt != 1) return cudaErrorInvalidValue;
-    return launch_tiled_t<true, 1>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+    return launch_tiled_t<true, 1>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, advance);
   }
-  return rpt == 2 ? launch_tiled_t<false, 2>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k)
-                  : launch_tiled_t<false, 1>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+  if (rpt == 2)
+    return launch_tiled_t<false, 2>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, advance);
+  return launch_tiled_t<false, 1>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, advance);
 }
 
 }  // namespace jams_llg

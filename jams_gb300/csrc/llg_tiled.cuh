@@ -590,7 +590,7 @@ __device__ __forceinline__ void store_plane(float4* ring, int x, const FetchPlan
 template <class F, int TZ, int TY, int RPT, int STAGE, int MINB, bool DIP>
 __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     tiled_stage(const __grid_constant__ Params P, const __grid_constant__ TiledParams TP, const float* s0,
-                const float* sin, float* out, float* aux, uint32_t kstep) {
+                const float* sin, float* out, float* aux, uint32_t kstep, uint32_t advance) {
   using G = Geo<F, TZ, TY, RPT>;
   constexpr int NR = STAGE == 1 ? 2 : 1;
   constexpr int TYT = TY / RPT;   // thread rows per basis site
@@ -598,6 +598,10 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   extern __shared__ float4 smem[];
   float4* ring0 = smem;                    // ring of the gathered state
   float4* ring1 = smem + 4 * G::PLANE;     // second ring (s0) for STAGE 1
+  // programmatic dependent launch: the next stage's CTAs may be scheduled
+  // once every CTA of this one has started; they set up, then wait for this
+  // launch to complete before they read what it wrote
+  asm volatile("griddepcontrol.launch_dependents;");
   const int4 tile = TP.tiles[blockIdx.x];
   const ReplicaDev& R = P.rep[tile.x];
   const View V = load_view(R);
@@ -618,7 +622,6 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     own[r] = (ty + r + F::RY) * G::PZ + (tz + F::RZ);
     yz[r] = y * V.st[1] + z * V.st[2] + b;
   }
-  const uint64_t step = *P.step_base + kstep;
   const float* gather_src = STAGE == 0 ? s0 : sin;
   const LocalField L = local_field(P, R, b, TP.exch_term);
   constexpr bool has_dip = DIP;   // the model has a dipole term (field planes in P.hdip32)
@@ -636,6 +639,11 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   const int xe = min(x0 + TP.TX, V.L[0]);
   FetchPlan<F, TZ, TY, RPT> fp;
   plan_fetch<F, TZ, TY, RPT>(V, y0, z0, tid, fp);
+  // everything below reads the output of earlier launches (spins, stored
+  // rhs, dipole field, step counter): wait for them to complete (returns at
+  // once for a launch without a programmatic dependency)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const uint64_t step = *P.step_base + kstep;
 
   {
     PlaneRegs<F, TZ, TY, RPT> pr;
@@ -791,6 +799,17 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     }
     __syncthreads();
   }
+  // the launch that ends a block of steps advances the noise step counter by
+  // `advance`: the last CTA to finish does it, when every CTA has read the
+  // counter (each read precedes its CTA's barriers and its ticket)
+  if (advance != 0 && tid == 0) {
+    __threadfence();
+    if (atomicAdd(P.ticket, 1u) == gridDim.x - 1) {
+      *P.step_base += advance;
+      *P.ticket = 0u;
+      __threadfence();
+    }
+  }
 }
 
 // ------------------------------------------------------------ launchers --
@@ -804,7 +823,7 @@ size_t smem_bytes(int stage) {
 
 template <class F, int TZ, int TY, int RPT, int STAGE, int MINB, bool DIP>
 cudaError_t launch_one(unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP, const float* s0,
-                       const float* sin, float* out, float* aux, uint32_t k) {
+                       const float* sin, float* out, float* aux, uint32_t k, uint32_t adv) {
   const size_t sm = smem_bytes<F, TZ, TY>(STAGE);
   static bool attr = false;
   if (!attr) {
@@ -813,28 +832,40 @@ cudaError_t launch_one(unsigned grid, cudaStream_t st, const Params& P, const Ti
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  const dim3 block(TZ, (TY / RPT) * F::NB);
-  tiled_stage<F, TZ, TY, RPT, STAGE, MINB, DIP><<<grid, block, sm, st>>>(P, TP, s0, sin, out, aux, k);
-  return cudaSuccess;
+  // launched with programmatic stream serialisation: its setup overlaps the
+  // end of the previous kernel in the stream (CUDA graphs keep the
+  // programmatic edge)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(TZ, (TY / RPT) * F::NB);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, tiled_stage<F, TZ, TY, RPT, STAGE, MINB, DIP>, P, TP, s0, sin, out, aux, k, adv);
 }
 
 template <class F, int TZ, int TY, int RPT, int MINB, bool DIP>
 cudaError_t launch_family(int stage, unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP,
-                          const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
+                          const float* s0, const float* sin, float* out, float* aux, uint32_t k, uint32_t adv) {
   switch (stage) {
-    case 0: return launch_one<F, TZ, TY, RPT, 0, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 1: return launch_one<F, TZ, TY, RPT, 1, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 2: return launch_one<F, TZ, TY, RPT, 2, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 3: return launch_one<F, TZ, TY, RPT, 3, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 4: return launch_one<F, TZ, TY, RPT, 4, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    case 5: return launch_one<F, TZ, TY, RPT, 5, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
-    default: return launch_one<F, TZ, TY, RPT, 6, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k);
+    case 0: return launch_one<F, TZ, TY, RPT, 0, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
+    case 1: return launch_one<F, TZ, TY, RPT, 1, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
+    case 2: return launch_one<F, TZ, TY, RPT, 2, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
+    case 3: return launch_one<F, TZ, TY, RPT, 3, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
+    case 4: return launch_one<F, TZ, TY, RPT, 4, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
+    case 5: return launch_one<F, TZ, TY, RPT, 5, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
+    default: return launch_one<F, TZ, TY, RPT, 6, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
   }
 }
 
 template <class F, int TZ, int TY, int RPT, bool DIP>
 cudaError_t launch_occ(int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
-                       const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux, uint32_t k) {
+                       const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux, uint32_t k,
+                       uint32_t adv) {
   // occupancy variant, as the resident threads of 2, 3 or 4 CTAs of 256
   // threads (up to 128, 80 or 64 registers per thread); CTAs of 128 threads
   // (narrow tiles, two rows per thread) run twice as many per SM with the
@@ -842,10 +873,12 @@ cudaError_t launch_occ(int occupancy, int stage, unsigned grid, cudaStream_t st,
   // they run at occupancy 2 only.
   constexpr int S = 256 / Geo<F, TZ, TY, RPT>::NT > 1 ? 256 / Geo<F, TZ, TY, RPT>::NT : 1;
   if constexpr (RPT == 1) {
-    if (occupancy >= 4) return launch_family<F, TZ, TY, 1, 4 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
-    if (occupancy == 3) return launch_family<F, TZ, TY, 1, 3 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+    if (occupancy >= 4) return launch_family<F, TZ, TY, 1, 4 * S, DIP>
+        (stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+    if (occupancy == 3) return launch_family<F, TZ, TY, 1, 3 * S, DIP>
+        (stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
   }
-  return launch_family<F, TZ, TY, RPT, 2 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k);
+  return launch_family<F, TZ, TY, RPT, 2 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
 }
 
 }  // namespace
@@ -861,27 +894,39 @@ cudaError_t launch_occ(int occupancy, int stage, unsigned grid, cudaStream_t st,
 template <bool DIP, int RPT>
 cudaError_t launch_tiled_t(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
                            const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
-                           float* aux, uint32_t k) {
+                           float* aux, uint32_t k, uint32_t adv) {
   if constexpr (RPT == 1) {
     switch (family) {
       case kFamSC:
-        return ty == 4 ? launch_occ<FamSC, 32, 4, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k)
-                       : launch_occ<FamSC, 32, 8, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-      case kFamBCC: return launch_occ<FamBCC, 32, 4, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-      case kFamBCC3: return launch_occ<FamBCC3, 32, 4, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-      case kFamTRI: return launch_occ<FamTRI, 256, 1, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-      case kFamFCC: return launch_occ<FamFCC, 32, 2, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-      case kFamFCC2: return launch_occ<FamFCC2, 32, 2, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+        return ty == 4 ? launch_occ<FamSC, 32, 4, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k,
+                                                          adv)
+                       : launch_occ<FamSC, 32, 8, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k,
+                                                          adv);
+      case kFamBCC: return launch_occ<FamBCC, 32, 4, 1, DIP>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+      case kFamBCC3: return launch_occ<FamBCC3, 32, 4, 1, DIP>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+      case kFamTRI: return launch_occ<FamTRI, 256, 1, 1, DIP>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+      case kFamFCC: return launch_occ<FamFCC, 32, 2, 1, DIP>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+      case kFamFCC2: return launch_occ<FamFCC2, 32, 2, 1, DIP>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
       default: return cudaErrorInvalidValue;
     }
   } else {
     if (ty != 8 && family == kFamSC) return cudaErrorInvalidValue;
     switch (family) {
-      case kFamSC: return launch_occ<FamSC, 32, 8, RPT, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-      case kFamBCC: return launch_occ<FamBCC, 32, 4, RPT, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-      case kFamBCC3: return launch_occ<FamBCC3, 32, 4, RPT, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-      case kFamFCC: return launch_occ<FamFCC, 32, 2, RPT, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
-      case kFamFCC2: return launch_occ<FamFCC2, 32, 2, RPT, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k);
+      case kFamSC: return launch_occ<FamSC, 32, 8, RPT, DIP>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+      case kFamBCC: return launch_occ<FamBCC, 32, 4, RPT, DIP>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+      case kFamBCC3: return launch_occ<FamBCC3, 32, 4, RPT, DIP>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+      case kFamFCC: return launch_occ<FamFCC, 32, 2, RPT, DIP>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+      case kFamFCC2: return launch_occ<FamFCC2, 32, 2, RPT, DIP>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
       default: return cudaErrorInvalidValue;
     }
   }

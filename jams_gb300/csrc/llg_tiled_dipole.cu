@@ -5,6 +5,6 @@
 namespace jams_llg {
 
 template cudaError_t launch_tiled_t<true, 1>(int, int, int, int, unsigned, cudaStream_t, const Params&,
-                                             const TiledParams&, const float*, const float*, float*, float*, uint32_t);
+                                             const TiledParams&, const float*, const float*, float*, float*, uint32_t, uint32_t);
 
 }  // namespace jams_llg
