@@ -313,6 +313,8 @@ def tiled_stem(name: str):
     """(family, tile z, tile y, stage) of a tiled_stage kernel name: template
     arguments <F, TZ, TY, RPT, STAGE, MINB, DIP>, or <F, TZ, TY, STAGE, MINB[,
     DIP]> in captures of the kernels before rows per thread existed."""
+    if not name.startswith("tiled_stage<"):
+        return None
     args = [a.strip() for a in name[name.index("<") + 1:name.rindex(">")].split(",")]
     return tuple(args[:3] + [args[4] if len(args) == 7 else args[3]])
 
@@ -329,7 +331,8 @@ def traffic_from_profiles(workload: str, kernel: str, precision: str):
         if e is None and kernel.startswith("tiled_stage<"):
             # the same family, tile and stage compiled for another occupancy
             # or rows per thread moves the same bytes
-            e = next((v for k, v in d.items() if tiled_stem(k) == tiled_stem(kernel)), None)
+            e = next((v for k, v in d.items() if k.startswith("tiled_stage<") and tiled_stem(k) == tiled_stem(kernel)),
+                     None)
         return None if e is None else float(e["dram_bytes_per_launch"])
     except (ValueError, OSError, KeyError, TypeError):
         return None
