@@ -84,6 +84,15 @@ struct DevBuf {
   }
 };
 
+// a pinned host word the status flag is copied into
+struct PinnedWord {
+  unsigned int* p = nullptr;
+  ~PinnedWord() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t alloc() { return p ? cudaSuccess : cudaHostAlloc((void**)&p, sizeof(unsigned int), cudaHostAllocDefault); }
+};
+
 struct GraphKey {
   int parity;
   int nsteps;
@@ -123,6 +132,7 @@ struct llg_handle {
   DevBuf<double> d_J64[kMaxExchange];
   DevBuf<uint16_t> d_mask[kMaxExchange];
   DevBuf<unsigned int> d_status;
+  PinnedWord h_status;
   DevBuf<uint64_t> d_step_base;
   DevBuf<unsigned int> d_ticket;
   DevBuf<double> d_scratch;        // N x 3 doubles for host transfers
@@ -713,6 +723,7 @@ int build(llg_handle* h, const llg_desc* d) {
   if ((ce = h->d_tab64.alloc(std::max<size_t>(tab64.size(), 1))) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   if ((ce = h->d_cnt64.alloc(std::max<size_t>(cnt64.size(), 1))) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   if ((ce = h->d_status.alloc(1)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+  if ((ce = h->h_status.alloc()) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   if ((ce = h->d_step_base.alloc(1)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   if ((ce = h->d_ticket.alloc(1)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   ups.push_back({h->d_tiles.p, h->tiles.data(), h->tiles.size() * sizeof(int2)});
@@ -979,9 +990,9 @@ int32_t llg_num_replicas(const llg_handle* h) { return h ? (int32_t)h->reps.size
 
 // the device address of a pinned, mapped host buffer (the unpack kernel then
 // reads it in place over the host link, in one pass with the layout
-// conversion), or null for pageable memory (copied by the DMA engines through
-// the device scratch buffer).  Results go back through the DMA engines: a
-// kernel's strided stores to host memory measured 2.6x slower.
+// conversion, and the pack kernel writes it in place with whole-line
+// stores), or null for pageable memory (copied by the DMA engines through
+// the device scratch buffer)
 static void* mapped_host(const void* p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -1021,11 +1032,17 @@ static int transfer_state(llg_handle* h, int32_t replica, const double* src, dou
       }
     } else {
       double* d = dst + 3 * host_off;
+      // pinned (mapped) host buffers are written in place by the pack kernel,
+      // whole cache lines at a time; other host buffers through a copy
+      void* m = device_ptr ? nullptr : mapped_host(d);
       if (device_ptr) dev_aos = d;
+      else if (m) dev_aos = static_cast<double*>(m);
       launch_pack(h->fp64, h->stream, h->state[sb].p, dev_aos, R.offset, R.n, h->npad);
-      if (!device_ptr) {
+      if (!device_ptr && !m) {
         ce = cudaMemcpyAsync(d, dev_aos, bytes, cudaMemcpyDeviceToHost, h->stream);
         if (ce != cudaSuccess) return h->cuda_fail(ce, "copying spins to the host");
+      }
+      if (!device_ptr) {
         ce = cudaStreamSynchronize(h->stream);
         if (ce != cudaSuccess) return h->cuda_fail(ce, "getting spins");
       }
@@ -1110,12 +1127,13 @@ int llg_step(llg_handle* h, int32_t nsteps) {
 int llg_synchronize(llg_handle* h) {
   if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
   cudaSetDevice(h->device);
-  cudaError_t ce = cudaStreamSynchronize(h->stream);
-  if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamSynchronize");
-  unsigned int status = 0;
-  ce = cudaMemcpy(&status, h->d_status.p, sizeof status, cudaMemcpyDeviceToHost);
+  // the status word comes back with the stream's work: one synchronisation
+  cudaError_t ce = cudaMemcpyAsync(h->h_status.p, h->d_status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                   h->stream);
   if (ce != cudaSuccess) return h->cuda_fail(ce, "reading status");
-  if (status & 1u) return h->fail(LLG_ERR_NONFINITE, "a spin became NaN or infinite");
+  ce = cudaStreamSynchronize(h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamSynchronize");
+  if (*h->h_status.p & 1u) return h->fail(LLG_ERR_NONFINITE, "a spin became NaN or infinite");
   return 0;
 }
 

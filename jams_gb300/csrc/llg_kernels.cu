@@ -683,14 +683,34 @@ __global__ void unpack_state(const double* __restrict__ aos, Real* __restrict__ 
   soa[2 * npad + offset + i] = (Real)aos[3 * i + 2];
 }
 
+// SoA planes -> AoS doubles for 256 spins per block, staged through shared
+// memory so that each warp writes 512 contiguous bytes (16-byte words when
+// the destination is 16-byte aligned): whole cache lines, which matters most
+// when the destination is mapped host memory across the host link
 template <typename Real>
-__global__ void pack_state(const Real* __restrict__ soa, double* __restrict__ aos, int64_t offset, int64_t n,
-                           int64_t npad) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  aos[3 * i] = (double)soa[offset + i];
-  aos[3 * i + 1] = (double)soa[npad + offset + i];
-  aos[3 * i + 2] = (double)soa[2 * npad + offset + i];
+__global__ void __launch_bounds__(256) pack_state(const Real* __restrict__ soa, double* __restrict__ aos,
+                                                  int64_t offset, int64_t n, int64_t npad) {
+  __shared__ __align__(16) double buf[3 * 256];
+  const int64_t base = (int64_t)blockIdx.x * 256;
+  const int cnt = (int)min((int64_t)256, n - base);
+  const int t = threadIdx.x;
+  if (t < cnt) {
+    const int64_t i = offset + base + t;
+    buf[3 * t] = (double)soa[i];
+    buf[3 * t + 1] = (double)soa[npad + i];
+    buf[3 * t + 2] = (double)soa[2 * npad + i];
+  }
+  __syncthreads();
+  double* out = aos + 3 * base;   // 6144-byte steps: every block has the alignment of aos
+  const int words = 3 * cnt;
+  if ((reinterpret_cast<uintptr_t>(out) & 15u) == 0) {
+    double2* o2 = reinterpret_cast<double2*>(out);
+    const double2* b2 = reinterpret_cast<const double2*>(buf);
+    for (int k = t; k < words / 2; k += 256) o2[k] = b2[k];
+    if ((words & 1) && t == 0) out[words - 1] = buf[words - 1];
+  } else {
+    for (int k = t; k < words; k += 256) out[k] = buf[k];
+  }
 }
 
 template __global__ void unpack_state<float>(const double*, float*, int64_t, int64_t, int64_t);
