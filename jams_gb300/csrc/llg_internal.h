@@ -78,7 +78,7 @@ struct ReplicaDev {
   int32_t vper[3];
 };
 
-// runtime data of the tiled FP32 kernels (llg_tiled.cu)
+// runtime data of the tiled FP32 kernels (llg_tiled.cuh)
 struct TiledParams {
   const int4* tiles;      // (replica, x0, y0, z0) per CTA
   int ntiles;

@@ -42,7 +42,7 @@ void launch_unpack(bool fp64, cudaStream_t st, const double* aos, void* soa, int
 void launch_pack(bool fp64, cudaStream_t st, const void* soa, double* aos, int64_t offset, int64_t n,
                  int64_t npad);
 
-// tiled FP32 kernels (llg_tiled.cu); family ids in llg_families.h
+// tiled FP32 kernels (llg_tiled.cuh, instantiated by llg_tiled*.cu); family ids in llg_families.h
 void tiled_geometry(int family, int* tz, int* ty);
 // ty: tile rows (the family's wide tile from tiled_geometry or the narrow
 // one from narrow_tile_rows); rpt: rows per thread, 1 or 2 (the wide tile of

@@ -1,7 +1,8 @@
 // Tiled FP32 stage kernels for lattices that match a compile-time stencil
-// family (llg_families.h).  Implementation header: llg_tiled.cu compiles the
-// kernels of models without a dipole term, llg_tiled_dipole.cu those with one
-// (DIP: the dipole field planes are read and added), in parallel.
+// family (llg_families.h).  Implementation header, compiled in parallel by
+// llg_tiled.cu (one row per thread, no dipole term), llg_tiled_dipole.cu
+// (DIP: the dipole field planes are read and added) and llg_tiled_pair.cu
+// (two rows per thread).
 //
 // 2.5-D streaming: a CTA owns a TY x TZ patch of cells (all basis sites) and
 // walks TX planes along the slowest axis X.  The spins of planes x-1, x, x+1
