@@ -1145,6 +1145,8 @@ int llg_set_iteration(llg_handle* h, int64_t iteration) {
   cudaSetDevice(h->device);
   uint64_t v = (uint64_t)iteration;
   cudaError_t ce = cudaMemcpyAsync(h->d_step_base.p, &v, sizeof v, cudaMemcpyHostToDevice, h->stream);
+  // the completion ticket of the launch that advances the counter starts at 0
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(h->d_ticket.p, 0, sizeof(unsigned int), h->stream);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->stream);
   if (ce != cudaSuccess) return h->cuda_fail(ce, "setting the iteration");
   h->iteration = iteration;
