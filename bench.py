@@ -96,8 +96,8 @@ def kernel_name(info: dict, integ: str, stage: int, precision: str, dipole: bool
         nt = info["tile_z"] * (info["tile_y"] // rpt) * {"fcc": 4, "fcc2": 4, "bcc": 2, "bcc3": 2}.get(
             info["family"], 1)
         minb = info["occupancy"] * max(1, 256 // nt)
-        return "tiled_stage<%s, %d, %d, %d, %d, %d, %s>" % (fam, info["tile_z"], info["tile_y"], rpt, st, minb,
-                                                          "true" if dipole else "false")
+        return "tiled_stage<%s, %d, %d, %d, %d, %d, %d>" % (fam, info["tile_z"], info["tile_y"], rpt, st, minb,
+                                                          1 if dipole else 0)
     suffix = "_f32" if precision == "fp32c" else "_f64"
     if integ == "heun":
         return ("heun_predict" if stage == 0 else "heun_correct") + suffix
