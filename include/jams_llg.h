@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define LLG_ABI_VERSION 2
+#define LLG_ABI_VERSION 3
 
 /* status codes */
 enum {
@@ -68,10 +68,22 @@ enum {
   LLG_TERM_EXCHANGE = 0,      /* module "exchange": bilinear 3x3 tensors */
   LLG_TERM_UNIAXIAL = 1,      /* module "uniaxial": -K (S.a)^p, p = 2, 4, 6 */
   LLG_TERM_CUBIC = 2,         /* module "cubic": K1 or K2 cubic anisotropy */
-  LLG_TERM_APPLIED_FIELD = 3, /* module "applied-field"/"zeeman": mu_s B */
-  LLG_TERM_DIPOLE = 4         /* modules "dipole-fft" (and its brute-force,
+  LLG_TERM_APPLIED_FIELD = 3, /* module "applied-field": mu_s B f(t), with
+                                 f = 1 or a sinc / sinc-cos pulse */
+  LLG_TERM_DIPOLE = 4,        /* modules "dipole-fft" (and its brute-force,
                                  tensor, neighbour-list, near-tree twins):
                                  magnetic dipole-dipole field within a cutoff */
+  LLG_TERM_ZEEMAN = 5         /* module "zeeman": mu_s (B_dc + B_ac cos(w t))
+                                 per basis site */
+};
+
+/* time dependence of an applied-field term (src/jams/hamiltonian/
+   applied_field.cc:10-103), t in ps at the stage's time (Heun: t0, t0 + dt;
+   RK4: t0, t0 + dt/2, t0 + dt/2, t0 + dt; t0 = iteration * dt) */
+enum {
+  LLG_PULSE_STATIC = 0,   /* B */
+  LLG_PULSE_SINC = 1,     /* B sinc(pi f_bw (t - t_c)) */
+  LLG_PULSE_SINC_COS = 2  /* B sinc(pi f_bw (t - t_c)) cos(2 pi f_c (t - t_c)) */
 };
 
 typedef struct {
@@ -103,6 +115,18 @@ typedef struct {
   double lattice_parameter;
   const double *lattice_vectors;  /* 9 */
   const double *positions;        /* 3 nb */
+  /* applied field: LLG_PULSE_* and its centre time (ps), bandwidth and
+     centre frequency (THz) */
+  int32_t pulse;
+  double time_center;
+  double freq_bandwidth;
+  double freq_center;
+  /* zeeman (src/jams/hamiltonian/zeeman.cc:12-71,106-121): per basis site
+     the dc field (T, 3 nb), the ac field (T, 3 nb; null: none) and its
+     frequency (THz, nb; the angular frequency is 2 pi times it) */
+  const double *dc_field;
+  const double *ac_field;
+  const double *ac_frequency;
 } llg_term;
 
 typedef struct {

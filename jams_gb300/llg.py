@@ -17,7 +17,7 @@ from . import workloads as W
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libjams_llg.so")
 
-LLG_ABI_VERSION = 2
+LLG_ABI_VERSION = 3
 FP64 = 0
 FP32C = 1
 HEUN = 0
@@ -56,6 +56,9 @@ class LlgTerm(ctypes.Structure):
         ("r_cutoff", ctypes.c_double), ("distance_tolerance", ctypes.c_double),
         ("lattice_parameter", ctypes.c_double), ("lattice_vectors", ctypes.POINTER(ctypes.c_double)),
         ("positions", ctypes.POINTER(ctypes.c_double)),
+        ("pulse", ctypes.c_int32), ("time_center", ctypes.c_double), ("freq_bandwidth", ctypes.c_double),
+        ("freq_center", ctypes.c_double), ("dc_field", ctypes.POINTER(ctypes.c_double)),
+        ("ac_field", ctypes.POINTER(ctypes.c_double)), ("ac_frequency", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -218,6 +221,14 @@ class Solver:
                 lt.r_cutoff, lt.distance_tolerance = float(t.r_cutoff), float(t.distance_tolerance)
                 lt.lattice_parameter = float(t.lattice_parameter)
                 lt.lattice_vectors, lt.positions = _dp(vec), _dp(pos)
+            lt.pulse, lt.time_center = int(t.pulse), float(t.time_center)
+            lt.freq_bandwidth, lt.freq_center = float(t.freq_bandwidth), float(t.freq_center)
+            for name in ("dc_field", "ac_field", "ac_frequency"):
+                v = getattr(t, name)
+                if v is not None:
+                    a = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+                    self._keep.append(a)
+                    setattr(lt, name, _dp(a))
         reps = (LlgReplica * len(workload.replicas))()
         for r, rp in enumerate(workload.replicas):
             for j in range(3):

@@ -38,6 +38,8 @@ TERM_UNIAXIAL = 1
 TERM_CUBIC = 2
 TERM_APPLIED_FIELD = 3
 TERM_DIPOLE = 4
+TERM_ZEEMAN = 5
+PULSE_STATIC, PULSE_SINC, PULSE_SINC_COS = 0, 1, 2
 
 HEUN = 0
 RK4 = 1
@@ -67,6 +69,16 @@ class Term:
     lattice_parameter: float = 0.0
     lattice_vectors: Optional[np.ndarray] = None  # (3, 3)
     positions: Optional[np.ndarray] = None  # (nb, 3)
+    # applied-field pulse: PULSE_*, centre time (ps), bandwidth and centre
+    # frequency (THz)
+    pulse: int = PULSE_STATIC
+    time_center: float = 0.0
+    freq_bandwidth: float = 0.0
+    freq_center: float = 0.0
+    # zeeman: dc and ac field per basis site (T, (nb, 3)), ac frequency (THz, (nb,))
+    dc_field: Optional[np.ndarray] = None
+    ac_field: Optional[np.ndarray] = None
+    ac_frequency: Optional[np.ndarray] = None
     name: str = ""
 
 
@@ -146,8 +158,23 @@ def cubic_term(nb: int, K: float, order: int = 1, u=(1, 0, 0), v=(0, 1, 0), w=(0
                 axis=np.tile(ax, (nb, 1, 1)), name="cubic")
 
 
-def field_term(B) -> Term:
-    return Term(kind=TERM_APPLIED_FIELD, B=tuple(float(b) for b in B), name="applied-field")
+def field_term(B, pulse=PULSE_STATIC, time_center=0.0, freq_bandwidth=0.0, freq_center=0.0) -> Term:
+    """Applied field B (T), static or times a sinc / sinc-cos pulse (centre
+    time in ps, bandwidth and centre frequency in THz)."""
+    return Term(kind=TERM_APPLIED_FIELD, B=tuple(float(b) for b in B), pulse=int(pulse),
+                time_center=float(time_center), freq_bandwidth=float(freq_bandwidth),
+                freq_center=float(freq_center), name="applied-field")
+
+
+def zeeman_term(dc, ac=None, frequency=None) -> Term:
+    """Zeeman term: per basis site dc field (T), optional ac field (T) and its
+    frequency (THz): mu_s (B_dc + B_ac cos(2 pi f t))."""
+    dc = np.ascontiguousarray(np.asarray(dc, dtype=np.float64).reshape(-1, 3))
+    t = Term(kind=TERM_ZEEMAN, dc_field=dc, name="zeeman")
+    if ac is not None:
+        t.ac_field = np.ascontiguousarray(np.asarray(ac, dtype=np.float64).reshape(-1, 3))
+        t.ac_frequency = np.ascontiguousarray(np.asarray(frequency, dtype=np.float64).reshape(-1))
+    return t
 
 
 def dipole_term(cell, basis_frac, r_cutoff: float, lattice_parameter: float, tolerance: float = 1e-4) -> Term:

@@ -480,7 +480,17 @@ int orc_create(const orc_model *m, orc_sim **out) {
         orc_destroy(s);
         return -1;
       }
-    } else if (tm->kind != ORC_TERM_APPLIED_FIELD) {
+    } else if (tm->kind == ORC_TERM_ZEEMAN) {
+      if (!tm->dc_field || (tm->ac_field && !tm->ac_frequency)) {
+        orc_destroy(s);
+        return fail("zeeman: dc field per basis site, ac field with its frequency");
+      }
+    } else if (tm->kind == ORC_TERM_APPLIED_FIELD) {
+      if (tm->pulse < ORC_PULSE_STATIC || tm->pulse > ORC_PULSE_SINC_COS) {
+        orc_destroy(s);
+        return fail("unknown field pulse type %d", tm->pulse);
+      }
+    } else {
       orc_destroy(s);
       return fail("unknown term kind %d", tm->kind);
     }
@@ -517,9 +527,15 @@ double orc_sigma(const orc_sim *s, int32_t b) { return s->sigma[b]; }
 /* fields                                                                    */
 /* ------------------------------------------------------------------------ */
 
-/* one term's field at spin i into f[3] */
+/* sinc(x) = sin(x) / x, 1 at 0 (src/jams/helpers/maths.h:437-446) */
+static double sinc_ref(double x) {
+  if (x == 0.0) return 1.0;
+  return sin(x) / x;
+}
+
+/* one term's field at spin i and solver time `time` (ps) into f[3] */
 static void term_field(const orc_sim *s, int t, const double *spins, int64_t i,
-                       double f[3]) {
+                       double time, double f[3]) {
   const orc_term *tm = &s->terms[t];
   const int b = (int)(i % s->m.nb);
   const double *sp = spins + 3 * i;
@@ -591,8 +607,31 @@ static void term_field(const orc_sim *s, int t, const double *spins, int64_t i,
       for (int l = 0; l < 3; ++l) f[l] = s->mus[i] * acc[l];
       break;
     }
-    default: { /* ORC_TERM_APPLIED_FIELD: src/jams/hamiltonian/applied_field.cc:146-148 */
-      for (int j = 0; j < 3; ++j) f[j] = s->mus[i] * tm->B[j];
+    case ORC_TERM_ZEEMAN: {
+      /* dc_local_field = dc mu_s, ac_local_field = ac mu_s, frequency 2 pi f
+         (zeeman.cc:26-71); field = dc_local + ac_local cos(w t) (:106-121) */
+      for (int j = 0; j < 3; ++j) {
+        double fj = tm->dc_field[3 * b + j] * s->mus[i];
+        if (tm->ac_field) {
+          const double w = 2.0 * kPi * tm->ac_frequency[b];
+          fj += (tm->ac_field[3 * b + j] * s->mus[i]) * cos(w * time);
+        }
+        f[j] = fj;
+      }
+      break;
+    }
+    default: { /* ORC_TERM_APPLIED_FIELD: src/jams/hamiltonian/applied_field.cc:10-103,146-148 */
+      double B[3] = {tm->B[0], tm->B[1], tm->B[2]};
+      if (tm->pulse != ORC_PULSE_STATIC) {
+        /* SincField / SincCosField::field: B sinc(pi f_bw (t - t0)) [cos(2 pi f_c (t - t0))] */
+        const double sv = sinc_ref(kPi * tm->freq_bandwidth * (time - tm->time_center));
+        for (int j = 0; j < 3; ++j) B[j] = B[j] * sv;
+        if (tm->pulse == ORC_PULSE_SINC_COS) {
+          const double cv = cos(2.0 * kPi * tm->freq_center * (time - tm->time_center));
+          for (int j = 0; j < 3; ++j) B[j] = B[j] * cv;
+        }
+      }
+      for (int j = 0; j < 3; ++j) f[j] = s->mus[i] * B[j];
       break;
     }
   }
@@ -600,7 +639,7 @@ static void term_field(const orc_sim *s, int t, const double *spins, int64_t i,
 
 /* Solver::compute_fields: copy of term 0 then daxpy(1.0) of the others
    (src/jams/core/solver.cc:43-57) */
-static void compute_fields(const orc_sim *s, const double *spins, double *h) {
+static void compute_fields(const orc_sim *s, const double *spins, double time, double *h) {
   const int64_t n = s->n;
   if (s->nt == 0) {
     memset(h, 0, sizeof(double) * 3 * n);
@@ -609,10 +648,10 @@ static void compute_fields(const orc_sim *s, const double *spins, double *h) {
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) {
     double f[3];
-    term_field(s, 0, spins, i, f);
+    term_field(s, 0, spins, i, time, f);
     double acc[3] = {f[0], f[1], f[2]};
     for (int t = 1; t < s->nt; ++t) {
-      term_field(s, t, spins, i, f);
+      term_field(s, t, spins, i, time, f);
       for (int j = 0; j < 3; ++j) acc[j] += 1.0 * f[j];
     }
     for (int j = 0; j < 3; ++j) h[3 * i + j] = acc[j];
@@ -620,8 +659,7 @@ static void compute_fields(const orc_sim *s, const double *spins, double *h) {
 }
 
 int orc_fields(orc_sim *s, const double *spins, double t, double *h) {
-  (void)t; /* static terms only */
-  compute_fields(s, spins, h);
+  compute_fields(s, spins, t, h);
   return 0;
 }
 
@@ -677,14 +715,16 @@ static inline void unit_vector(double v[3]) {
   for (int j = 0; j < 3; ++j) v[j] = v[j] / length;
 }
 
-/* HeunLLGSolver::run: src/jams/solvers/cpu_llg_heun.cc:45-148 */
+/* HeunLLGSolver::run: src/jams/solvers/cpu_llg_heun.cc:45-148; fields at
+   t0 = iteration * dt, then at t0 + dt */
 static void heun_step(orc_sim *s, double *spins, uint64_t step) {
   const int64_t n = s->n, n3 = 3 * n;
   const double dt = s->m.dt;
+  const double t0 = (double)step * dt;
   const int thermal = s->m.temperature > 0.0;
   memcpy(s->s_old, spins, sizeof(double) * n3);
   if (thermal) draw_noise(s, step);
-  compute_fields(s, spins, s->h);
+  compute_fields(s, spins, t0, s->h);
   scale_field(s, s->h, thermal);
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) {
@@ -698,7 +738,7 @@ static void heun_step(orc_sim *s, double *spins, uint64_t step) {
     unit_vector(v);
     for (int j = 0; j < 3; ++j) spins[3 * i + j] = v[j];
   }
-  compute_fields(s, spins, s->h);
+  compute_fields(s, spins, t0 + dt, s->h);
   scale_field(s, s->h, thermal);
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) {
@@ -716,9 +756,9 @@ static void heun_step(orc_sim *s, double *spins, uint64_t step) {
 
 /* k = -gamma (S x H' + alpha S x (S x H')), H' = H / mu_s + noise
    (src/jams/solvers/cuda_llg_rk4_kernel.cuh:26-53) */
-static void rk4_derivative(orc_sim *s, const double *spins, double *k, int thermal) {
+static void rk4_derivative(orc_sim *s, const double *spins, double time, double *k, int thermal) {
   const int64_t n = s->n;
-  compute_fields(s, spins, s->h);
+  compute_fields(s, spins, time, s->h);
   scale_field(s, s->h, thermal);
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) llg_rhs(s->gyro[i], s->alpha[i], spins + 3 * i, s->h + 3 * i, k + 3 * i);
@@ -728,25 +768,27 @@ static void rk4_derivative(orc_sim *s, const double *spins, double *k, int therm
    host: stages s_old + c dt k (cublasDcopy + cublasDaxpy), combination
    s_old + dt (k1 + 2 k2 + 2 k3 + k4) / 6 (cuda_rk4_base_kernel.cuh:14-16),
    then normalise (cuda_spin_ops.cu:4-16, with s / |s| in place of the
-   device's approximate reciprocal square root). */
+   device's approximate reciprocal square root).  Stage times t0, t0 + dt/2,
+   t0 + dt/2, t0 + dt (cuda_rk4_base.cu:53-88). */
 static void rk4_step(orc_sim *s, double *spins, uint64_t step) {
   const int64_t n = s->n, n3 = 3 * n;
   const double dt = s->m.dt;
+  const double t0 = (double)step * dt;
   const int thermal = s->m.temperature > 0.0;
   memcpy(s->s_old, spins, sizeof(double) * n3);
   if (thermal) draw_noise(s, step);
-  rk4_derivative(s, spins, s->k1, thermal);
+  rk4_derivative(s, spins, t0, s->k1, thermal);
   double c = 0.5 * dt;
 #pragma omp parallel for schedule(static)
   for (int64_t q = 0; q < n3; ++q) s->tmp[q] = s->s_old[q] + c * s->k1[q];
-  rk4_derivative(s, s->tmp, s->k2, thermal);
+  rk4_derivative(s, s->tmp, t0 + 0.5 * dt, s->k2, thermal);
 #pragma omp parallel for schedule(static)
   for (int64_t q = 0; q < n3; ++q) s->tmp[q] = s->s_old[q] + c * s->k2[q];
-  rk4_derivative(s, s->tmp, s->k3, thermal);
+  rk4_derivative(s, s->tmp, t0 + 0.5 * dt, s->k3, thermal);
   c = dt;
 #pragma omp parallel for schedule(static)
   for (int64_t q = 0; q < n3; ++q) s->tmp[q] = s->s_old[q] + c * s->k3[q];
-  rk4_derivative(s, s->tmp, s->k4, thermal);
+  rk4_derivative(s, s->tmp, t0 + dt, s->k4, thermal);
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) {
     double v[3];
@@ -773,7 +815,6 @@ int orc_run(orc_sim *s, double *spins, int64_t first_step, int32_t nsteps) {
 /* ------------------------------------------------------------------------ */
 
 int orc_energies(orc_sim *s, const double *spins, double t, double *e_terms) {
-  (void)t;
   const int64_t n = s->n;
   for (int tt = 0; tt < s->nt; ++tt) {
     const orc_term *tm = &s->terms[tt];
@@ -785,7 +826,7 @@ int orc_energies(orc_sim *s, const double *spins, double t, double *e_terms) {
       switch (tm->kind) {
         case ORC_TERM_EXCHANGE:
           /* -1/2 sum s.h (sparse_interaction.cc:86-100) */
-          term_field(s, tt, spins, i, f);
+          term_field(s, tt, spins, i, t, f);
           e += -(sp[0] * f[0] + sp[1] * f[1] + sp[2] * f[2]);
           break;
         case ORC_TERM_UNIAXIAL: {
@@ -808,12 +849,12 @@ int orc_energies(orc_sim *s, const double *spins, double t, double *e_terms) {
         }
         case ORC_TERM_DIPOLE:
           /* -1/2 sum s.h (cuda_dipole_fft.cu:156-167) */
-          term_field(s, tt, spins, i, f);
+          term_field(s, tt, spins, i, t, f);
           e += -(sp[0] * f[0] + sp[1] * f[1] + sp[2] * f[2]);
           break;
         default:
-          /* applied_field.cc:150-155 */
-          term_field(s, tt, spins, i, f);
+          /* applied_field.cc:150-155, zeeman.cc:82-87 */
+          term_field(s, tt, spins, i, t, f);
           e += -(sp[0] * f[0] + sp[1] * f[1] + sp[2] * f[2]);
           break;
       }

@@ -16,7 +16,14 @@
  *       src/jams/interface/sparse_blas.h:13-27,57-81     (Xcsrmv_general)
  *   - uniaxial field/energy: src/jams/hamiltonian/uniaxial_anisotropy.cc:126-172
  *   - cubic field/energy:    src/jams/hamiltonian/cubic_anisotropy.cc:135-226
- *   - applied field:         src/jams/hamiltonian/applied_field.cc:84-148
+ *   - applied field:         src/jams/hamiltonian/applied_field.cc:10-148
+ *                            (static, sinc and sinc-cos pulses at the
+ *                            solver time; src/jams/helpers/maths.h:437-446)
+ *   - zeeman field:          src/jams/hamiltonian/zeeman.cc:12-71,106-121
+ *   - stage times:           src/jams/solvers/cpu_llg_heun.cc:45-148 (t0,
+ *                            t0 + dt), src/jams/solvers/cuda_rk4_base.cu:50-108
+ *                            (t0, t0 + dt/2, t0 + dt/2, t0 + dt), with
+ *                            t0 = iteration * dt
  *   - field summation:       src/jams/core/solver.cc:43-57 (copy + daxpy)
  *   - Heun step:             src/jams/solvers/cpu_llg_heun.cc:28-148
  *   - RK4 step (no CPU version exists in the reference; restated from the
@@ -57,8 +64,11 @@ enum {
   ORC_TERM_UNIAXIAL = 1,
   ORC_TERM_CUBIC = 2,
   ORC_TERM_APPLIED_FIELD = 3,
-  ORC_TERM_DIPOLE = 4
+  ORC_TERM_DIPOLE = 4,
+  ORC_TERM_ZEEMAN = 5
 };
+
+enum { ORC_PULSE_STATIC = 0, ORC_PULSE_SINC = 1, ORC_PULSE_SINC_COS = 2 };
 
 enum { ORC_HEUN = 0, ORC_RK4 = 1 };
 
@@ -86,6 +96,17 @@ typedef struct {
   double lattice_parameter;
   const double *lattice_vectors;
   const double *positions;
+  /* applied field: ORC_PULSE_*, centre time (ps), bandwidth and centre
+     frequency (THz) */
+  int32_t pulse;
+  double time_center;
+  double freq_bandwidth;
+  double freq_center;
+  /* zeeman: per basis site dc field and ac field (T, 3 nb; ac may be null),
+     ac frequency (THz, nb) */
+  const double *dc_field;
+  const double *ac_field;
+  const double *ac_frequency;
 } orc_term;
 
 typedef struct {

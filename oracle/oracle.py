@@ -37,6 +37,13 @@ class OrcTerm(ctypes.Structure):
         ("lattice_parameter", ctypes.c_double),
         ("lattice_vectors", ctypes.POINTER(ctypes.c_double)),
         ("positions", ctypes.POINTER(ctypes.c_double)),
+        ("pulse", ctypes.c_int32),
+        ("time_center", ctypes.c_double),
+        ("freq_bandwidth", ctypes.c_double),
+        ("freq_center", ctypes.c_double),
+        ("dc_field", ctypes.POINTER(ctypes.c_double)),
+        ("ac_field", ctypes.POINTER(ctypes.c_double)),
+        ("ac_frequency", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -153,6 +160,14 @@ class _Packed:
                 ot.r_cutoff, ot.distance_tolerance = float(t.r_cutoff), float(t.distance_tolerance)
                 ot.lattice_parameter = float(t.lattice_parameter)
                 ot.lattice_vectors, ot.positions = _dp(vec), _dp(pos)
+            ot.pulse, ot.time_center = int(t.pulse), float(t.time_center)
+            ot.freq_bandwidth, ot.freq_center = float(t.freq_bandwidth), float(t.freq_center)
+            for name in ("dc_field", "ac_field", "ac_frequency"):
+                v = getattr(t, name)
+                if v is not None:
+                    a = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+                    self.keep.append(a)
+                    setattr(ot, name, _dp(a))
         self.terms = terms
         mus = np.ascontiguousarray(m.mus, dtype=np.float64)
         gyro = np.ascontiguousarray(m.gyro, dtype=np.float64)
@@ -192,6 +207,7 @@ class OracleSim:
         self.n = int(self.L.orc_num_spins(h))
         self.n_terms = len(workload.model.terms)
         self.iteration = 0
+        self.dt = workload.model.dt
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -205,16 +221,20 @@ class OracleSim:
         self.iteration = fs + nsteps
         return s
 
-    def fields(self, spins: np.ndarray) -> np.ndarray:
+    def time(self) -> float:
+        """The solver time (ps) after the steps run so far: iteration * dt."""
+        return self.iteration * self.dt
+
+    def fields(self, spins: np.ndarray, t: Optional[float] = None) -> np.ndarray:
         s = np.ascontiguousarray(spins, dtype=np.float64)
         h = np.empty_like(s)
-        self.L.orc_fields(self.h, _dp(s), 0.0, _dp(h))
+        self.L.orc_fields(self.h, _dp(s), self.time() if t is None else float(t), _dp(h))
         return h
 
-    def energies(self, spins: np.ndarray) -> np.ndarray:
+    def energies(self, spins: np.ndarray, t: Optional[float] = None) -> np.ndarray:
         s = np.ascontiguousarray(spins, dtype=np.float64)
         e = np.empty(self.n_terms)
-        self.L.orc_energies(self.h, _dp(s), 0.0, _dp(e))
+        self.L.orc_energies(self.h, _dp(s), self.time() if t is None else float(t), _dp(e))
         return e
 
     def magnetisation(self, spins: np.ndarray) -> np.ndarray:

@@ -8,7 +8,7 @@
 // src/jams/core/solver.cc, src/jams/hamiltonian/sparse_interaction.cc,
 // src/jams/hamiltonian/uniaxial_anisotropy.cc,
 // src/jams/hamiltonian/cubic_anisotropy.cc,
-// src/jams/hamiltonian/applied_field.cc,
+// src/jams/hamiltonian/applied_field.cc, src/jams/hamiltonian/zeeman.cc,
 // src/jams/hamiltonian/dipole_bruteforce.cc, src/jams/lattice/minimum_image.cc,
 // src/jams/containers/cell.cc, src/jams/core/physics.cc,
 // src/jams/core/base.cc, src/jams/common.cc, and the header-only CSR builder
@@ -52,6 +52,7 @@
 #include <jams/hamiltonian/dipole_bruteforce.h>
 #include <jams/hamiltonian/sparse_interaction.h>
 #include <jams/hamiltonian/uniaxial_anisotropy.h>
+#include <jams/hamiltonian/zeeman.h>
 #include <jams/physics/empty.h>
 #include <jams/solvers/cpu_llg_heun.h>
 
@@ -343,7 +344,28 @@ __attribute__((visibility("default"))) int ref_create(const orc_model* m, double
       } else if (tm.kind == ORC_TERM_APPLIED_FIELD) {
         hs.add("module", Setting::string("applied-field"));
         hs.add("field", vec3(tm.B));
+        if (tm.pulse != ORC_PULSE_STATIC) {
+          // the config's units: seconds and hertz (applied_field.cc:36-38,64-67)
+          hs.add("type", Setting::string(tm.pulse == ORC_PULSE_SINC ? "sinc" : "sinc-cos"));
+          hs.add("time_center", Setting::number(tm.time_center * 1e-12));
+          hs.add("freq_bandwidth", Setting::number(tm.freq_bandwidth * 1e12));
+          if (tm.pulse == ORC_PULSE_SINC_COS) hs.add("freq_center", Setting::number(tm.freq_center * 1e12));
+        }
         g_solver->register_hamiltonian(new AppliedFieldHamiltonian(hs, n));
+      } else if (tm.kind == ORC_TERM_ZEEMAN) {
+        // per material (one per basis site): dc field, ac field and frequency
+        hs.add("module", Setting::string("zeeman"));
+        Setting& dc = hs.add("dc_local_field", list());
+        for (int b = 0; b < m->nb; ++b) dc.add(vec3(tm.dc_field + 3 * b));
+        if (tm.ac_field) {
+          Setting& ac = hs.add("ac_local_field", list());
+          Setting& fr = hs.add("ac_local_frequency", list());
+          for (int b = 0; b < m->nb; ++b) {
+            ac.add(vec3(tm.ac_field + 3 * b));
+            fr.add(Setting::number(tm.ac_frequency[b]));
+          }
+        }
+        g_solver->register_hamiltonian(new ZeemanHamiltonian(hs, n));
       } else if (tm.kind == ORC_TERM_DIPOLE) {
         hs.add("module", Setting::string("dipole-bruteforce"));
         hs.add("r_cutoff", Setting::number(tm.r_cutoff));
@@ -387,7 +409,8 @@ __attribute__((visibility("default"))) int ref_energies(const double* spins, dou
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < 3; ++j) globals::s(i, j) = spins[3 * i + j];
   int t = 0;
-  for (auto& hh : g_solver->hamiltonians()) e[t++] = hh->calculate_total_energy(0.0);
+  // at the solver time, as the energy monitor (src/jams/monitors/energy.cc:28)
+  for (auto& hh : g_solver->hamiltonians()) e[t++] = hh->calculate_total_energy(g_solver->time());
   return 0;
 }
 

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from jams_gb300 import workloads as W
-from tests.golden.cases import cases, dipole_cases
+from tests.golden.cases import cases, dipole_cases, pulse_cases
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -28,6 +28,51 @@ def test_oracle_matches_reference_golden_vectors(oracle, name):
         s = sim.run(s, k - done, first_step=done)
         done = k
         assert np.array_equal(s, g["s%d" % k]), "max |dS| = %g after %d steps" % (np.abs(s - g["s%d" % k]).max(), k)
+
+
+@pytest.mark.parametrize("name", sorted(pulse_cases().keys()))
+def test_oracle_matches_reference_pulse_golden_vectors(oracle, name):
+    """Time-dependent applied fields (sinc, sinc-cos pulses) and zeeman dc / ac
+    fields at the stage times t0 and t0 + dt of every Heun step: fields,
+    energies and trajectories equal the reference's own applied_field.cc and
+    zeeman.cc, and so do the fields and energies at the solver time 100 dt."""
+    w = pulse_cases()[name]
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    sim = oracle.OracleSim(w)
+    s0 = g["s0"]
+    assert np.array_equal(sim.fields(s0), g["fields"])
+    np.testing.assert_allclose(sim.energies(s0), g["energies"], rtol=1e-13, atol=1e-12)
+    s = s0
+    done = 0
+    for k in (1, 10, 100):
+        s = sim.run(s, k - done, first_step=done)
+        done = k
+        assert np.array_equal(s, g["s%d" % k]), "max |dS| = %g after %d steps" % (np.abs(s - g["s%d" % k]).max(), k)
+    assert np.array_equal(sim.fields(s), g["fields100"])
+    np.testing.assert_allclose(sim.energies(s), g["energies100"], rtol=1e-13, atol=1e-12)
+    assert not np.array_equal(g["fields100"], g["fields"])
+
+
+def test_oracle_pulse_shapes(oracle):
+    """The applied field of one spin follows B sinc(pi f_bw (t - t_c)) and
+    B sinc(...) cos(2 pi f_c (t - t_c)); the zeeman field dc + ac cos(2 pi f t)."""
+    B = np.array([0.3, -0.2, 1.5])
+    tc, fbw, fc, fz = 0.02, 60.0, 90.0, 25.0
+    for pulse in (W.PULSE_SINC, W.PULSE_SINC_COS):
+        w = W.sc_ferromagnet(L=1, J=0.0, dz=0.0)
+        w.model.terms = [W.field_term(B, pulse=pulse, time_center=tc, freq_bandwidth=fbw, freq_center=fc),
+                         W.zeeman_term([(0.1, 0.0, 0.2)], [(0.0, 0.4, 0.0)], [fz])]
+        sim = oracle.OracleSim(w)
+        s = np.array([[0.0, 0.0, 1.0]])
+        mus = w.model.mus[0]
+        for t in (0.0, 0.013, 0.02, 0.05):
+            x = math.pi * fbw * (t - tc)
+            f = 1.0 if x == 0.0 else math.sin(x) / x
+            if pulse == W.PULSE_SINC_COS:
+                f *= math.cos(2 * math.pi * fc * (t - tc))
+            want = mus * B * f + mus * (np.array([0.1, 0.0, 0.2]) + np.array([0.0, 0.4, 0.0]) *
+                                        math.cos(2 * math.pi * fz * t))
+            np.testing.assert_allclose(sim.fields(s, t)[0], want, rtol=1e-12, atol=1e-15)
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle", "_ref",
