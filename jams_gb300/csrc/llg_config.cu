@@ -10,9 +10,10 @@
 //   hamiltonians     exchange (src/jams/hamiltonian/exchange.cc:15-171 and
 //                    src/jams/core/interactions.cc:128-348), uniaxial
 //                    (uniaxial_anisotropy.cc:48-118), cubic
-//                    (cubic_anisotropy.cc:40-125), applied-field
-//                    (applied_field.cc:84-124), zeeman dc_local_field
-//                    (zeeman.cc:12-38)
+//                    (cubic_anisotropy.cc:40-125), applied-field with
+//                    its static / sinc / sinc-cos types
+//                    (applied_field.cc:10-124), zeeman dc and ac fields
+//                    (zeeman.cc:12-71)
 //   solver           t_step / t_max in seconds, module, gilbert_prefactor
 //                    (src/jams/solvers/cuda_llg_heun.cu:21-35)
 //   physics          temperature (src/jams/core/physics.cc:79-100)
@@ -408,6 +409,7 @@ struct Model {
     std::vector<int32_t> bi, bj, T;
     std::vector<double> J, K, axis;
     std::vector<double> vectors, positions;   // dipole geometry
+    std::vector<double> dc, ac, freq;         // zeeman fields per basis site
   };
   std::vector<Term> terms;
   // solver / physics / sim
@@ -835,21 +837,51 @@ Model build_model(const Node& root) {
     } else if (t.module == "cubic" || t.module == "cubic-anisotropy") {
       build_cubic(m, h, t);
     } else if (t.module == "applied-field") {
-      if (h.find("type") && lower(h.at("type").str()) != "static")
-        throw CfgError("applied-field: only the static field type is on this path");
+      // static, sinc or sinc-cos field (applied_field.cc:82-110); time_center
+      // in seconds, freq_bandwidth and freq_center in hertz, converted to ps
+      // and THz as the reference does (:36-38, 64-67)
       const V3 B = vec3(h.at("field"));
       t.t.kind = LLG_TERM_APPLIED_FIELD;
       for (int c = 0; c < 3; ++c) t.t.B[c] = B[c];
+      t.t.pulse = LLG_PULSE_STATIC;
+      if (h.find("type")) {
+        const std::string type = lower(h.at("type").str());
+        if (type == "sinc") t.t.pulse = LLG_PULSE_SINC;
+        else if (type == "sinc-cos") t.t.pulse = LLG_PULSE_SINC_COS;
+        else if (type != "static") throw CfgError("applied-field: unknown field pulse type " + type);
+      }
+      if (t.t.pulse != LLG_PULSE_STATIC) {
+        t.t.time_center = h.at("time_center").num() / 1e-12;
+        t.t.freq_bandwidth = h.at("freq_bandwidth").num() / 1e12;
+        if (t.t.pulse == LLG_PULSE_SINC_COS) t.t.freq_center = h.at("freq_center").num() / 1e12;
+      }
     } else if (t.module == "zeeman") {
-      if (h.find("ac_local_field") || h.find("ac_local_frequency"))
-        throw CfgError("zeeman: ac fields are not on this path");
-      t.t.kind = LLG_TERM_APPLIED_FIELD;
-      if (const Node* dc = h.find("dc_local_field")) {
-        // one field per material; this path needs the same field for all
-        const V3 B = vec3(dc->at(0));
-        for (size_t q = 1; q < dc->size(); ++q)
-          if (!approx_eq(vec3(dc->at(q)), B, 0.0)) throw CfgError("zeeman: per-material fields differ");
-        for (int c = 0; c < 3; ++c) t.t.B[c] = B[c];
+      // dc field, ac field and ac frequency per material (zeeman.cc:12-71)
+      t.t.kind = LLG_TERM_ZEEMAN;
+      const size_t nm = m.mat_names.size(), nb = m.basis.size();
+      const Node* dc = h.find("dc_local_field");
+      const Node* ac = h.find("ac_local_field");
+      const Node* fr = h.find("ac_local_frequency");
+      if (dc && dc->size() != nm) throw CfgError("zeeman: dc_local_field must be specified for every material");
+      if ((ac != nullptr) != (fr != nullptr)) throw CfgError("zeeman: ac_local_field must have a field and a frequency");
+      if (ac && (ac->size() != nm || fr->size() != nm))
+        throw CfgError("zeeman: ac_local_field and ac_local_frequency must be specified for every material");
+      t.dc.assign(3 * nb, 0.0);
+      if (ac) {
+        t.ac.assign(3 * nb, 0.0);
+        t.freq.assign(nb, 0.0);
+      }
+      for (size_t b = 0; b < nb; ++b) {
+        const size_t mi = (size_t)m.basis[b].mat;
+        if (dc) {
+          const V3 v = vec3(dc->at(mi));
+          for (int c = 0; c < 3; ++c) t.dc[3 * b + c] = v[c];
+        }
+        if (ac) {
+          const V3 v = vec3(ac->at(mi));
+          for (int c = 0; c < 3; ++c) t.ac[3 * b + c] = v[c];
+          t.freq[b] = fr->at(mi).num();
+        }
       }
     } else if (t.module == "dipole-fft" || t.module == "dipole-bruteforce" || t.module == "dipole-tensor" ||
                t.module == "dipole-neighbour-list" || t.module == "dipole-neartree") {
@@ -886,6 +918,9 @@ void fill_desc(Model& m, llg_desc& d, llg_replica& rep, std::vector<llg_term>& t
     lt.axis = t.axis.empty() ? nullptr : t.axis.data();
     lt.lattice_vectors = t.vectors.empty() ? nullptr : t.vectors.data();
     lt.positions = t.positions.empty() ? nullptr : t.positions.data();
+    lt.dc_field = t.dc.empty() ? nullptr : t.dc.data();
+    lt.ac_field = t.ac.empty() ? nullptr : t.ac.data();
+    lt.ac_frequency = t.freq.empty() ? nullptr : t.freq.data();
     terms.push_back(lt);
   }
   d = llg_desc{};
@@ -1031,6 +1066,13 @@ int llg_config_describe(const char* config_text, const char* patch_text, char* j
       arr("K", t.K);
       arr("axis", t.axis);
       arr("B", std::vector<double>{t.t.B[0], t.t.B[1], t.t.B[2]});
+      if (t.t.kind == LLG_TERM_APPLIED_FIELD)
+        arr("pulse", std::vector<double>{(double)t.t.pulse, t.t.time_center, t.t.freq_bandwidth, t.t.freq_center});
+      if (t.t.kind == LLG_TERM_ZEEMAN) {
+        arr("dc_field", t.dc);
+        arr("ac_field", t.ac);
+        arr("ac_frequency", t.freq);
+      }
       if (t.t.kind == LLG_TERM_DIPOLE) {
         arr("dipole", std::vector<double>{t.t.r_cutoff, t.t.distance_tolerance, t.t.lattice_parameter});
         arr("lattice_vectors", t.vectors);

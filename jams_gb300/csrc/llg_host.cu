@@ -50,7 +50,8 @@ void set_thread_error(const char* msg) { g_tls_error = msg; }
 
 namespace {
 
-// src/jams/helpers/consts.h:32
+// src/jams/helpers/consts.h:16,32
+constexpr double kPi = 3.14159265358979323846;
 constexpr double kBoltzmannIU = 0.0861733326;
 
 struct ExchangeHost {
@@ -82,6 +83,15 @@ struct DevBuf {
     if (count == 0) return cudaSuccess;
     return cudaMalloc((void**)&p, count * sizeof(T));
   }
+};
+
+// a pinned host buffer (staging of host -> device copies)
+struct PinnedBuf {
+  unsigned char* p = nullptr;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t alloc(size_t bytes) { return cudaHostAlloc((void**)&p, bytes, cudaHostAllocDefault); }
 };
 
 // a pinned host word the status flag is copied into
@@ -161,9 +171,28 @@ struct llg_handle {
   DipoleGeometry dip_geom{};
   DipoleField* dipole = nullptr;
   DevBuf<unsigned char> d_hdip[2];
+  // time-dependent fields (applied-field pulse, zeeman ac field): their
+  // parameters, a device table of the time factors of every stage of up to
+  // pulse_cap steps ([iteration of entry 0][pad][doubles][floats]), filled
+  // per llg_step chunk through two pinned staging buffers, and the factors
+  // at the current solver time for fields and energies
+  bool pulsed = false;
+  int pulse_type = LLG_PULSE_STATIC;
+  double pulse_tc = 0.0, pulse_fbw = 0.0, pulse_fc = 0.0;
+  bool zeeman_ac = false;
+  double zeeman_w[kMaxBasis] = {};
+  int pulse_cap = 0;
+  DevBuf<unsigned char> d_pulse;
+  PinnedBuf pulse_host[2];
+  cudaEvent_t pulse_ev[2] = {nullptr, nullptr};
+  int pulse_slot = 0;
+  DevBuf<unsigned char> d_pulse_now;
+  PinnedBuf pulse_now_host;
   std::string async_err;     // a failure inside an enqueue (reported by llg_step)
 
   ~llg_handle() {
+    for (auto& e : pulse_ev)
+      if (e) cudaEventDestroy(e);
     if (dipole) dipole_destroy(dipole);
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
     if (own_stream) cudaStreamDestroy(own_stream);
@@ -436,7 +465,7 @@ int build(llg_handle* h, const llg_desc* d) {
   // terms
   std::vector<ExchangeHost> ex;
   h->term_B.assign((size_t)d->n_terms * 3, 0.0);
-  int field_terms = 0;
+  int field_terms = 0, zeeman_terms = 0;
   for (int t = 0; t < d->n_terms; ++t) {
     const llg_term& T = d->terms[t];
     TermDev& TD = P.term[t];
@@ -485,8 +514,44 @@ int build(llg_handle* h, const llg_desc* d) {
       }
       case LLG_TERM_APPLIED_FIELD:
         for (int a = 0; a < 3; ++a) h->term_B[3 * t + a] = T.B[a];
+        if (T.pulse < LLG_PULSE_STATIC || T.pulse > LLG_PULSE_SINC_COS)
+          return h->fail(LLG_ERR_BAD_DESC, "applied-field term %d: unknown pulse type %d", t, T.pulse);
+        if (!std::isfinite(T.time_center) || !std::isfinite(T.freq_bandwidth) || !std::isfinite(T.freq_center))
+          return h->fail(LLG_ERR_BAD_DESC, "applied-field term %d: non-finite pulse parameters", t);
+        h->pulse_type = T.pulse;
+        h->pulse_tc = T.time_center;
+        h->pulse_fbw = T.freq_bandwidth;
+        h->pulse_fc = T.freq_center;
+        if (T.pulse != LLG_PULSE_STATIC) h->pulsed = true;
         ++field_terms;
         break;
+      case LLG_TERM_ZEEMAN: {
+        // mu_s B_dc and mu_s B_ac per basis site, as dc_local_field and
+        // ac_local_field (src/jams/hamiltonian/zeeman.cc:26-71)
+        if (!T.dc_field || (T.ac_field && !T.ac_frequency))
+          return h->fail(LLG_ERR_BAD_DESC, "zeeman term %d: dc field per basis site, ac field with its frequency", t);
+        TD.order = T.ac_field ? 1 : 0;
+        for (int b = 0; b < d->nb; ++b) {
+          for (int a = 0; a < 3; ++a) {
+            const double dc = T.dc_field[3 * b + a] * d->mus[b];
+            const double ac = T.ac_field ? T.ac_field[3 * b + a] * d->mus[b] : 0.0;
+            if (!std::isfinite(dc) || !std::isfinite(ac))
+              return h->fail(LLG_ERR_BAD_DESC, "zeeman term %d: non-finite field", t);
+            TD.axis[b][a] = dc;
+            TD.axis[b][3 + a] = ac;
+            TD.axisf[b][a] = (float)dc;
+            TD.axisf[b][3 + a] = (float)ac;
+          }
+          if (T.ac_field) {
+            if (!std::isfinite(T.ac_frequency[b]))
+              return h->fail(LLG_ERR_BAD_DESC, "zeeman term %d: non-finite frequency", t);
+            h->zeeman_w[b] = 2.0 * kPi * T.ac_frequency[b];
+          }
+        }
+        if (T.ac_field) h->zeeman_ac = h->pulsed = true;
+        ++zeeman_terms;
+        break;
+      }
       case LLG_TERM_DIPOLE: {
         if (h->has_dipole) return h->fail(LLG_ERR_UNSUPPORTED, "more than one dipole term");
         if (!T.lattice_vectors || !T.positions)
@@ -509,6 +574,7 @@ int build(llg_handle* h, const llg_desc* d) {
     }
   }
   if (field_terms > 1) return h->fail(LLG_ERR_UNSUPPORTED, "at most one applied-field term");
+  if (zeeman_terms > 1) return h->fail(LLG_ERR_UNSUPPORTED, "at most one zeeman term");
   P.nexch = (int)ex.size();
 
   // stencil reach over all exchange terms
@@ -759,6 +825,29 @@ int build(llg_handle* h, const llg_desc* d) {
   P.status = h->d_status.p;
   P.step_base = h->d_step_base.p;
   P.ticket = h->d_ticket.p;
+  if (h->pulsed) {
+    // factor table of pulse_cap steps (a multiple of the even graph block)
+    const int ns = h->integrator == LLG_HEUN ? 2 : 4;
+    const int K = h->steps_per_graph + (h->steps_per_graph & 1);
+    h->pulse_cap = K * std::max(1, 4096 / K);
+    const size_t nv = (size_t)h->pulse_cap * ns * kPulseVals;
+    const size_t bytes = 16 + nv * (sizeof(double) + sizeof(float));
+    if ((ce = h->d_pulse.alloc(bytes)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+    for (int k = 0; k < 2; ++k) {
+      if ((ce = h->pulse_host[k].alloc(bytes)) != cudaSuccess) return h->cuda_fail(ce, "pinned alloc");
+      if ((ce = cudaEventCreateWithFlags(&h->pulse_ev[k], cudaEventDisableTiming)) != cudaSuccess)
+        return h->cuda_fail(ce, "cudaEventCreate");
+    }
+    P.pulse_base = reinterpret_cast<const uint64_t*>(h->d_pulse.p);
+    P.pulse64 = reinterpret_cast<const double*>(h->d_pulse.p + 16);
+    P.pulse32 = reinterpret_cast<const float*>(h->d_pulse.p + 16 + nv * sizeof(double));
+    P.pulse_stages = ns;
+    const size_t now_bytes = kPulseVals * (sizeof(double) + sizeof(float));
+    if ((ce = h->d_pulse_now.alloc(now_bytes)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
+    if ((ce = h->pulse_now_host.alloc(now_bytes)) != cudaSuccess) return h->cuda_fail(ce, "pinned alloc");
+    P.pulse_now64 = reinterpret_cast<const double*>(h->d_pulse_now.p);
+    P.pulse_now32 = reinterpret_cast<const float*>(h->d_pulse_now.p + kPulseVals * sizeof(double));
+  }
   size_t maxn = 0;
   for (auto& R : h->reps) maxn = std::max<size_t>(maxn, (size_t)R.n);
   if ((ce = h->d_scratch.alloc(3 * maxn)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
@@ -835,6 +924,87 @@ Real* buf(llg_handle* h, int k) {
 }
 
 int num_stages(const llg_handle* h) { return h->integrator == LLG_HEUN ? 2 : 4; }
+
+// time factors at solver time t (ps), the reference's double expressions:
+// f[0] = sinc(pi f_bw (t - t_c)), f[1] = cos(2 pi f_c (t - t_c)) of the
+// applied-field pulse (src/jams/hamiltonian/applied_field.cc:17-78,
+// src/jams/helpers/maths.h:437-446; 1 where the pulse has no such factor),
+// f[2 + b] = cos(w_b t) of the zeeman ac field (zeeman.cc:115-117)
+void pulse_factors(const llg_handle* h, double t, double* f) {
+  f[0] = 1.0;
+  f[1] = 1.0;
+  if (h->pulse_type != LLG_PULSE_STATIC) {
+    const double x = kPi * h->pulse_fbw * (t - h->pulse_tc);
+    f[0] = x == 0.0 ? 1.0 : std::sin(x) / x;
+    if (h->pulse_type == LLG_PULSE_SINC_COS) f[1] = std::cos(2.0 * kPi * h->pulse_fc * (t - h->pulse_tc));
+  }
+  for (int b = 0; b < kMaxBasis; ++b) f[2 + b] = (h->zeeman_ac && b < h->nb) ? std::cos(h->zeeman_w[b] * t) : 1.0;
+}
+
+// the solver time of each stage of iteration n: Heun t0, t0 + dt
+// (src/jams/solvers/cuda_llg_heun.cu:64-122); RK4 t0, t0 + dt/2, t0 + dt/2,
+// t0 + dt (cuda_rk4_base.cu:50-108); t0 = n dt
+void stage_times(const llg_handle* h, int64_t n, double* ts) {
+  const double dt = h->dt, t0 = (double)n * dt;
+  if (h->integrator == LLG_HEUN) {
+    ts[0] = t0;
+    ts[1] = t0 + dt;
+  } else {
+    ts[0] = t0;
+    ts[1] = t0 + 0.5 * dt;
+    ts[2] = t0 + 0.5 * dt;
+    ts[3] = t0 + dt;
+  }
+}
+
+// the factor table for iterations it0 .. it0 + nsteps - 1 (nsteps <=
+// pulse_cap), enqueued on the stream before the launches that read it
+int upload_pulse_table(llg_handle* h, int64_t it0, int nsteps) {
+  const int ns = num_stages(h);
+  const size_t nv = (size_t)h->pulse_cap * ns * kPulseVals;
+  const size_t used = (size_t)nsteps * ns * kPulseVals;
+  const int slot = h->pulse_slot;
+  h->pulse_slot ^= 1;
+  // the copy that last read this staging buffer has finished
+  cudaError_t ce = cudaEventSynchronize(h->pulse_ev[slot]);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "pulse table");
+  unsigned char* host = h->pulse_host[slot].p;
+  const uint64_t base = (uint64_t)it0;
+  std::memcpy(host, &base, sizeof base);
+  double* f64 = reinterpret_cast<double*>(host + 16);
+  float* f32 = reinterpret_cast<float*>(host + 16 + nv * sizeof(double));
+  double ts[4];
+  for (int k = 0; k < nsteps; ++k) {
+    stage_times(h, it0 + k, ts);
+    for (int st = 0; st < ns; ++st) {
+      double* f = f64 + ((size_t)k * ns + st) * kPulseVals;
+      pulse_factors(h, ts[st], f);
+      for (int v = 0; v < kPulseVals; ++v) f32[((size_t)k * ns + st) * kPulseVals + v] = (float)f[v];
+    }
+  }
+  unsigned char* dev = h->d_pulse.p;
+  ce = cudaMemcpyAsync(dev, host, 16 + used * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(dev + 16 + nv * sizeof(double), host + 16 + nv * sizeof(double), used * sizeof(float),
+                         cudaMemcpyHostToDevice, h->stream);
+  if (ce == cudaSuccess) ce = cudaEventRecord(h->pulse_ev[slot], h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "uploading the pulse table");
+  return 0;
+}
+
+// the factors at the current solver time (iteration dt), for fields and
+// energies; the caller synchronises the stream before it returns
+int upload_pulse_now(llg_handle* h) {
+  if (!h->pulsed) return 0;
+  double* f = reinterpret_cast<double*>(h->pulse_now_host.p);
+  float* f32 = reinterpret_cast<float*>(h->pulse_now_host.p + kPulseVals * sizeof(double));
+  pulse_factors(h, (double)h->iteration * h->dt, f);
+  for (int v = 0; v < kPulseVals; ++v) f32[v] = (float)f[v];
+  cudaError_t ce = cudaMemcpyAsync(h->d_pulse_now.p, h->pulse_now_host.p,
+                                   kPulseVals * (sizeof(double) + sizeof(float)), cudaMemcpyHostToDevice, h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "uploading the pulse factors");
+  return 0;
+}
 
 // launches stage `stage` of step `ks` of a block; `cur` is the buffer that
 // holds the state at the start of the step (FP32 Heun alternates 0 and 2).
@@ -1071,12 +1241,8 @@ int llg_get_state_device(llg_handle* h, int32_t replica, double* s_dev) {
   return transfer_state(h, replica, nullptr, s_dev, true);
 }
 
-int llg_step(llg_handle* h, int32_t nsteps) {
-  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
-  if (nsteps < 0) return h->fail(LLG_ERR_BAD_DESC, "nsteps must be >= 0");
-  cudaSetDevice(h->device);
-  int rc = sync_replicas(h);
-  if (rc) return rc;
+// nsteps steps as CUDA-graph blocks (the pulse table, if any, covers them)
+static int step_blocks(llg_handle* h, int32_t nsteps) {
   h->last_launches = 0;
   const bool alternates = next_buffer(h, 0) != 0;
   int K = h->steps_per_graph;
@@ -1121,6 +1287,30 @@ int llg_step(llg_handle* h, int32_t nsteps) {
   }
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) return h->cuda_fail(ce, "launching LLG steps");
+  return 0;
+}
+
+int llg_step(llg_handle* h, int32_t nsteps) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (nsteps < 0) return h->fail(LLG_ERR_BAD_DESC, "nsteps must be >= 0");
+  cudaSetDevice(h->device);
+  int rc = sync_replicas(h);
+  if (rc) return rc;
+  if (!h->pulsed) return step_blocks(h, nsteps);
+  // time-dependent fields: chunks of at most pulse_cap steps, each after
+  // the upload of its factor table
+  int64_t launches = 0;
+  h->last_launches = 0;
+  for (int done = 0; done < nsteps;) {
+    const int c = std::min(nsteps - done, h->pulse_cap);
+    rc = upload_pulse_table(h, h->iteration, c);
+    if (rc) return rc;
+    rc = step_blocks(h, c);
+    launches += h->last_launches;
+    if (rc) return rc;
+    done += c;
+  }
+  h->last_launches = launches;
   return 0;
 }
 
@@ -1186,6 +1376,8 @@ int llg_fields(llg_handle* h, int32_t replica, double* h_host) {
   const ReplicaDev& R = h->reps[replica];
   const dim3 grid((unsigned)h->P.ntiles);
   const int sb = state_buffer(h);
+  rc = upload_pulse_now(h);   // fields at the solver time
+  if (rc) return rc;
   const Params P = launch_params(h, h->state[sb].p, 0);
   if (!h->async_err.empty()) {
     const std::string e = h->async_err;
@@ -1214,6 +1406,8 @@ int llg_observables(llg_handle* h, int32_t replica, double* m4, double* e_terms)
   if (rc) return rc;
   const int nq = 4 + h->nterms;
   const int sb = state_buffer(h);
+  rc = upload_pulse_now(h);   // energies at the solver time
+  if (rc) return rc;
   const Params P = launch_params(h, h->state[sb].p, 0);
   if (!h->async_err.empty()) {
     const std::string e = h->async_err;
@@ -1380,6 +1574,11 @@ int llg_profile_stages(llg_handle* h, int32_t nsteps, double* ms) {
   cudaSetDevice(h->device);
   int rc = sync_replicas(h);
   if (rc) return rc;
+  if (h->pulsed) {
+    if (nsteps > h->pulse_cap) return h->fail(LLG_ERR_BAD_DESC, "profile at most %d steps", h->pulse_cap);
+    rc = upload_pulse_table(h, h->iteration, nsteps);
+    if (rc) return rc;
+  }
   const int ns = num_stages(h);
   // per stage: start, after the dipole field evaluation, end
   std::vector<cudaEvent_t> ev((size_t)nsteps * ns * 3);

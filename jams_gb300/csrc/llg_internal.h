@@ -25,7 +25,12 @@ constexpr int kMaxSlots = 96;      // neighbour slots per basis site and term
 constexpr int kBlock = 256;        // threads per CTA, one spin per thread
 constexpr int32_t kMissing = INT32_MIN;  // neighbour outside an open boundary
 
-enum TermKind { kExchange = 0, kUniaxial = 1, kCubic = 2, kAppliedField = 3, kDipole = 4 };
+enum TermKind { kExchange = 0, kUniaxial = 1, kCubic = 2, kAppliedField = 3, kDipole = 4, kZeeman = 5 };
+
+// time factors of the time-dependent fields at one stage time t: the
+// applied-field pulse's sinc and cos factors (1 when absent) and, per basis
+// site, the zeeman term's cos(w_b t)
+constexpr int kPulseVals = 2 + kMaxBasis;
 
 // per exchange term, FP32 form: isotropic parts grouped into shells
 // (sum of neighbour spins times one J), anisotropic remainders per slot
@@ -48,10 +53,10 @@ struct ExchangeF64 {
 
 struct TermDev {
   int kind;
-  int order;
+  int order;              // uniaxial power, cubic order; zeeman: 1 with an ac field
   int exch;               // index into the exchange tables
   double K[kMaxBasis];
-  double axis[kMaxBasis][9];
+  double axis[kMaxBasis][9];  // zeeman: mu_s B_dc (0..2) and mu_s B_ac (3..5)
   float Kf[kMaxBasis];
   float axisf[kMaxBasis][9];
 };
@@ -128,7 +133,25 @@ struct Params {
   const float* hdip32_s0;
   const double* hdip64;
   const double* hdip64_s0;
+  // time-dependent fields (null without): kPulseVals factors per stage of
+  // every step from iteration *pulse_base on, [step][stage][kPulseVals], and
+  // the factors at the current solver time for fields and energies
+  const double* pulse64;
+  const float* pulse32;
+  const uint64_t* pulse_base;
+  int pulse_stages;
+  const double* pulse_now64;
+  const float* pulse_now32;
 };
+
+// the time factors of stage `stage` of iteration `step`, or null (no
+// time-dependent field: pulse factors 1)
+__device__ __forceinline__ const double* pulse_at64(const Params& P, uint64_t step, int stage) {
+  return P.pulse64 ? P.pulse64 + ((int64_t)(step - *P.pulse_base) * P.pulse_stages + stage) * kPulseVals : nullptr;
+}
+__device__ __forceinline__ const float* pulse_at32(const Params& P, uint64_t step, int stage) {
+  return P.pulse32 ? P.pulse32 + ((int64_t)(step - *P.pulse_base) * P.pulse_stages + stage) * kPulseVals : nullptr;
+}
 
 // the dipole planes of the input state in the precision Real
 template <class Real>

@@ -150,10 +150,11 @@ __device__ __forceinline__ void exchange_f32(const Params& P, int t, const Repli
   }
 }
 
-// total field (meV) of all terms at spin s, compensated, FP32
+// total field (meV) of all terms at spin s, compensated, FP32; pf: the time
+// factors of the stage (null: no time-dependent field)
 __device__ __forceinline__ void field_f32(const Params& P, const ReplicaDev& R, Site st, int64_t gi,
                                           const Planes<const float>& S, const float s[3], float h[3],
-                                          const float* hd) {
+                                          const float* hd, const float* pf) {
   float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
   const int b = st.b;
   for (int t = 0; t < P.nterms; ++t) {
@@ -201,9 +202,15 @@ __device__ __forceinline__ void field_f32(const Params& P, const ReplicaDev& R, 
           for (int m = 0; m < 3; ++m) acc_add(hi[m], lo[m], hd[m * P.npad + gi]);
         }
         break;
-      default: {  // applied field: mu_s B
+      case kZeeman: {  // mu_s B_dc + mu_s B_ac cos(w t)
 #pragma unroll
-        for (int m = 0; m < 3; ++m) acc_add(hi[m], lo[m], P.mus32[b] * R.Bf[m]);
+        for (int m = 0; m < 3; ++m)
+          acc_add(hi[m], lo[m], T.order ? T.axisf[b][m] + T.axisf[b][3 + m] * pf[2 + b] : T.axisf[b][m]);
+        break;
+      }
+      default: {  // applied field: mu_s B, times the pulse factors
+#pragma unroll
+        for (int m = 0; m < 3; ++m) acc_add(hi[m], lo[m], P.mus32[b] * (pf ? R.Bf[m] * pf[0] * pf[1] : R.Bf[m]));
         break;
       }
     }
@@ -285,10 +292,12 @@ __device__ __forceinline__ void exchange_f64(const Params& P, int t, const Repli
   f[2] = s2;
 }
 
-// one term's field, FP64, reference association order
+// one term's field, FP64, reference association order; pf: the time factors
+// of the stage (null: no time-dependent field)
 __device__ __forceinline__ void term_field_f64(const Params& P, const TermDev& T, const ReplicaDev& R,
                                                Site st, int64_t gi, const Planes<const double>& S,
-                                               const double s[3], double f[3], const double* hd) {
+                                               const double s[3], double f[3], const double* hd,
+                                               const double* pf) {
   const int b = st.b;
   switch (T.kind) {
     case kExchange:
@@ -335,10 +344,17 @@ __device__ __forceinline__ void term_field_f64(const Params& P, const TermDev& T
 #pragma unroll
       for (int m = 0; m < 3; ++m) f[m] = hd ? hd[m * P.npad + gi] : 0.0;
       break;
-    default: {
-      // src/jams/hamiltonian/applied_field.cc:146-148
+    case kZeeman:
+      // dc_local_field + ac_local_field cos(w t), both already times mu_s
+      // (src/jams/hamiltonian/zeeman.cc:26-71,106-121)
 #pragma unroll
-      for (int m = 0; m < 3; ++m) f[m] = dm(P.mus[b], R.B[m]);
+      for (int m = 0; m < 3; ++m) f[m] = T.order ? da(T.axis[b][m], dm(T.axis[b][3 + m], pf[2 + b])) : T.axis[b][m];
+      break;
+    default: {
+      // mu_s (B sinc) cos (src/jams/hamiltonian/applied_field.cc:17-78,
+      // 146-148); static: mu_s B
+#pragma unroll
+      for (int m = 0; m < 3; ++m) f[m] = dm(P.mus[b], pf ? dm(dm(R.B[m], pf[0]), pf[1]) : R.B[m]);
       break;
     }
   }
@@ -347,11 +363,11 @@ __device__ __forceinline__ void term_field_f64(const Params& P, const TermDev& T
 // Solver::compute_fields: copy of term 0 then daxpy(1.0) of the others
 __device__ __forceinline__ void field_f64(const Params& P, const ReplicaDev& R, Site st, int64_t gi,
                                           const Planes<const double>& S, const double s[3], double h[3],
-                                          const double* hd) {
+                                          const double* hd, const double* pf) {
   h[0] = h[1] = h[2] = 0.0;
   for (int t = 0; t < P.nterms; ++t) {
     double f[3];
-    term_field_f64(P, P.term[t], R, st, gi, S, s, f, hd);
+    term_field_f64(P, P.term[t], R, st, gi, S, s, f, hd, pf);
     if (t == 0) {
       h[0] = f[0];
       h[1] = f[1];
@@ -438,7 +454,7 @@ __global__ void __launch_bounds__(kBlock) heun_predict_f32(const __grid_constant
   const Planes<const float> S = planes(s0, P.npad);
   const float s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
   float h[3], w[3], rhs[3];
-  field_f32(P, R, st, me.gi, S, s, h, P.hdip32);
+  field_f32(P, R, st, me.gi, S, s, h, P.hdip32, pulse_at32(P, step, 0));
   noise_f32(P, R, me.r, st.b, me.i, step, w);
   rhs_f32(P, st.b, s, h, w, rhs);
   float v[3];
@@ -468,9 +484,9 @@ __global__ void __launch_bounds__(kBlock) heun_correct_f32(const __grid_constant
   float w[3];
   noise_f32(P, R, me.r, st.b, me.i, step, w);
   float h[3], r0[3], r1[3];
-  field_f32(P, R, st, me.gi, SP, p, h, P.hdip32);
+  field_f32(P, R, st, me.gi, SP, p, h, P.hdip32, pulse_at32(P, step, 1));
   rhs_f32(P, st.b, p, h, w, r1);
-  field_f32(P, R, st, me.gi, S0, a, h, P.hdip32_s0);
+  field_f32(P, R, st, me.gi, S0, a, h, P.hdip32_s0, pulse_at32(P, step, 0));
   rhs_f32(P, st.b, a, h, w, r0);
   const float hdt = 0.5f * P.dt32;
   float v[3];
@@ -497,7 +513,7 @@ __global__ void __launch_bounds__(kBlock) heun_predict_f64(const __grid_constant
   const Planes<const double> S = planes(s0, P.npad);
   const double s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
   double h[3], w[3], rhs[3];
-  field_f64(P, R, st, me.gi, S, s, h, P.hdip64);
+  field_f64(P, R, st, me.gi, S, s, h, P.hdip64, pulse_at64(P, step, 0));
   noise_f64(P, R, me.r, st.b, me.i, step, w);
   rhs_f64(P, st.b, R.thermal != 0, s, h, w, rhs);
   const Planes<double> D = planes(ds, P.npad);
@@ -527,7 +543,7 @@ __global__ void __launch_bounds__(kBlock) heun_correct_f64(const __grid_constant
   const Planes<const double> SP = planes(sp, P.npad);
   const double p[3] = {SP.x[me.gi], SP.y[me.gi], SP.z[me.gi]};
   double h[3], w[3], rhs[3];
-  field_f64(P, R, st, me.gi, SP, p, h, P.hdip64);
+  field_f64(P, R, st, me.gi, SP, p, h, P.hdip64, pulse_at64(P, step, 1));
   noise_f64(P, R, me.r, st.b, me.i, step, w);
   rhs_f64(P, st.b, R.thermal != 0, p, h, w, rhs);
   const Planes<const double> S0 = planes(s0, P.npad);
@@ -565,7 +581,7 @@ __global__ void __launch_bounds__(kBlock) rk4_stage_f32(const __grid_constant__ 
   const Planes<const float> SI = planes(sin, P.npad);
   const float s[3] = {SI.x[me.gi], SI.y[me.gi], SI.z[me.gi]};
   float h[3], w[3], k[3];
-  field_f32(P, R, st, me.gi, SI, s, h, P.hdip32);
+  field_f32(P, R, st, me.gi, SI, s, h, P.hdip32, pulse_at32(P, step, STAGE - 1));
   noise_f32(P, R, me.r, st.b, me.i, step, w);
   rhs_f32(P, st.b, s, h, w, k);
   const Planes<const float> S0 = planes(s0, P.npad);
@@ -617,7 +633,7 @@ __global__ void __launch_bounds__(kBlock) rk4_stage_f64(const __grid_constant__ 
   const Planes<const double> SI = planes(sin, P.npad);
   const double s[3] = {SI.x[me.gi], SI.y[me.gi], SI.z[me.gi]};
   double h[3], w[3], k[3];
-  field_f64(P, R, st, me.gi, SI, s, h, P.hdip64);
+  field_f64(P, R, st, me.gi, SI, s, h, P.hdip64, pulse_at64(P, step, STAGE - 1));
   noise_f64(P, R, me.r, st.b, me.i, step, w);
   rhs_f64(P, st.b, R.thermal != 0, s, h, w, k);
   const Planes<const double> S0 = planes(s0, P.npad);
@@ -729,7 +745,7 @@ __global__ void __launch_bounds__(kBlock) fields_f32(const __grid_constant__ Par
   const Planes<const float> S = planes(s0, P.npad);
   const float s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
   float h[3];
-  field_f32(P, R, st, me.gi, S, s, h, P.hdip32);
+  field_f32(P, R, st, me.gi, S, s, h, P.hdip32, P.pulse_now32);
   out[3 * (int64_t)me.i] = h[0];
   out[3 * (int64_t)me.i + 1] = h[1];
   out[3 * (int64_t)me.i + 2] = h[2];
@@ -745,7 +761,7 @@ __global__ void __launch_bounds__(kBlock) fields_f64(const __grid_constant__ Par
   const Planes<const double> S = planes(s0, P.npad);
   const double s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
   double h[3];
-  field_f64(P, R, st, me.gi, S, s, h, P.hdip64);
+  field_f64(P, R, st, me.gi, S, s, h, P.hdip64, P.pulse_now64);
   out[3 * (int64_t)me.i] = h[0];
   out[3 * (int64_t)me.i + 1] = h[1];
   out[3 * (int64_t)me.i + 2] = h[2];

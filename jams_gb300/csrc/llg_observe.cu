@@ -102,9 +102,18 @@ __global__ void __launch_bounds__(kBlock) observe_kernel(const __grid_constant__
         if (hd)
           e = -0.5 * (sv[0] * (double)hd[gi] + sv[1] * (double)hd[P.npad + gi] +
                       sv[2] * (double)hd[2 * P.npad + gi]);
+      } else if (T.kind == kZeeman) {
+        // -S . (mu_s B_dc + mu_s B_ac cos(w t)) at the solver time (zeeman.cc:82-87)
+        const double* pf = P.pulse_now64;
+        double f[3];
+        for (int m = 0; m < 3; ++m) f[m] = (T.order && pf) ? T.axis[b][m] + T.axis[b][3 + m] * pf[2 + b] : T.axis[b][m];
+        e = -(sv[0] * f[0] + sv[1] * f[1] + sv[2] * f[2]);
       } else {
-        // -S . (mu_s B)   (applied_field.cc:150-155)
-        e = -(sv[0] * mu * R.B[0] + sv[1] * mu * R.B[1] + sv[2] * mu * R.B[2]);
+        // -S . (mu_s B f(t)) at the solver time   (applied_field.cc:150-155)
+        const double* pf = P.pulse_now64;
+        double f[3];
+        for (int m = 0; m < 3; ++m) f[m] = mu * (pf ? (R.B[m] * pf[0]) * pf[1] : R.B[m]);
+        e = -(sv[0] * f[0] + sv[1] * f[1] + sv[2] * f[2]);
       }
       q[4 + t] = e;
     }

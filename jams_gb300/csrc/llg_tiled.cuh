@@ -152,9 +152,25 @@ struct LocalField {
   float ck;       // 2 K of the cubic term (0: none)
   int corder;
   float cu[9];
-  float hb[3];    // mu_s B
+  float hb[3];    // mu_s B of the applied-field and zeeman terms
   float inv_mus, mg, alpha;
 };
+
+// mu_s B of the applied-field term (times the pulse factors) plus the zeeman
+// term's mu_s B_dc + mu_s B_ac cos(w t), at the time factors pf (null: none)
+__device__ __forceinline__ void field_terms_hb(const Params& P, const ReplicaDev& R, int b, const float* pf,
+                                               float hb[3]) {
+  hb[0] = hb[1] = hb[2] = 0.f;
+  for (int t = 0; t < P.nterms; ++t) {
+    const TermDev& T = P.term[t];
+    if (T.kind == kAppliedField) {
+      for (int m = 0; m < 3; ++m) hb[m] = fa(hb[m], fm(P.mus32[b], pf ? fm(fm(R.Bf[m], pf[0]), pf[1]) : R.Bf[m]));
+    } else if (T.kind == kZeeman) {
+      for (int m = 0; m < 3; ++m)
+        hb[m] = fa(hb[m], (T.order && pf) ? ff(T.axisf[b][3 + m], pf[2 + b], T.axisf[b][m]) : T.axisf[b][m]);
+    }
+  }
+}
 
 __device__ __forceinline__ LocalField local_field(const Params& P, const ReplicaDev& R, int b, int skip) {
   LocalField L;
@@ -180,10 +196,9 @@ __device__ __forceinline__ LocalField local_field(const Params& P, const Replica
       L.ck = fm(2.0f, T.Kf[b]);
       L.corder = T.order;
       for (int m = 0; m < 9; ++m) L.cu[m] = T.axisf[b][m];
-    } else if (T.kind == kAppliedField) {
-      for (int m = 0; m < 3; ++m) L.hb[m] = fm(P.mus32[b], R.Bf[m]);
     }
   }
+  field_terms_hb(P, R, b, nullptr, L.hb);
   L.inv_mus = P.inv_mus32[b];
   L.mg = -P.gyro32[b];
   L.alpha = P.alpha32[b];
@@ -624,7 +639,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     yz[r] = y * V.st[1] + z * V.st[2] + b;
   }
   const float* gather_src = STAGE == 0 ? s0 : sin;
-  const LocalField L = local_field(P, R, b, TP.exch_term);
+  LocalField L = local_field(P, R, b, TP.exch_term);
   constexpr bool has_dip = DIP;   // the model has a dipole term (field planes in P.hdip32)
   const float dt = P.dt32;
   // planes of this replica (outputs, stored rhs / k sum, own start state)
@@ -645,6 +660,14 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   // once for a launch without a programmatic dependency)
   asm volatile("griddepcontrol.wait;" ::: "memory");
   const uint64_t step = *P.step_base + kstep;
+  // time-dependent fields: the factors of this stage (Heun predictor 0,
+  // corrector 1; RK4 stages 0..3) and, for the recomputed rhs(s0), of the
+  // predictor
+  float hb0[3] = {L.hb[0], L.hb[1], L.hb[2]};
+  if (P.pulse32) {
+    field_terms_hb(P, R, b, pulse_at32(P, step, STAGE == 0 ? 0 : (STAGE <= 2 ? 1 : STAGE - 3)), L.hb);
+    if (STAGE == 1) field_terms_hb(P, R, b, pulse_at32(P, step, 0), hb0);
+  }
 
   {
     PlaneRegs<F, TZ, TY, RPT> pr;
@@ -747,7 +770,11 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
           float a[3], r0[3];
           if (STAGE == 1) {
             float h0[3];
-            field_tiled<F, TZ, TY>(L, TP, b, ring1, x, own[r], cy1[r], h0, a, has_dip, dip0[r]);
+            LocalField L0 = L;
+            L0.hb[0] = hb0[0];
+            L0.hb[1] = hb0[1];
+            L0.hb[2] = hb0[2];
+            field_tiled<F, TZ, TY>(L0, TP, b, ring1, x, own[r], cy1[r], h0, a, has_dip, dip0[r]);
             llg_rhs_t(L, a, h0, w[r], r0);
           } else {
 #pragma unroll

@@ -117,6 +117,48 @@ def test_config_errors_are_reported(llg, bad, msg):
         llg.describe_config(cfg)
 
 
+PULSE_HAMILTONIANS = """hamiltonians = (
+  { module = "exchange"; energy_units = "meV"; interactions = ( ("A", "A", [1.0, 0.0, 0.0], 1.0) ); },
+  { module = "applied-field"; type = "sinc-cos"; field = [0.5, -0.3, 2.0]; time_center = 1.0e-14;
+    freq_bandwidth = 5.0e13; freq_center = 8.0e13; },
+  { module = "zeeman"; dc_local_field = ( [0.1, 0.2, -0.3] ); ac_local_field = ( [0.4, 0.0, 0.3] );
+    ac_local_frequency = ( 30.0 ); }
+);
+"""
+
+
+def pulse_config(hamiltonians=PULSE_HAMILTONIANS):
+    cfg = C.sc_ferromagnet(L=4)
+    return cfg[: cfg.index("hamiltonians")] + hamiltonians + cfg[cfg.index("solver"):]
+
+
+def test_time_dependent_fields_in_config(llg):
+    """applied-field type sinc-cos (time_center in s, frequencies in Hz,
+    converted to ps and THz as applied_field.cc:36-38,64-67) and a zeeman term
+    with dc and ac fields per material (zeeman.cc:12-71)."""
+    d = llg.describe_config(pulse_config())
+    af, ze = d["terms"][1], d["terms"][2]
+    assert af["kind"] == W.TERM_APPLIED_FIELD and ze["kind"] == W.TERM_ZEEMAN
+    assert af["B"] == [0.5, -0.3, 2.0]
+    assert af["pulse"] == [W.PULSE_SINC_COS, 1.0e-14 / 1e-12, 5.0e13 / 1e12, 8.0e13 / 1e12]
+    assert ze["dc_field"] == [0.1, 0.2, -0.3]
+    assert ze["ac_field"] == [0.4, 0.0, 0.3]
+    assert ze["ac_frequency"] == [30.0]
+    sinc = pulse_config(PULSE_HAMILTONIANS.replace('type = "sinc-cos"', 'type = "SINC"'))
+    assert llg.describe_config(sinc)["terms"][1]["pulse"][:3] == [W.PULSE_SINC, 1.0e-14 / 1e-12, 5.0e13 / 1e12]
+
+
+@pytest.mark.parametrize("change,msg", [
+    (('type = "sinc-cos"', 'type = "gaussian"'), "unknown field pulse type gaussian"),
+    (("ac_local_frequency = ( 30.0 );", ""), "must have a field and a frequency"),
+    (("dc_local_field = ( [0.1, 0.2, -0.3] );", "dc_local_field = ( [0.1, 0.2, -0.3], [0.0, 0.0, 1.0] );"),
+     "every material"),
+])
+def test_time_dependent_field_config_errors(llg, change, msg):
+    with pytest.raises(llg.LLGError, match=msg):
+        llg.describe_config(pulse_config(PULSE_HAMILTONIANS.replace(*change)))
+
+
 def test_duplicate_site_pair_is_rejected_at_create(llg):
     """Reaching the same site twice is an error in the reference
     (interactions.cc:371-380); it is raised by llg_create before any device
