@@ -115,6 +115,9 @@ def parse(argv=None):
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--ref-gpu", default="auto", choices=["auto", "on", "off"],
+                   help="time the restated reference GPU path (baseline/refgpu.cu) on replica 0: auto = single-replica "
+                        "Heun workloads up to 4.2 M spins")
     p.add_argument("--profile-steps", type=int, default=50)
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--tuning", default="", help="planes_per_cta,flags,occupancy instead of autotuning (flags: 1 stored rhs, 2 narrow tile, "
@@ -319,6 +322,43 @@ def tiled_stem(name: str):
     return tuple(args[:3] + [args[4] if len(args) == 7 else args[3]])
 
 
+def reference_gpu_rate(args, w):
+    """The reference's GPU Heun path restated (baseline/refgpu.cu: cuSPARSE
+    CSR SpMV, cuRAND, cuBLAS and its two update kernels, FP64) on replica 0 of
+    the workload, on this GPU: spin-steps/s over about one second of steps."""
+    supported = {W.TERM_EXCHANGE, W.TERM_UNIAXIAL, W.TERM_CUBIC, W.TERM_APPLIED_FIELD}
+    n = int(np.prod(w.replicas[0].L)) * w.model.nb
+    why = None
+    if args.ref_gpu == "off":
+        return None
+    if w.model.integrator != W.HEUN:
+        why = "the reference GPU path restated here is Heun"
+    elif any(t.kind not in supported or t.pulse != W.PULSE_STATIC for t in w.model.terms):
+        why = "terms outside the restatement (exchange, uniaxial, cubic, static field)"
+    elif args.ref_gpu == "auto" and (len(w.replicas) > 1 or n > (1 << 22)):
+        why = "skipped by default above 4.2 M spins or for several replicas (--ref-gpu on)"
+    if why:
+        return {"unavailable": why}
+    try:
+        from baseline import refgpu as R
+
+        R.build()
+        ref = R.RefGpu(w)
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": "ref-GPU baseline: %s" % str(e)[-200:]}
+    ref.set_state(W.initial_state(w, 0))
+    ref.run(5)
+    probe = ref.run(10)
+    k = int(min(2000, max(20, 1000.0 / max(probe / 10, 1e-3))))
+    ms = ref.run(k)
+    ref.close()
+    return {"value": n * k / (ms * 1e-3), "unit": "spin-steps/s", "kind": "port", "precision": "fp64",
+            "ms_per_step": ms / k, "steps": k, "spins": n,
+            "sample": "replica 0, %d steps after 15 warm-up steps, CUDA events on the baseline's stream" % k,
+            "path": "CUDAHeunLLGSolver::run restated: cuSPARSE CSR SpMV (ALG1), cuRAND normals, blocking field "
+                    "copy + cuBLAS daxpy, 84x3-thread update kernels"}
+
+
 def traffic_from_profiles(workload: str, kernel: str, precision: str):
     """DRAM bytes (read + write) of one launch of `kernel` on `workload`, from
     the committed ncu summary profiles/dram_traffic.json, or None."""
@@ -512,6 +552,10 @@ def main():
                "sample": "%d Heun/RK4 steps of replica 0 (%d spins), oracle restatement of the reference CPU path"
                          % (n_steps, n_rep)}
 
+    ref_gpu = None
+    if rank == 0 and world == 1:
+        ref_gpu = reference_gpu_rate(args, w)
+
     # |M| of every replica of every rank at the end of the run
     mags = [float(sol.observables(r)[0][3]) for r in range(len(w.replicas))]
     mags = gather_scalars(mags, world, torch.device("cuda", local))
@@ -528,7 +572,7 @@ def main():
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         "steady_state_graph": steady, "wall_s_timed_region": t_wall,
         "final_abs_m": {"mean": float(np.mean([m for r in mags for m in r])), "ranks": len(mags)},
-        "dipole": dipole,
+        "dipole": dipole, "reference_gpu": ref_gpu,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -185,6 +185,78 @@ def read_array_file(path: str, dataset: str = "/spins") -> np.ndarray:
     return out if cols.value > 1 else out.reshape(-1)
 
 
+def build_desc(workload: W.Workload, precision: int = FP32C, device: int = 0, steps_per_graph: int = 100,
+               rk4_normalise_stages: bool = False):
+    """The llg_desc of a workload and the arrays it points into (keep them
+    alive while the descriptor is used)."""
+    m = workload.model
+    keep = []
+    terms = (LlgTerm * max(len(m.terms), 1))()
+    for k, t in enumerate(m.terms):
+        lt = terms[k]
+        lt.kind, lt.order = t.kind, t.order
+        if t.bi is not None:
+            arrs = [np.ascontiguousarray(t.bi, dtype=np.int32), np.ascontiguousarray(t.bj, dtype=np.int32),
+                    np.ascontiguousarray(t.T, dtype=np.int32).reshape(-1),
+                    np.ascontiguousarray(t.J, dtype=np.float64).reshape(-1)]
+            keep += arrs
+            lt.n_int = len(arrs[0])
+            lt.bi, lt.bj, lt.T, lt.J = _ip(arrs[0]), _ip(arrs[1]), _ip(arrs[2]), _dp(arrs[3])
+        if t.K is not None:
+            K = np.ascontiguousarray(t.K, dtype=np.float64)
+            ax = np.ascontiguousarray(t.axis, dtype=np.float64).reshape(-1)
+            keep += [K, ax]
+            lt.K, lt.axis = _dp(K), _dp(ax)
+        for j in range(3):
+            lt.B[j] = float(t.B[j])
+        if t.kind == W.TERM_DIPOLE:
+            vec = np.ascontiguousarray(t.lattice_vectors, dtype=np.float64).reshape(-1)
+            pos = np.ascontiguousarray(t.positions, dtype=np.float64).reshape(-1)
+            keep += [vec, pos]
+            lt.r_cutoff, lt.distance_tolerance = float(t.r_cutoff), float(t.distance_tolerance)
+            lt.lattice_parameter = float(t.lattice_parameter)
+            lt.lattice_vectors, lt.positions = _dp(vec), _dp(pos)
+        lt.pulse, lt.time_center = int(t.pulse), float(t.time_center)
+        lt.freq_bandwidth, lt.freq_center = float(t.freq_bandwidth), float(t.freq_center)
+        for name in ("dc_field", "ac_field", "ac_frequency"):
+            v = getattr(t, name)
+            if v is not None:
+                a = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+                keep.append(a)
+                setattr(lt, name, _dp(a))
+    reps = (LlgReplica * len(workload.replicas))()
+    for r, rp in enumerate(workload.replicas):
+        for j in range(3):
+            reps[r].L[j] = int(rp.L[j])
+        reps[r].temperature = float(rp.temperature)
+        if rp.B is not None:
+            reps[r].use_B = 1
+            for j in range(3):
+                reps[r].B[j] = float(rp.B[j])
+    mats = [np.ascontiguousarray(x, dtype=np.float64) for x in (m.mus, m.gyro, m.alpha)]
+    keep += mats
+    d = LlgDesc()
+    d.abi_version = LLG_ABI_VERSION
+    d.nb = m.nb
+    for j in range(3):
+        d.periodic[j] = int(m.periodic[j])
+    d.mus, d.gyro, d.alpha = _dp(mats[0]), _dp(mats[1]), _dp(mats[2])
+    d.n_terms = len(m.terms)
+    d.terms = ctypes.cast(terms, ctypes.POINTER(LlgTerm))
+    d.dt = m.dt
+    d.gilbert_prefactor = int(bool(m.gilbert_prefactor))
+    d.integrator = int(m.integrator)
+    d.precision = int(precision)
+    d.rk4_normalise_stages = int(bool(rk4_normalise_stages))
+    d.seed = int(workload.seed)
+    d.n_replicas = len(workload.replicas)
+    d.replicas = ctypes.cast(reps, ctypes.POINTER(LlgReplica))
+    d.device = int(device)
+    d.steps_per_graph = int(steps_per_graph)
+    keep += [terms, reps]
+    return d, keep
+
+
 class Solver:
     """A JAMS LLG solver (Heun or RK4) on one GPU for all replicas of a
     workload: the CUDAHeunLLGSolver / CUDALLGRK4Solver of the reference with
@@ -195,70 +267,8 @@ class Solver:
         self.L = lib()
         self.workload = workload
         m = workload.model
-        self._keep = []
-        terms = (LlgTerm * max(len(m.terms), 1))()
-        for k, t in enumerate(m.terms):
-            lt = terms[k]
-            lt.kind, lt.order = t.kind, t.order
-            if t.bi is not None:
-                arrs = [np.ascontiguousarray(t.bi, dtype=np.int32), np.ascontiguousarray(t.bj, dtype=np.int32),
-                        np.ascontiguousarray(t.T, dtype=np.int32).reshape(-1),
-                        np.ascontiguousarray(t.J, dtype=np.float64).reshape(-1)]
-                self._keep += arrs
-                lt.n_int = len(arrs[0])
-                lt.bi, lt.bj, lt.T, lt.J = _ip(arrs[0]), _ip(arrs[1]), _ip(arrs[2]), _dp(arrs[3])
-            if t.K is not None:
-                K = np.ascontiguousarray(t.K, dtype=np.float64)
-                ax = np.ascontiguousarray(t.axis, dtype=np.float64).reshape(-1)
-                self._keep += [K, ax]
-                lt.K, lt.axis = _dp(K), _dp(ax)
-            for j in range(3):
-                lt.B[j] = float(t.B[j])
-            if t.kind == W.TERM_DIPOLE:
-                vec = np.ascontiguousarray(t.lattice_vectors, dtype=np.float64).reshape(-1)
-                pos = np.ascontiguousarray(t.positions, dtype=np.float64).reshape(-1)
-                self._keep += [vec, pos]
-                lt.r_cutoff, lt.distance_tolerance = float(t.r_cutoff), float(t.distance_tolerance)
-                lt.lattice_parameter = float(t.lattice_parameter)
-                lt.lattice_vectors, lt.positions = _dp(vec), _dp(pos)
-            lt.pulse, lt.time_center = int(t.pulse), float(t.time_center)
-            lt.freq_bandwidth, lt.freq_center = float(t.freq_bandwidth), float(t.freq_center)
-            for name in ("dc_field", "ac_field", "ac_frequency"):
-                v = getattr(t, name)
-                if v is not None:
-                    a = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
-                    self._keep.append(a)
-                    setattr(lt, name, _dp(a))
-        reps = (LlgReplica * len(workload.replicas))()
-        for r, rp in enumerate(workload.replicas):
-            for j in range(3):
-                reps[r].L[j] = int(rp.L[j])
-            reps[r].temperature = float(rp.temperature)
-            if rp.B is not None:
-                reps[r].use_B = 1
-                for j in range(3):
-                    reps[r].B[j] = float(rp.B[j])
-        mats = [np.ascontiguousarray(x, dtype=np.float64) for x in (m.mus, m.gyro, m.alpha)]
-        self._keep += mats
-        d = LlgDesc()
-        d.abi_version = LLG_ABI_VERSION
-        d.nb = m.nb
-        for j in range(3):
-            d.periodic[j] = int(m.periodic[j])
-        d.mus, d.gyro, d.alpha = _dp(mats[0]), _dp(mats[1]), _dp(mats[2])
-        d.n_terms = len(m.terms)
-        d.terms = ctypes.cast(terms, ctypes.POINTER(LlgTerm))
-        d.dt = m.dt
-        d.gilbert_prefactor = int(bool(m.gilbert_prefactor))
-        d.integrator = int(m.integrator)
-        d.precision = int(precision)
-        d.rk4_normalise_stages = int(bool(rk4_normalise_stages))
-        d.seed = int(workload.seed)
-        d.n_replicas = len(workload.replicas)
-        d.replicas = ctypes.cast(reps, ctypes.POINTER(LlgReplica))
-        d.device = int(device)
-        d.steps_per_graph = int(steps_per_graph)
-        self._terms, self._reps, self._desc = terms, reps, d
+        d, self._keep = build_desc(workload, precision, device, steps_per_graph, rk4_normalise_stages)
+        self._desc = d
         h = ctypes.c_void_p()
         rc = self.L.llg_create(ctypes.byref(d), ctypes.byref(h))
         if rc != 0:
