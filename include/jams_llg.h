@@ -230,6 +230,16 @@ int llg_fields(llg_handle *h, int32_t replica, double *h_host);
    (Hamiltonian::calculate_total_energy). */
 int llg_observables(llg_handle *h, int32_t replica, double *m4, double *e_terms);
 
+/* Magnetisation by groups of basis sites, as MagnetisationMonitor
+   (src/jams/monitors/magnetisation.cc:20-104): group_of_basis[b] in
+   [0, ngroups) is the group of basis site b (grouping "materials": its
+   material; "positions": b; "none": 0).  m4[4g..4g+2] = sum mu_s S over the
+   spins of group g and m4[4g+3] = |sum mu_s S|, divided by the group's
+   sum mu_s (normalize != 0) or by the Bohr magneton in meV/T (normalize = 0,
+   moments in Bohr magnetons).  Synchronous. */
+int llg_magnetisation_groups(llg_handle *h, int32_t replica, const int32_t *group_of_basis, int32_t ngroups,
+                             int32_t normalize, double *m4);
+
 /* Geometric topological charge of a one-basis-site triangular monolayer
    replica (src/jams/monitors/topological_charge_geometrical_def.cc:159-181). */
 int llg_topological_charge(llg_handle *h, int32_t replica, double *q);

@@ -1043,6 +1043,9 @@ int llg_config_describe(const char* config_text, const char* patch_text, char* j
       }
       o << "]";
     };
+    std::vector<double> basis_material;
+    for (const Basis& b : m.basis) basis_material.push_back((double)b.mat);
+    arr("basis_material", basis_material);   // material index of each basis site (magnetisation grouping)
     arr("mus", m.mus);
     arr("gyro", m.gyro);
     arr("alpha", m.alpha);

@@ -853,7 +853,7 @@ int build(llg_handle* h, const llg_desc* d) {
   if ((ce = h->d_scratch.alloc(3 * maxn)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   size_t max_tiles = 0;
   for (int r = 0; r < d->n_replicas; ++r) max_tiles = std::max<size_t>(max_tiles, h->rep_ntiles[r]);
-  const size_t nq = 4 + (size_t)kMaxTerms;
+  const size_t nq = 4 + (size_t)kMaxTerms + 4 * (size_t)kMaxBasis;
   if ((ce = h->d_partials.alloc(std::max<size_t>(max_tiles, 1) * nq)) != cudaSuccess) return h->cuda_fail(ce, "alloc");
   h->h_partials.resize(std::max<size_t>(max_tiles, 1) * nq);
   h->params_dirty = true;
@@ -1397,14 +1397,17 @@ int llg_fields(llg_handle* h, int32_t replica, double* h_host) {
   return 0;
 }
 
-int llg_observables(llg_handle* h, int32_t replica, double* m4, double* e_terms) {
+// the replica's observable sums in the observe kernel's layout: mu_s S and
+// mu_s (0..3), the energy of every term (4..), mu_s S and mu_s per basis site
+// (4 + nterms + 4 b ..)
+static int observe_sums(llg_handle* h, int32_t replica, std::vector<double>& sum) {
   if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
   if (replica < 0 || replica >= (int32_t)h->reps.size())
     return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
   cudaSetDevice(h->device);
   int rc = sync_replicas(h);
   if (rc) return rc;
-  const int nq = 4 + h->nterms;
+  const int nq = 4 + h->nterms + 4 * h->nb;
   const int sb = state_buffer(h);
   rc = upload_pulse_now(h);   // energies at the solver time
   if (rc) return rc;
@@ -1418,7 +1421,8 @@ int llg_observables(llg_handle* h, int32_t replica, double* m4, double* e_terms)
                h->d_partials.p, h->h_partials.data(), nq, h->stream);
   if (rc) return h->cuda_fail(cudaGetLastError(), "observables");
   // ordered sums over tiles (deterministic), Neumaier compensation
-  std::vector<double> sum(nq, 0.0), comp(nq, 0.0);
+  sum.assign(nq, 0.0);
+  std::vector<double> comp(nq, 0.0);
   for (int t = 0; t < h->rep_ntiles[replica]; ++t)
     for (int q = 0; q < nq; ++q) {
       const double x = h->h_partials[(size_t)t * nq + q];
@@ -1427,6 +1431,13 @@ int llg_observables(llg_handle* h, int32_t replica, double* m4, double* e_terms)
       sum[q] = s;
     }
   for (int q = 0; q < nq; ++q) sum[q] += comp[q];
+  return 0;
+}
+
+int llg_observables(llg_handle* h, int32_t replica, double* m4, double* e_terms) {
+  std::vector<double> sum;
+  const int rc = observe_sums(h, replica, sum);
+  if (rc) return rc;
   if (m4) {
     m4[0] = sum[0] / sum[3];
     m4[1] = sum[1] / sum[3];
@@ -1435,6 +1446,31 @@ int llg_observables(llg_handle* h, int32_t replica, double* m4, double* e_terms)
   }
   if (e_terms)
     for (int t = 0; t < h->nterms; ++t) e_terms[t] = sum[4 + t];
+  return 0;
+}
+
+int llg_magnetisation_groups(llg_handle* h, int32_t replica, const int32_t* group_of_basis, int32_t ngroups,
+                             int32_t normalize, double* m4) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (!group_of_basis || !m4 || ngroups < 1) return h->fail(LLG_ERR_BAD_DESC, "bad group arguments");
+  for (int b = 0; b < h->nb; ++b)
+    if (group_of_basis[b] < 0 || group_of_basis[b] >= ngroups)
+      return h->fail(LLG_ERR_BAD_DESC, "basis site %d: group %d outside [0, %d)", b, group_of_basis[b], ngroups);
+  std::vector<double> sum;
+  const int rc = observe_sums(h, replica, sum);
+  if (rc) return rc;
+  constexpr double kBohrMagnetonIU = 0.0578838181;   // meV/T, src/jams/helpers/consts.h:30
+  std::vector<double> g(4 * (size_t)ngroups, 0.0);
+  for (int b = 0; b < h->nb; ++b)
+    for (int k = 0; k < 4; ++k) g[4 * (size_t)group_of_basis[b] + k] += sum[4 + h->nterms + 4 * b + k];
+  for (int q = 0; q < ngroups; ++q) {
+    const double* x = &g[4 * (size_t)q];
+    const double f = normalize ? 1.0 / x[3] : 1.0 / kBohrMagnetonIU;
+    m4[4 * q] = x[0] * f;
+    m4[4 * q + 1] = x[1] * f;
+    m4[4 * q + 2] = x[2] * f;
+    m4[4 * q + 3] = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) * f;
+  }
   return 0;
 }
 

@@ -30,7 +30,10 @@ __device__ __forceinline__ int axis_class_o(int c, int L, int R, int ncls) {
   return R;
 }
 
-// per-spin contributions: q0..2 = mu_s S, q3 = mu_s, q4+t = energy of term t
+// per-spin contributions: q0..2 = mu_s S, q3 = mu_s, q4+t = energy of term t,
+// then per basis site b: q[4 + nterms + 4b + 0..3] = mu_s S, mu_s of the
+// site's spins (zero elsewhere), for the magnetisation by material or
+// position (src/jams/monitors/magnetisation.cc:20-104)
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) observe_kernel(const __grid_constant__ Params P,
                                                          const Real* __restrict__ s, int first_tile,
@@ -41,9 +44,9 @@ __global__ void __launch_bounds__(kBlock) observe_kernel(const __grid_constant__
   const ReplicaDev& R = P.rep[tile.x];
   const int32_t i = tile.y + (int32_t)threadIdx.x;
   const bool active = i < R.n;
-  double q[4 + kMaxTerms];
+  double q[4 + kMaxTerms + 4 * kMaxBasis];
 #pragma unroll
-  for (int k = 0; k < 4 + kMaxTerms; ++k) q[k] = 0.0;
+  for (int k = 0; k < 4 + kMaxTerms + 4 * kMaxBasis; ++k) q[k] = 0.0;
   if (active) {
     const int64_t gi = R.offset + i;
     const int b = i % P.nb;
@@ -62,6 +65,11 @@ __global__ void __launch_bounds__(kBlock) observe_kernel(const __grid_constant__
     q[1] = mu * sv[1];
     q[2] = mu * sv[2];
     q[3] = mu;
+    double* qb = q + 4 + P.nterms + 4 * b;
+    qb[0] = q[0];
+    qb[1] = q[1];
+    qb[2] = q[2];
+    qb[3] = mu;
     for (int t = 0; t < P.nterms; ++t) {
       const TermDev& T = P.term[t];
       double e = 0.0;

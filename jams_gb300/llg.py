@@ -36,7 +36,7 @@ EXPORTED = [
     "llg_profile_stages", "llg_kernel_info", "llg_set_tuning", "llg_autotune", "llg_magnetisation_noalloc",
     "llg_create_from_config", "llg_config_describe", "llg_max_steps",
     "llg_write_array_file", "llg_read_array_file", "llg_write_spins", "llg_read_spins",
-    "llg_save_checkpoint", "llg_load_checkpoint",
+    "llg_save_checkpoint", "llg_load_checkpoint", "llg_magnetisation_groups",
 ]
 
 
@@ -110,6 +110,7 @@ def lib():
         L.llg_set_field.argtypes = [vp, i32, dp]
         L.llg_fields.argtypes = [vp, i32, dp]
         L.llg_observables.argtypes = [vp, i32, dp, dp]
+        L.llg_magnetisation_groups.argtypes = [vp, i32, ctypes.POINTER(i32), i32, i32, dp]
         L.llg_topological_charge.argtypes = [vp, i32, dp]
         L.llg_set_stream.argtypes = [vp, vp]
         L.llg_last_launch_count.argtypes = [vp]
@@ -377,6 +378,17 @@ class Solver:
         e = np.empty(max(self.n_terms, 1))
         self._check(self.L.llg_observables(self.h, replica, _dp(m4), _dp(e)))
         return m4, e[: self.n_terms]
+
+    def magnetisation_groups(self, group_of_basis: Sequence[int], replica: int = 0,
+                             normalize: bool = True) -> np.ndarray:
+        """Magnetisation by groups of basis sites (the reference monitor's
+        "materials" / "positions" / "none" grouping): rows (mx, my, mz, |m|)
+        per group, over sum mu_s or in Bohr magnetons (normalize=False)."""
+        g = np.ascontiguousarray(group_of_basis, dtype=np.int32)
+        ng = int(g.max()) + 1 if g.size else 1
+        out = np.empty((ng, 4))
+        self._check(self.L.llg_magnetisation_groups(self.h, replica, _ip(g), ng, int(bool(normalize)), _dp(out)))
+        return out
 
     def topological_charge(self, replica: int = 0) -> float:
         q = np.empty(1)

@@ -334,3 +334,43 @@ def test_fcc_families_match_oracle(llg, oracle, J2):
     d.step(1000)
     assert np.array_equal(d.get_state(0), ref)
 
+
+
+@pytest.mark.parametrize("prec", ["FP64", "FP32C"])
+def test_magnetisation_by_material_and_position(llg, prec):
+    """The reference monitor's groupings (magnetisation.cc:20-104): per basis
+    position, per material (here two materials on the fcc cell's four sites),
+    and none; normalised by sum mu_s or in Bohr magnetons."""
+    w = W.fcc_ferromagnet(L=(3, 4, 5), T=0.0, start="random")
+    w.model.mus = np.array([2.0, 1.5, 1.5, 2.0]) * W.K_BOHR_MAGNETON_IU
+    s = solver(llg, w, getattr(llg, prec))
+    s0 = W.initial_state(w, 0)
+    s.set_state(s0)
+    s.step(3)
+    st = s.get_state(0)
+    nb = w.model.nb
+    mus = np.tile(w.model.mus, len(st) // nb)
+    ms = st * mus[:, None]
+
+    def want(groups, normalize):
+        out = []
+        for g in range(max(groups) + 1):
+            sel = np.isin(np.arange(len(st)) % nb, [b for b in range(nb) if groups[b] == g])
+            v = ms[sel].sum(axis=0)
+            f = 1.0 / mus[sel].sum() if normalize else 1.0 / W.K_BOHR_MAGNETON_IU
+            out.append(np.concatenate([v * f, [np.linalg.norm(v) * f]]))
+        return np.array(out)
+
+    for groups in ([0, 1, 2, 3], [0, 1, 1, 0], [0, 0, 0, 0]):
+        for normalize in (True, False):
+            got = s.magnetisation_groups(groups, normalize=normalize)
+            np.testing.assert_allclose(got, want(groups, normalize), rtol=1e-12, atol=1e-12)
+    m4, _ = s.observables(0)
+    np.testing.assert_allclose(s.magnetisation_groups([0, 0, 0, 0])[0], m4, rtol=1e-13, atol=1e-15)
+    import ctypes
+
+    g = np.array([0, 1, 2, 5], dtype=np.int32)
+    out = np.empty(12)
+    rc = s.L.llg_magnetisation_groups(s.h, 0, g.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 3, 1,
+                                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert rc < 0 and "outside" in s.L.llg_last_error(s.h).decode()
