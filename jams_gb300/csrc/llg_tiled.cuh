@@ -161,6 +161,7 @@ struct LocalField {
 __device__ __forceinline__ void field_terms_hb(const Params& P, const ReplicaDev& R, int b, const float* pf,
                                                float hb[3]) {
   hb[0] = hb[1] = hb[2] = 0.f;
+#pragma unroll 1
   for (int t = 0; t < P.nterms; ++t) {
     const TermDev& T = P.term[t];
     if (T.kind == kAppliedField) {
@@ -198,7 +199,7 @@ __device__ __forceinline__ LocalField local_field(const Params& P, const Replica
       for (int m = 0; m < 9; ++m) L.cu[m] = T.axisf[b][m];
     }
   }
-  field_terms_hb(P, R, b, nullptr, L.hb);
+  // L.hb: field_terms_hb once the stage's time is known
   L.inv_mus = P.inv_mus32[b];
   L.mg = -P.gyro32[b];
   L.alpha = P.alpha32[b];
@@ -660,14 +661,12 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   // once for a launch without a programmatic dependency)
   asm volatile("griddepcontrol.wait;" ::: "memory");
   const uint64_t step = *P.step_base + kstep;
-  // time-dependent fields: the factors of this stage (Heun predictor 0,
-  // corrector 1; RK4 stages 0..3) and, for the recomputed rhs(s0), of the
-  // predictor
-  float hb0[3] = {L.hb[0], L.hb[1], L.hb[2]};
-  if (P.pulse32) {
-    field_terms_hb(P, R, b, pulse_at32(P, step, STAGE == 0 ? 0 : (STAGE <= 2 ? 1 : STAGE - 3)), L.hb);
-    if (STAGE == 1) field_terms_hb(P, R, b, pulse_at32(P, step, 0), hb0);
-  }
+  // applied-field and zeeman terms at this stage's time (Heun predictor 0,
+  // corrector 1; RK4 stages 0..3) and, for the recomputed rhs(s0), at the
+  // predictor's
+  field_terms_hb(P, R, b, pulse_at32(P, step, STAGE == 0 ? 0 : (STAGE <= 2 ? 1 : STAGE - 3)), L.hb);
+  float hb0[3] = {0.f, 0.f, 0.f};
+  if (STAGE == 1) field_terms_hb(P, R, b, pulse_at32(P, step, 0), hb0);
 
   {
     PlaneRegs<F, TZ, TY, RPT> pr;
