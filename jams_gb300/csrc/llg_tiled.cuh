@@ -627,7 +627,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   const int tid = threadIdx.x + TZ * threadIdx.y;
   const int tz = threadIdx.x;
   const int ty = (threadIdx.y % TYT) * RPT;   // the first of the thread's rows
-  const int b = threadIdx.y / TYT;
+  const int b = __shfl_sync(0xffffffffu, (int)(threadIdx.y / TYT), 0);   // uniform per warp
   const float amp = R.amp32[b];
   const int z = z0 + tz;
   bool active[RPT];   // the row's cell lies in the lattice
