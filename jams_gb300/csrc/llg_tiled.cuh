@@ -518,15 +518,27 @@ struct View {
   int64_t offset;
 };
 
+// a value that is the same in every lane, taken from lane 0: the compiler
+// then knows it is warp-uniform and can keep it in a uniform register.
+// U = false leaves it in ordinary registers (the two-rows-per-thread kernels
+// measured faster that way: their register allocation spilled more with the
+// per-CTA view in uniform registers).
+template <bool U = true, typename T>
+__device__ __forceinline__ T uniform(T v) {
+  if constexpr (U) return __shfl_sync(0xffffffffu, v, 0);
+  else return v;
+}
+
+template <bool U>
 __device__ __forceinline__ View load_view(const ReplicaDev& R) {
   View v;
 #pragma unroll
   for (int l = 0; l < 3; ++l) {
-    v.L[l] = R.vL[l];
-    v.st[l] = (int)R.vs[l];
-    v.per[l] = R.vper[l] != 0;
+    v.L[l] = uniform<U>(R.vL[l]);
+    v.st[l] = uniform<U>((int)R.vs[l]);
+    v.per[l] = uniform<U>(R.vper[l]) != 0;
   }
-  v.offset = R.offset;
+  v.offset = uniform<U>((long long)R.offset);
   return v;
 }
 
@@ -619,16 +631,19 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   // once every CTA of this one has started; they set up, then wait for this
   // launch to complete before they read what it wrote
   asm volatile("griddepcontrol.launch_dependents;");
-  const int4 tile = TP.tiles[blockIdx.x];
+  const int4 tile0 = TP.tiles[blockIdx.x];
+  constexpr bool UV = RPT == 1;   // per-CTA view in uniform registers
+  const int4 tile =
+      make_int4(uniform<UV>(tile0.x), uniform<UV>(tile0.y), uniform<UV>(tile0.z), uniform<UV>(tile0.w));
   const ReplicaDev& R = P.rep[tile.x];
-  const View V = load_view(R);
-  const int thermal = R.thermal;
+  const View V = load_view<UV>(R);
+  const int thermal = uniform<UV>(R.thermal);
   const int x0 = tile.y, y0 = tile.z, z0 = tile.w;
   const int tid = threadIdx.x + TZ * threadIdx.y;
   const int tz = threadIdx.x;
   const int ty = (threadIdx.y % TYT) * RPT;   // the first of the thread's rows
   const int b = __shfl_sync(0xffffffffu, (int)(threadIdx.y / TYT), 0);   // uniform per warp
-  const float amp = R.amp32[b];
+  const float amp = uniform<UV>(R.amp32[b]);
   const int z = z0 + tz;
   bool active[RPT];   // the row's cell lies in the lattice
   int own[RPT], yz[RPT];
@@ -660,7 +675,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   // rhs, dipole field, step counter): wait for them to complete (returns at
   // once for a launch without a programmatic dependency)
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  const uint64_t step = *P.step_base + kstep;
+  const uint64_t step = uniform<UV>((unsigned long long)*P.step_base) + kstep;
   // applied-field and zeeman terms at this stage's time (Heun predictor 0,
   // corrector 1; RK4 stages 0..3) and, for the recomputed rhs(s0), at the
   // predictor's
