@@ -1160,8 +1160,7 @@ int32_t llg_num_replicas(const llg_handle* h) { return h ? (int32_t)h->reps.size
 
 // the device address of a pinned, mapped host buffer (the unpack kernel then
 // reads it in place over the host link, in one pass with the layout
-// conversion, and the pack kernel writes it in place with whole-line
-// stores), or null for pageable memory (copied by the DMA engines through
+// conversion), or null for pageable memory (copied by the DMA engines through
 // the device scratch buffer)
 static void* mapped_host(const void* p) {
   cudaPointerAttributes a;
@@ -1201,18 +1200,15 @@ static int transfer_state(llg_handle* h, int32_t replica, const double* src, dou
         if (ce != cudaSuccess) return h->cuda_fail(ce, "setting spins");
       }
     } else {
+      // results go back through the copy engines: the pack kernel's own
+      // stores into pinned host memory were as fast (78 us for 12.6 MB) on
+      // some runs and 7x slower on others
       double* d = dst + 3 * host_off;
-      // pinned (mapped) host buffers are written in place by the pack kernel,
-      // whole cache lines at a time; other host buffers through a copy
-      void* m = device_ptr ? nullptr : mapped_host(d);
       if (device_ptr) dev_aos = d;
-      else if (m) dev_aos = static_cast<double*>(m);
       launch_pack(h->fp64, h->stream, h->state[sb].p, dev_aos, R.offset, R.n, h->npad);
-      if (!device_ptr && !m) {
+      if (!device_ptr) {
         ce = cudaMemcpyAsync(d, dev_aos, bytes, cudaMemcpyDeviceToHost, h->stream);
         if (ce != cudaSuccess) return h->cuda_fail(ce, "copying spins to the host");
-      }
-      if (!device_ptr) {
         ce = cudaStreamSynchronize(h->stream);
         if (ce != cudaSuccess) return h->cuda_fail(ce, "getting spins");
       }

@@ -93,9 +93,10 @@ def test_checkpoint_rejects_other_models_and_corruption(llg, tmp_path):
 
 
 def test_pinned_host_buffers_go_through_the_mapped_path(llg):
-    """Pinned host buffers are read and written in place by the pack/unpack
-    kernels; the result equals the pageable (copied) path bit for bit,
-    including a replica's rows in the middle of a pinned buffer."""
+    """Pinned host buffers are read in place by the unpack kernel (results
+    come back through the copy engines); the result equals the pageable
+    (copied) path bit for bit, including a replica's rows in the middle of a
+    pinned buffer."""
     torch = pytest.importorskip("torch")
     w = W.sc_temperature_sweep(n_replicas=3, L_min=5, L_max=8)
     sizes = [int(np.prod(r.L)) for r in w.replicas]
