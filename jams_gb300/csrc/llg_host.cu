@@ -1060,10 +1060,12 @@ bool launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
       float* s0 = buf<float>(h, cur);
       float* sp = buf<float>(h, 1);
       float* s1 = buf<float>(h, 2 - cur);
+      // rhs(s0) stored by the predictor for the corrector
+      float* rhs0 = reinterpret_cast<float*>(h->aux.p);
       if (stage == 0)
-        heun_predict_f32<<<grid, kBlock, 0, st>>>(P, s0, sp, ks);
+        heun_predict_f32<<<grid, kBlock, 0, st>>>(P, s0, sp, rhs0, ks);
       else
-        heun_correct_f32<<<grid, kBlock, 0, st>>>(P, s0, sp, s1, ks);
+        heun_correct_f32<<<grid, kBlock, 0, st>>>(P, s0, sp, s1, rhs0, ks);
     }
   } else {
     // state stays in buffer 0; 1 and 2 hold stage states, aux the k sum

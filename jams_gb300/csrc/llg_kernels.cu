@@ -443,8 +443,10 @@ __device__ __forceinline__ Me whoami(const Params& P, const ReplicaDev*& Rp) {
 // ================================================================== Heun ==
 
 // predictor: s_pred = unit(s0 + dt rhs(s0)); FP64 also stores ds = rhs/2
+// rhs0 (non-null): rhs(s0) stored for the corrector
 __global__ void __launch_bounds__(kBlock) heun_predict_f32(const __grid_constant__ Params P, const float* __restrict__ s0,
-                                                          float* __restrict__ sp, uint32_t kstep) {
+                                                          float* __restrict__ sp, float* __restrict__ rhs0,
+                                                          uint32_t kstep) {
   const ReplicaDev* Rp;
   const Me me = whoami(P, Rp);
   if (!me.active) return;
@@ -465,12 +467,19 @@ __global__ void __launch_bounds__(kBlock) heun_predict_f32(const __grid_constant
   O.x[me.gi] = v[0];
   O.y[me.gi] = v[1];
   O.z[me.gi] = v[2];
+  if (rhs0) {
+    const Planes<float> A = planes(rhs0, P.npad);
+    A.x[me.gi] = rhs[0];
+    A.y[me.gi] = rhs[1];
+    A.z[me.gi] = rhs[2];
+  }
 }
 
-// corrector: s1 = unit(s0 + dt (rhs(s0) + rhs(s_pred)) / 2); rhs(s0) recomputed
+// corrector: s1 = unit(s0 + dt (rhs(s0) + rhs(s_pred)) / 2); rhs(s0) read
+// from the predictor's store (rhs0 non-null, the same value) or recomputed
 __global__ void __launch_bounds__(kBlock) heun_correct_f32(const __grid_constant__ Params P, const float* __restrict__ s0,
-                                                          const float* __restrict__ sp,
-                                                          float* __restrict__ s1, uint32_t kstep) {
+                                                          const float* __restrict__ sp, float* __restrict__ s1,
+                                                          const float* __restrict__ rhs0, uint32_t kstep) {
   const ReplicaDev* Rp;
   const Me me = whoami(P, Rp);
   if (!me.active) return;
@@ -484,10 +493,18 @@ __global__ void __launch_bounds__(kBlock) heun_correct_f32(const __grid_constant
   float w[3];
   noise_f32(P, R, me.r, st.b, me.i, step, w);
   float h[3], r0[3], r1[3];
+  if (rhs0) {
+    const Planes<const float> A = planes(rhs0, P.npad);
+    r0[0] = A.x[me.gi];
+    r0[1] = A.y[me.gi];
+    r0[2] = A.z[me.gi];
+  }
   field_f32(P, R, st, me.gi, SP, p, h, P.hdip32, pulse_at32(P, step, 1));
   rhs_f32(P, st.b, p, h, w, r1);
-  field_f32(P, R, st, me.gi, S0, a, h, P.hdip32_s0, pulse_at32(P, step, 0));
-  rhs_f32(P, st.b, a, h, w, r0);
+  if (!rhs0) {
+    field_f32(P, R, st, me.gi, S0, a, h, P.hdip32_s0, pulse_at32(P, step, 0));
+    rhs_f32(P, st.b, a, h, w, r0);
+  }
   const float hdt = 0.5f * P.dt32;
   float v[3];
 #pragma unroll

@@ -8,9 +8,10 @@
 namespace jams_llg {
 
 __global__ void heun_predict_f32(const __grid_constant__ Params P, const float* __restrict__ s0,
-                                 float* __restrict__ sp, uint32_t kstep);
+                                 float* __restrict__ sp, float* __restrict__ rhs0, uint32_t kstep);
 __global__ void heun_correct_f32(const __grid_constant__ Params P, const float* __restrict__ s0,
-                                 const float* __restrict__ sp, float* __restrict__ s1, uint32_t kstep);
+                                 const float* __restrict__ sp, float* __restrict__ s1,
+                                 const float* __restrict__ rhs0, uint32_t kstep);
 __global__ void heun_predict_f64(const __grid_constant__ Params P, const double* __restrict__ s0,
                                  double* __restrict__ sp, double* __restrict__ ds, uint32_t kstep);
 __global__ void heun_correct_f64(const __grid_constant__ Params P, const double* s0, const double* sp,
