@@ -49,7 +49,9 @@ enum {
   LLG_ERR_NONFINITE = -5,    /* a spin became NaN or infinite */
   LLG_ERR_NO_DEVICE = -6,    /* no usable sm_103 device */
   LLG_ERR_UNSUPPORTED = -7,  /* combination not implemented */
-  LLG_ERR_IO = -8            /* a file could not be read, written or parsed */
+  LLG_ERR_IO = -8,           /* a file could not be read, written or parsed */
+  LLG_ERR_BOUNDS = -9        /* bounds-checked build: a kernel met an index outside its array (the access was
+                                skipped) */
 };
 
 /* arithmetic form */

@@ -1321,6 +1321,8 @@ int llg_synchronize(llg_handle* h) {
   if (ce != cudaSuccess) return h->cuda_fail(ce, "reading status");
   ce = cudaStreamSynchronize(h->stream);
   if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaStreamSynchronize");
+  if (*h->h_status.p & 2u)
+    return h->fail(LLG_ERR_BOUNDS, "a kernel met an index outside its array (bounds-checked build; access skipped)");
   if (*h->h_status.p & 1u) return h->fail(LLG_ERR_NONFINITE, "a spin became NaN or infinite");
   return 0;
 }

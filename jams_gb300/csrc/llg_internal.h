@@ -27,6 +27,18 @@ constexpr int32_t kMissing = INT32_MIN;  // neighbour outside an open boundary
 
 enum TermKind { kExchange = 0, kUniaxial = 1, kCubic = 2, kAppliedField = 3, kDipole = 4, kZeeman = 5 };
 
+// Bounds-checked build (compiled with LLG_BOUNDS_CHECK, a library of its own):
+// every gathered or stored index is checked against its array; an index
+// outside sets status bit 1, the access is skipped and llg_synchronize
+// reports LLG_ERR_BOUNDS.  Nothing asserts or traps.  In the normal build
+// the check is compiled out.
+#ifdef LLG_BOUNDS_CHECK
+#define LLG_IN_RANGE(P, j, lo, hi) \
+  (((int64_t)(j) >= (int64_t)(lo) && (int64_t)(j) < (int64_t)(hi)) ? true : (atomicOr((P).status, 2u), false))
+#else
+#define LLG_IN_RANGE(P, j, lo, hi) true
+#endif
+
 // time factors of the time-dependent fields at one stage time t: the
 // applied-field pulse's sinc and cos factors (1 when absent) and, per basis
 // site, the zeeman term's cos(w_b t)

@@ -122,7 +122,7 @@ __device__ __forceinline__ void exchange_f32(const Params& P, int t, const Repli
     const int end = E.group_end[b][g];
     for (; slot < end; ++slot) {
       const int32_t off = __ldg(tab + slot);
-      if (off != kMissing) {
+      if (off != kMissing && LLG_IN_RANGE(P, gi + off, R.offset, R.offset + R.n)) {
         const int64_t j = gi + off;
         ax += __ldg(S.x + j);
         ay += __ldg(S.y + j);
@@ -137,7 +137,7 @@ __device__ __forceinline__ void exchange_f32(const Params& P, int t, const Repli
   const int ns = E.nslot[b];
   for (; slot < ns; ++slot) {
     const int32_t off = __ldg(tab + slot);
-    if (off == kMissing) continue;
+    if (off == kMissing || !LLG_IN_RANGE(P, gi + off, R.offset, R.offset + R.n)) continue;
     const int64_t j = gi + off;
     const float sx = __ldg(S.x + j), sy = __ldg(S.y + j), sz = __ldg(S.z + j);
     const float* Jr = E.rest_j + ((int64_t)b * kMaxSlots + slot) * 9;
@@ -271,6 +271,7 @@ __device__ __forceinline__ void exchange_f64(const Params& P, int t, const Repli
   for (int k = 0; k < cnt; ++k) {
     const int2 ent = __ldg(list + k);
     const int64_t j = gi + ent.x;
+    if (!LLG_IN_RANGE(P, j, R.offset, R.offset + R.n)) continue;
     const double sj[3] = {__ldg(S.x + j), __ldg(S.y + j), __ldg(S.z + j)};
     const double* J = E.J + (int64_t)ent.y * 9;
     const unsigned mask = __ldg(E.mask + ent.y);

@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(kBlock) observe_kernel(const __grid_constant__
         for (int k = 0; k < cnt; ++k) {
           const int2 ent = list[k];
           double sj[3];
+          if (!LLG_IN_RANGE(P, gi + ent.x, R.offset, R.offset + R.n)) continue;
           load3(s, P.npad, gi + ent.x, sj);
           const double* J = P.ex64[x].J + (int64_t)ent.y * 9;
           for (int m = 0; m < 3; ++m) f[m] += J[3 * m] * sj[0] + J[3 * m + 1] * sj[1] + J[3 * m + 2] * sj[2];

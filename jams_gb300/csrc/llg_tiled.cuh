@@ -579,15 +579,17 @@ __device__ __forceinline__ void plan_fetch(const View& V, int y0, int z0, int ti
 }
 
 template <class F, int TZ, int TY, int RPT>
-__device__ __forceinline__ void fetch_plane(const View& V, const float* __restrict__ s, int64_t npad, int x,
-                                            const FetchPlan<F, TZ, TY, RPT>& fp, PlaneRegs<F, TZ, TY, RPT>& pr) {
+__device__ __forceinline__ void fetch_plane(const Params& P, const View& V, const float* __restrict__ s,
+                                            int64_t npad, int x, const FetchPlan<F, TZ, TY, RPT>& fp,
+                                            PlaneRegs<F, TZ, TY, RPT>& pr) {
   using G = Geo<F, TZ, TY, RPT>;
   bool xvalid = true;
   const int gx = wrap_sel(x, V.L[0], V.per[0], xvalid);
   const float* sx = s + V.offset + gx * V.st[0];
 #pragma unroll
   for (int q = 0; q < G::PER_THREAD; ++q) {
-    const bool valid = xvalid && fp.idx[q] >= 0;
+    const bool valid = xvalid && fp.idx[q] >= 0 &&
+                       LLG_IN_RANGE(P, (int64_t)gx * V.st[0] + fp.idx[q], 0, (int64_t)V.L[0] * V.st[0]);
     const int i = fp.idx[q];
     pr.v[q][0] = valid ? __ldg(sx + i) : 0.f;
     pr.v[q][1] = valid ? __ldg(sx + npad + i) : 0.f;
@@ -596,13 +598,14 @@ __device__ __forceinline__ void fetch_plane(const View& V, const float* __restri
 }
 
 template <class F, int TZ, int TY, int RPT>
-__device__ __forceinline__ void store_plane(float4* ring, int x, const FetchPlan<F, TZ, TY, RPT>& fp,
+__device__ __forceinline__ void store_plane(const Params& P, float4* ring, int x, const FetchPlan<F, TZ, TY, RPT>& fp,
                                             const PlaneRegs<F, TZ, TY, RPT>& pr) {
   using G = Geo<F, TZ, TY, RPT>;
   float4* slot = ring + (x & 3) * G::PLANE;
 #pragma unroll
   for (int q = 0; q < G::PER_THREAD; ++q)
-    if (fp.dst[q] >= 0) slot[fp.dst[q]] = make_float4(pr.v[q][0], pr.v[q][1], pr.v[q][2], 0.f);
+    if (fp.dst[q] >= 0 && LLG_IN_RANGE(P, fp.dst[q], 0, G::PLANE))
+      slot[fp.dst[q]] = make_float4(pr.v[q][0], pr.v[q][1], pr.v[q][2], 0.f);
 }
 
 }  // namespace
@@ -652,6 +655,9 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     const int y = y0 + ty + r;
     active[r] = y < V.L[1] && z < V.L[2];
     own[r] = (ty + r + F::RY) * G::PZ + (tz + F::RZ);
+    // the stencil offsets are compile-time; they stay inside the ring slot
+    // when the thread's own cell does
+    if (!LLG_IN_RANGE(P, own[r], F::RY * G::PZ + F::RZ, (TY + F::RY) * G::PZ)) active[r] = false;
     yz[r] = y * V.st[1] + z * V.st[2] + b;
   }
   const float* gather_src = STAGE == 0 ? s0 : sin;
@@ -687,11 +693,11 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     PlaneRegs<F, TZ, TY, RPT> pr;
 #pragma unroll
     for (int d = -1; d <= 1; ++d) {
-      fetch_plane<F, TZ, TY, RPT>(V, gather_src, P.npad, x0 + d, fp, pr);
-      store_plane<F, TZ, TY, RPT>(ring0, x0 + d, fp, pr);
+      fetch_plane<F, TZ, TY, RPT>(P, V, gather_src, P.npad, x0 + d, fp, pr);
+      store_plane<F, TZ, TY, RPT>(P, ring0, x0 + d, fp, pr);
       if (NR == 2) {
-        fetch_plane<F, TZ, TY, RPT>(V, s0, P.npad, x0 + d, fp, pr);
-        store_plane<F, TZ, TY, RPT>(ring1, x0 + d, fp, pr);
+        fetch_plane<F, TZ, TY, RPT>(P, V, s0, P.npad, x0 + d, fp, pr);
+        store_plane<F, TZ, TY, RPT>(P, ring1, x0 + d, fp, pr);
       }
     }
   }
@@ -713,8 +719,8 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     const bool more = x + 1 < xe;
     PlaneRegs<F, TZ, TY, RPT> pf0, pf1;
     if (more) {
-      fetch_plane<F, TZ, TY, RPT>(V, gather_src, P.npad, x + 2, fp, pf0);
-      if (NR == 2) fetch_plane<F, TZ, TY, RPT>(V, s0, P.npad, x + 2, fp, pf1);
+      fetch_plane<F, TZ, TY, RPT>(P, V, gather_src, P.npad, x + 2, fp, pf0);
+      if (NR == 2) fetch_plane<F, TZ, TY, RPT>(P, V, s0, P.npad, x + 2, fp, pf1);
     }
     // one row: skipped outside the lattice; two rows: both computed (rows
     // outside the lattice see zeros in the ring), their loads and stores
@@ -729,7 +735,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
 #pragma unroll
       for (int r = 0; r < RPT; ++r) {
         const int i = x * V.st[0] + yz[r];   // spin index in the replica
-        const bool ld = RPT == 1 || active[r];
+        const bool ld = (RPT == 1 || active[r]) && LLG_IN_RANGE(P, i, 0, (int64_t)V.L[0] * V.st[0]);
         ir[r] = i;
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
@@ -763,7 +769,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
 #pragma unroll
       for (int r = 0; r < RPT; ++r) {
         const int i = ir[r];
-        const bool st = RPT == 1 || active[r];
+        const bool st = (RPT == 1 || active[r]) && LLG_IN_RANGE(P, i, 0, (int64_t)V.L[0] * V.st[0]);
         float h[3], s[3], k[3];
         field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own[r], cy0[r], h, s, has_dip, dip[r]);
         llg_rhs_t(L, s, h, w[r], k);
@@ -836,8 +842,8 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
       }
     }
     if (more) {
-      store_plane<F, TZ, TY, RPT>(ring0, x + 2, fp, pf0);
-      if (NR == 2) store_plane<F, TZ, TY, RPT>(ring1, x + 2, fp, pf1);
+      store_plane<F, TZ, TY, RPT>(P, ring0, x + 2, fp, pf0);
+      if (NR == 2) store_plane<F, TZ, TY, RPT>(P, ring1, x + 2, fp, pf1);
     }
     __syncthreads();
   }

@@ -26,6 +26,7 @@ RK4 = 1
 ERRORS = {
     -1: "LLG_ERR_BAD_DESC", -2: "LLG_ERR_OOM", -3: "LLG_ERR_CUDA", -4: "LLG_ERR_TIMEOUT",
     -5: "LLG_ERR_NONFINITE", -6: "LLG_ERR_NO_DEVICE", -7: "LLG_ERR_UNSUPPORTED", -8: "LLG_ERR_IO",
+    -9: "LLG_ERR_BOUNDS",
 }
 
 EXPORTED = [
@@ -80,16 +81,18 @@ class LlgDesc(ctypes.Structure):
     ]
 
 
-_lib = None
+_libs = {}
+LIB_PATH_CHECKED = os.path.join(HERE, "_build_checked", "libjams_llg.so")
 
 
-def lib():
-    """Loads libjams_llg.so (raises if it has not been built)."""
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise RuntimeError("libjams_llg.so is not built: run jams_gb300.build.build() (%s)" % LIB_PATH)
-        L = ctypes.CDLL(LIB_PATH)
+def lib(checked: bool = False):
+    """Loads libjams_llg.so (raises if it has not been built); checked=True:
+    the bounds-checked build (jams_gb300.build.build(checked=True))."""
+    path = LIB_PATH_CHECKED if checked else LIB_PATH
+    if path not in _libs:
+        if not os.path.exists(path):
+            raise RuntimeError("libjams_llg.so is not built: run jams_gb300.build.build() (%s)" % path)
+        L = ctypes.CDLL(path)
         vp, i32, i64, dp = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)
         L.llg_create.argtypes = [ctypes.POINTER(LlgDesc), ctypes.POINTER(vp)]
         L.llg_destroy.argtypes = [vp]
@@ -131,8 +134,8 @@ def lib():
             getattr(L, f).argtypes = [vp, i32, cp]
         for f in ("llg_save_checkpoint", "llg_load_checkpoint"):
             getattr(L, f).argtypes = [vp, cp]
-        _lib = L
-    return _lib
+        _libs[path] = L
+    return _libs[path]
 
 
 def _dp(a):
@@ -264,8 +267,8 @@ class Solver:
     its Hamiltonian terms fused into the stage kernels."""
 
     def __init__(self, workload: W.Workload, precision: int = FP32C, device: int = 0,
-                 steps_per_graph: int = 100, rk4_normalise_stages: bool = False):
-        self.L = lib()
+                 steps_per_graph: int = 100, rk4_normalise_stages: bool = False, checked: bool = False):
+        self.L = lib(checked)
         self.workload = workload
         m = workload.model
         d, self._keep = build_desc(workload, precision, device, steps_per_graph, rk4_normalise_stages)
