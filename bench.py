@@ -130,6 +130,7 @@ def parse(argv=None):
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-accuracy", action="store_true", help="skip the FP32C-vs-FP64 accuracy check")
     p.add_argument("--ref-gpu", default="auto", choices=["auto", "on", "off"],
                    help="time the restated reference GPU path (baseline/refgpu.cu) on replica 0: auto = single-replica "
                         "Heun workloads up to 4.2 M spins")
@@ -335,6 +336,41 @@ def tiled_stem(name: str):
         return None
     args = [a.strip() for a in name[name.index("<") + 1:name.rindex(">")].split(",")]
     return tuple(args[:3] + [args[4] if len(args) == 7 else args[3]])
+
+
+def accuracy_vs_fp64(w, steps=1000, cap=32):
+    """max |dS|, d|M| and dE of the FP32C form against the FP64 form (which
+    equals the oracle, and through it the reference's CPU solver, bit for
+    bit) after `steps` T = 0 steps.  The workload's Hamiltonian and integrator on
+    replica 0 with at most `cap` cells per axis and a random start."""
+    import copy
+
+    from jams_gb300 import llg
+
+    w2 = copy.deepcopy(w)
+    r0 = w2.replicas[0]
+    r0.L = tuple(min(int(l), cap) for l in r0.L)
+    r0.temperature = 0.0
+    w2.replicas = [r0]
+    w2.start = "random"
+    s0 = W.initial_state(w2, 0)
+    out = {}
+    for name, prec in (("fp64", llg.FP64), ("fp32c", llg.FP32C)):
+        sol = llg.Solver(w2, precision=prec)
+        sol.set_state(s0)
+        sol.step(steps)
+        m4, e = sol.observables(0)
+        out[name] = (sol.get_state(0), m4[3], e)
+        sol.close()
+    (a, ma, ea), (b, mb, eb) = out["fp64"], out["fp32c"]
+    return {"max_dS": float(np.abs(a - b).max()), "d_abs_M": float(abs(ma - mb)),
+            "max_dE_rel": float(np.max(np.abs(ea - eb) / np.maximum(np.abs(ea), 1e-30))),
+            "steps": steps, "T": 0.0, "spins": int(len(s0)),
+            "sample": "replica 0 of the workload's model at %s cells, random start, FP32C vs FP64 (the FP64 form "
+                      "equals the oracle %s)" % ("x".join(str(l) for l in r0.L),
+                                                 "within FFT rounding" if any(t.kind == W.TERM_DIPOLE
+                                                                              for t in w.model.terms)
+                                                 else "bit for bit")}
 
 
 def reference_gpu_rate(args, w):
@@ -568,8 +604,11 @@ def main():
                          % (n_steps, n_rep)}
 
     ref_gpu = None
+    accuracy = None
     if rank == 0 and world == 1:
         ref_gpu = reference_gpu_rate(args, w)
+        if args.precision == "fp32c" and not args.no_accuracy:
+            accuracy = accuracy_vs_fp64(w)
 
     # |M| of every replica of every rank at the end of the run
     mags = [float(sol.observables(r)[0][3]) for r in range(len(w.replicas))]
@@ -587,7 +626,7 @@ def main():
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         "steady_state_graph": steady, "wall_s_timed_region": t_wall,
         "final_abs_m": {"mean": float(np.mean([m for r in mags for m in r])), "ranks": len(mags)},
-        "dipole": dipole, "reference_gpu": ref_gpu,
+        "dipole": dipole, "reference_gpu": ref_gpu, "accuracy": accuracy,
     }
     if rank == 0:
         print(json.dumps(line))
