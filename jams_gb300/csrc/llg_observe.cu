@@ -5,7 +5,7 @@
 // src/jams/monitors/topological_charge_geometrical_def.cc:159-181); here each
 // 256-spin tile reduces in shared memory in a fixed tree order and the host
 // adds the per-tile partials in tile order, so results do not depend on
-// scheduling.
+// scheduling: a shuffle tree inside each warp, then the warps in order.
 #include <cmath>
 
 #include "llg_kernels.h"
@@ -23,6 +23,21 @@ __device__ __forceinline__ void load3(const Real* base, int64_t npad, int64_t j,
 
 __device__ __forceinline__ int cls_total(const ReplicaDev& R) { return R.ncls[0] * R.ncls[1] * R.ncls[2]; }
 
+// sum over the block in a fixed order: a shuffle tree inside each warp, then
+// the warps' sums in warp order by thread 0 (the only thread that gets the
+// total); every thread of the block calls it
+__device__ __forceinline__ double block_sum(double v, double* warp_sums) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double total = 0.0;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < kBlock / 32; ++k) total += warp_sums[k];
+  __syncthreads();
+  return total;
+}
+
 __device__ __forceinline__ int axis_class_o(int c, int L, int R, int ncls) {
   if (ncls == L) return c;
   if (c < R) return c;
@@ -38,7 +53,7 @@ template <typename Real>
 __global__ void __launch_bounds__(kBlock) observe_kernel(const __grid_constant__ Params P,
                                                          const Real* __restrict__ s, int first_tile,
                                                          double* __restrict__ partials, int nq) {
-  __shared__ double red[kBlock];
+  __shared__ double red[kBlock / 32];
   const int tile_index = first_tile + blockIdx.x;
   const int2 tile = P.tiles[tile_index];
   const ReplicaDev& R = P.rep[tile.x];
@@ -128,14 +143,8 @@ __global__ void __launch_bounds__(kBlock) observe_kernel(const __grid_constant__
     }
   }
   for (int k = 0; k < nq; ++k) {
-    red[threadIdx.x] = q[k];
-    __syncthreads();
-    for (int w = kBlock / 2; w > 0; w >>= 1) {
-      if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) partials[(int64_t)blockIdx.x * nq + k] = red[0];
-    __syncthreads();
+    const double total = block_sum(q[k], red);
+    if (threadIdx.x == 0) partials[(int64_t)blockIdx.x * nq + k] = total;
   }
 }
 
@@ -153,7 +162,7 @@ __device__ __forceinline__ double solid_angle(const double* a, const double* b, 
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) charge_kernel(const __grid_constant__ Params P, const Real* __restrict__ s,
                                                         int replica, double* __restrict__ partials) {
-  __shared__ double red[kBlock];
+  __shared__ double red[kBlock / 32];
   const ReplicaDev& R = P.rep[replica];
   const int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
   const int L1 = R.L[0], L2 = R.L[1];
@@ -169,13 +178,8 @@ __global__ void __launch_bounds__(kBlock) charge_kernel(const __grid_constant__ 
     load3(s, P.npad, R.offset + (int64_t)p1 * L2 + p2, s11);
     qsum = solid_angle(s00, s10, s01) + solid_angle(s10, s11, s01);
   }
-  red[threadIdx.x] = qsum;
-  __syncthreads();
-  for (int w = kBlock / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
+  const double total = block_sum(qsum, red);
+  if (threadIdx.x == 0) partials[blockIdx.x] = total;
 }
 
 }  // namespace
