@@ -588,6 +588,22 @@ def main():
                 dst.copy_(src)
             torch.cuda.synchronize()
             link[name] = n_spins * 24 * 20 / (time.perf_counter() - t1) / 1e9
+        # both directions at once (two streams): what each direction keeps
+        # when the link is shared; the set / step / get loop cannot use it,
+        # since each step's input is the previous step's result
+        host2 = torch.empty_like(host, pin_memory=True)
+        dev2 = torch.empty_like(dev)
+        s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(20):
+            with torch.cuda.stream(s_in):
+                dev.copy_(host, non_blocking=True)
+            with torch.cuda.stream(s_out):
+                host2.copy_(dev2, non_blocking=True)
+        torch.cuda.synchronize()
+        link["duplex_each_way"] = n_spins * 24 * 20 / (time.perf_counter() - t1) / 1e9
+        del host2, dev2
         floor_s = n_spins * 24 * (1.0 / link["h2d"] + 1.0 / link["d2h"]) / 1e9 + ms_per_step * 1e-3
         e2e = {"value": job_rate(n_spins, world, ke, dt), "unit": "spin-steps/s", "h2d_bytes_per_step": n_spins * 24,
                "d2h_bytes_per_step": n_spins * 24, "steps": ke,
