@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -708,8 +709,40 @@ int build(llg_handle* h, const llg_desc* d) {
     n_uni += d->terms[t].kind == LLG_TERM_UNIAXIAL;
     n_cub += d->terms[t].kind == LLG_TERM_CUBIC;
   }
-  if (!h->fp64 && ex.size() == 1 && n_uni <= 1 && n_cub <= 1) {
-    const llg_term& T = d->terms[ex[0].term];
+  // FP32C: several exchange terms (isotropic exchange and DMI given as
+  // separate modules, say) are summed per (site, translation, partner) into
+  // one template, in term order and in FP64, which then has to match a
+  // stencil family.  The reference sums their fields term by term
+  // (src/jams/core/solver.cc:43-57); the FP32C form rounds once.
+  std::vector<int32_t> m_bi, m_bj, m_T;
+  std::vector<double> m_J;
+  llg_term merged{};
+  if (!h->fp64 && ex.size() > 1) {
+    std::map<std::array<int32_t, 5>, size_t> at;
+    for (const ExchangeHost& X : ex) {
+      const llg_term& t = d->terms[X.term];
+      for (int e = 0; e < t.n_int; ++e) {
+        const std::array<int32_t, 5> key = {t.bi[e], t.T[3 * e], t.T[3 * e + 1], t.T[3 * e + 2], t.bj[e]};
+        auto it = at.find(key);
+        if (it == at.end()) {
+          it = at.emplace(key, m_bi.size()).first;
+          m_bi.push_back(key[0]);
+          m_T.insert(m_T.end(), {key[1], key[2], key[3]});
+          m_bj.push_back(key[4]);
+          m_J.insert(m_J.end(), 9, 0.0);
+        }
+        for (int a = 0; a < 9; ++a) m_J[9 * it->second + a] += t.J[9 * e + a];
+      }
+    }
+    merged.kind = LLG_TERM_EXCHANGE;
+    merged.n_int = (int32_t)m_bi.size();
+    merged.bi = m_bi.data();
+    merged.bj = m_bj.data();
+    merged.T = m_T.data();
+    merged.J = m_J.data();
+  }
+  if (!h->fp64 && !ex.empty() && n_uni <= 1 && n_cub <= 1) {
+    const llg_term& T = ex.size() == 1 ? d->terms[ex[0].term] : merged;
     h->family = find_family(d, T, h->TP);
     if (h->family != kFamNone) {
       h->tiled = true;

@@ -19,6 +19,7 @@ Unit conventions follow the reference:
 """
 from __future__ import annotations
 
+import copy
 import dataclasses
 import itertools
 import math
@@ -386,6 +387,34 @@ def triangular_dmi_field_sweep(L=2048, n_fields=16, B_max=2.0, steps=5000, T=5.0
     return Workload(name=f"tri{Ls[0]}_dmi_x{n_fields}", model=model, replicas=reps, steps=steps,
                     seed=seed, start="random",
                     description="triangular monolayer J1=1 D=0.3 meV, K1=0.2 meV, RK4 a=0.3, B_z sweep")
+
+
+def split_exchange(w: Workload, offdiag: float = 0.0) -> Workload:
+    """The same workload with its first term (an exchange template) given as
+    two exchange terms of half strength each, as a config with two exchange
+    modules would give it.  With offdiag != 0 the second term also carries a
+    symmetric off-diagonal tensor part J_xy = J_yx = offdiag * J_xx on one
+    pair: its first entry and the reverse entry (partner and site swapped,
+    translation negated), so the coupling stays reciprocal.  The lattice
+    families' stencils take isotropic J only (the triangular family aside),
+    so the FP32C form then runs the gather kernels; without it the two terms
+    are summed into one stencil."""
+    w2 = copy.deepcopy(w)
+    ex = w2.model.terms[0]
+    assert ex.kind == TERM_EXCHANGE
+    Jb = ex.J * 0.5
+    if offdiag:
+        Jb = Jb.copy()
+        rev = [e for e in range(len(ex.bi)) if ex.bi[e] == ex.bj[0] and ex.bj[e] == ex.bi[0]
+               and np.array_equal(ex.T[e], -ex.T[0])]
+        for e in [0] + rev[:1]:
+            Jb[e, 0, 1] += offdiag * Jb[e, 0, 0]
+            Jb[e, 1, 0] += offdiag * Jb[e, 0, 0]
+    w2.model.terms = [Term(kind=ex.kind, bi=ex.bi, bj=ex.bj, T=ex.T, J=ex.J * 0.5, name="exchange-a"),
+                      Term(kind=ex.kind, bi=ex.bi, bj=ex.bj, T=ex.T, J=Jb, name="exchange-b")] + \
+        w2.model.terms[1:]
+    w2.name += "_split" if not offdiag else "_generic"
+    return w2
 
 
 # --------------------------------------------------------------------------

@@ -1,10 +1,9 @@
-"""The bounds-checked build (compiled with LLG_BOUNDS_CHECK, the stand-in for
-a memory checker, which is not available on this machine). Every gathered neighbour,
+"""The bounds-checked build (compiled with LLG_BOUNDS_CHECK, in place of a
+memory checker). Every gathered neighbour,
 fetched plane, ring slot and written spin index is checked against its array.
 A miss would set a status bit that llg_synchronize reports as LLG_ERR_BOUNDS,
 and the access would be skipped. Across the kernel forms it must run clean
 and give the same spins, fields and energies as the normal build, bit for bit."""
-import copy
 
 import numpy as np
 import pytest
@@ -24,11 +23,8 @@ def checked(llg):
 
 
 def _generic(w):
-    w = copy.deepcopy(w)
-    ex = w.model.terms[0]
-    w.model.terms = [W.Term(kind=ex.kind, bi=ex.bi, bj=ex.bj, T=ex.T, J=ex.J * 0.5),
-                     W.Term(kind=ex.kind, bi=ex.bi, bj=ex.bj, T=ex.T, J=ex.J * 0.5)] + w.model.terms[1:]
-    return w
+    # two exchange terms, one with an off-diagonal part: the gather kernels
+    return W.split_exchange(w, offdiag=0.05)
 
 
 def _open_sc():

@@ -230,16 +230,27 @@ def test_tiled_families_selected(llg):
 
 
 def _split_exchange(w):
-    """The same Hamiltonian with the exchange split into two half-strength
-    terms: no tiled family applies (gather kernels)."""
-    import copy
+    """The same Hamiltonian with the exchange as two terms, the second with a
+    small symmetric off-diagonal part: no tiled family applies (gather
+    kernels)."""
+    return W.split_exchange(w, offdiag=0.05)
 
-    w2 = copy.deepcopy(w)
-    ex = w2.model.terms[0]
-    half = W.Term(kind=ex.kind, bi=ex.bi, bj=ex.bj, T=ex.T, J=ex.J * 0.5, name="exchange-a")
-    w2.model.terms = [half, W.Term(kind=ex.kind, bi=ex.bi, bj=ex.bj, T=ex.T, J=ex.J * 0.5, name="exchange-b")] + \
-        w2.model.terms[1:]
-    return w2
+
+def test_exchange_terms_are_summed_into_one_stencil(llg):
+    """Two half-strength exchange terms run the tiled kernels of the
+    family; their sum is exact, so the FP32C states equal the single-term
+    run's bit for bit."""
+    w = W.bcc_three_shell(L=8, T=300.0, start="random")
+    w2 = W.split_exchange(w)
+    s0 = W.initial_state(w, 0)
+    out = []
+    for m in (w, w2):
+        s = solver(llg, m, llg.FP32C)
+        assert s.kernel_info()["family"] == "bcc3"
+        s.set_state(s0)
+        s.step(50)
+        out.append(s.get_state(0))
+    assert np.array_equal(out[0], out[1])
 
 
 def test_fp32c_gather_kernels_within_bound(llg, oracle):

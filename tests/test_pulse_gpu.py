@@ -87,13 +87,9 @@ def test_fp64_pulse_table_chunks(llg, oracle):
 
 
 def _split_exchange(w):
-    """The exchange as two half-strength terms: the gather kernels run."""
-    w2 = copy.deepcopy(w)
-    ex = w2.model.terms[0]
-    w2.model.terms = [W.Term(kind=ex.kind, bi=ex.bi, bj=ex.bj, T=ex.T, J=ex.J * 0.5, name="exchange-a"),
-                      W.Term(kind=ex.kind, bi=ex.bi, bj=ex.bj, T=ex.T, J=ex.J * 0.5, name="exchange-b")] + \
-        w2.model.terms[1:]
-    return w2
+    """The exchange as two terms, the second with a small symmetric
+    off-diagonal part: the gather kernels run."""
+    return W.split_exchange(w, offdiag=0.05)
 
 
 @pytest.mark.parametrize("name", sorted(pulse_cases().keys()))
