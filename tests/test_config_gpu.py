@@ -40,3 +40,26 @@ def test_config_rk4_triangular(llg, oracle):
     ref = oracle.OracleSim(w).run(s0, 30)
     s.step(30)
     assert np.array_equal(s.get_state(0), ref)
+
+
+def test_two_exchange_modules_run_the_tiled_kernels(llg):
+    """A config with the three bcc shells split over two exchange modules:
+    FP32C sums them into the three-shell stencil, so the run equals the
+    one-module config's bit for bit, and the two terms' exchange energies add
+    up to the one term's."""
+    one = C.bcc_three_shell(L=6, T=300.0, steps=20, spin='"random"')
+    shell1 = '      ("Fe", "Fe", [0.5, 0.5, 0.5], 2.0),    // shell 1: 8 at a<111>/2\n'
+    assert one.count(shell1) == 1
+    two = one.replace(shell1, '      ("Fe", "Fe", [0.5, 0.5, 0.5], 2.0)\n    );\n  },\n  {\n'
+                              '    module = "exchange";\n    energy_units = "meV";\n    interactions = (\n')
+    a = llg.Solver.from_config(one, precision=llg.FP32C)
+    b = llg.Solver.from_config(two, precision=llg.FP32C)
+    assert a.n_terms + 1 == b.n_terms
+    assert a.kernel_info()["family"] == b.kernel_info()["family"] == "bcc3"
+    assert np.array_equal(a.get_state(0), b.get_state(0))
+    a.step(20)
+    b.step(20)
+    assert np.array_equal(a.get_state(0), b.get_state(0))
+    ea, eb = a.observables(0)[1], b.observables(0)[1]
+    np.testing.assert_allclose(eb[0] + eb[1], ea[0], rtol=1e-12)
+    np.testing.assert_allclose(eb[2:], ea[1:], rtol=1e-12)
