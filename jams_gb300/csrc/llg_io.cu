@@ -18,10 +18,12 @@
 //    every number read in file order.
 //
 // Host code only; no device work.
+#include <algorithm>
 #include <cerrno>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <fstream>
 #include <sstream>
 #include <string>
@@ -341,9 +343,23 @@ struct File {
   int so = 8, sl = 8;  // size of offsets / lengths
   uint64_t base = 0;
   std::string err;
+  // a field read outside the file (a corrupt offset or length): the read
+  // gives 0 and the parse fails once the flag is seen
+  mutable bool oob = false;
 
   bool in(uint64_t at, uint64_t n) const { return at <= d.size() && n <= d.size() - at; }
+  uint8_t u8(uint64_t at) const {
+    if (at >= d.size()) {
+      oob = true;
+      return 0;
+    }
+    return d[at];
+  }
   uint64_t uint(uint64_t at, int n) const {
+    if (!in(at, (uint64_t)n)) {
+      oob = true;
+      return 0;
+    }
     uint64_t v = 0;
     for (int i = 0; i < n; ++i) v |= (uint64_t)d[at + i] << (8 * i);
     return v;
@@ -420,6 +436,7 @@ bool header_messages(File& F, uint64_t at, std::vector<Message>& msgs) {
       p = data + size;
     }
   }
+  if (F.oob) return F.fail("object header field outside the file");
   return true;
 }
 
@@ -438,6 +455,7 @@ bool find_in_symbol_table(File& F, uint64_t btree, uint64_t heap, const std::str
   for (int c = 0; c < used; ++c) {
     const uint64_t child = F.addr(p + F.sl);
     p += F.sl + F.so;
+    if (F.oob) return F.fail("group B-tree entry outside the file");
     if (level > 0) {
       if (find_in_symbol_table(F, child, heap - F.base, name, header, depth + 1)) return true;
       if (!F.err.empty()) return false;
@@ -453,7 +471,8 @@ bool find_in_symbol_table(File& F, uint64_t btree, uint64_t heap, const std::str
       const uint64_t noff = F.uint(ep, F.so);
       if (noff >= heap_size || !F.in(heap_data + noff, 1)) return F.fail("bad link name offset");
       const char* nm = (const char*)&F.d[heap_data + noff];
-      const size_t maxlen = heap_size - noff;
+      // the name ends within the heap and within the file
+      const size_t maxlen = (size_t)std::min<uint64_t>(heap_size - noff, F.d.size() - (heap_data + noff));
       if (strnlen(nm, maxlen) == name.size() && std::memcmp(nm, name.data(), name.size()) == 0) {
         header = F.addr(ep + F.so);
         return true;
@@ -473,18 +492,19 @@ bool find_link(File& F, uint64_t group_header, const std::string& name, uint64_t
     if (m.type == 0x02) return F.fail("groups with dense link storage are not supported");
     if (m.type == 0x06) {  // link message
       uint64_t p = m.at;
-      const int flags = F.d[p + 1];
+      const int flags = F.u8(p + 1);
       p += 2;
       int ltype = 0;
-      if (flags & 0x08) ltype = F.d[p++];
+      if (flags & 0x08) ltype = F.u8(p++);
       if (flags & 0x04) p += 8;  // creation order
       if (flags & 0x10) p += 1;  // character set
       const int lsz = 1 << (flags & 3);
       const uint64_t nlen = F.uint(p, lsz);
       p += lsz;
-      if (p + nlen > m.at + m.size) return F.fail("bad link message");
+      if (F.oob || p + nlen > m.at + m.size) return F.fail("bad link message");
       if (ltype == 0 && nlen == name.size() && std::memcmp(&F.d[p], name.data(), nlen) == 0) {
         header = F.addr(p + nlen);
+        if (F.oob) return F.fail("bad link message");
         return true;
       }
     }
@@ -572,17 +592,17 @@ int read_h5(const std::string& path, const std::string& dataset, std::vector<dou
   for (const Message& m : msgs) {
     const uint64_t p = m.at;
     if (m.type == 0x01) {  // dataspace
-      const int v = F.d[p], rank = F.d[p + 1];
+      const int v = F.u8(p), rank = F.u8(p + 1);
       const uint64_t q = p + (v == 1 ? 8 : 4);
       for (int r = 0; r < rank; ++r) dims.push_back(F.uint(q + (uint64_t)r * F.sl, F.sl));
     } else if (m.type == 0x03) {  // datatype
-      tfloat = (F.d[p] & 0x0f) == 1;
-      tle = (F.d[p + 1] & 0x41) == 0;
+      tfloat = (F.u8(p) & 0x0f) == 1;
+      tle = (F.u8(p + 1) & 0x41) == 0;
       tsize = (int)F.uint(p + 4, 4);
     } else if (m.type == 0x08) {  // layout
-      const int v = F.d[p];
+      const int v = F.u8(p);
       if (v == 3 || v == 4) {
-        layout = F.d[p + 1];
+        layout = F.u8(p + 1);
         if (layout == 1) {
           data_at = F.addr(p + 2);
           data_size = F.uint(p + 2 + F.so, F.sl);
@@ -591,8 +611,8 @@ int read_h5(const std::string& path, const std::string& dataset, std::vector<dou
           data_at = p + 4 - F.base;
         }
       } else if (v == 1 || v == 2) {
-        const int rank = F.d[p + 1];
-        layout = F.d[p + 2];
+        const int rank = F.u8(p + 1);
+        layout = F.u8(p + 2);
         if (layout == 1) {
           data_at = F.addr(p + 8);
           uint64_t n = 1;
@@ -604,6 +624,10 @@ int read_h5(const std::string& path, const std::string& dataset, std::vector<dou
       err = "dataset /" + dataset + " uses a filter pipeline (compression): not supported";
       return 1;
     }
+  }
+  if (F.oob) {
+    err = "dataset /" + dataset + ": a header field lies outside the file";
+    return 1;
   }
   if (layout != 0 && layout != 1) {
     err = "dataset /" + dataset + " is chunked or virtual: only contiguous and compact datasets are supported";
@@ -617,10 +641,22 @@ int read_h5(const std::string& path, const std::string& dataset, std::vector<dou
     err = "dataset /" + dataset + " is not one- or two-dimensional";
     return 1;
   }
-  rows = (int64_t)dims[0];
-  cols = dims.size() == 2 ? (int64_t)dims[1] : 1;
-  const uint64_t n = (uint64_t)rows * (uint64_t)cols;
+  // extents below 2^40 and at most 2^34 values, so that neither the value
+  // count nor the byte count wraps; a dataset never written (no data
+  // address) reads as zeros, up to 2^24 values
+  const uint64_t d0 = dims[0], d1 = dims.size() == 2 ? dims[1] : 1;
+  if (d0 >= (1ull << 40) || d1 >= (1ull << 40) || (d1 != 0 && d0 > (1ull << 34) / d1)) {
+    err = "dataset /" + dataset + " has extents too large for this reader";
+    return 1;
+  }
+  rows = (int64_t)d0;
+  cols = (int64_t)d1;
+  const uint64_t n = d0 * d1;
   if (data_at == kUndef) {  // never written: fill value 0
+    if (n > (1ull << 24)) {
+      err = "dataset /" + dataset + " was never written and is too large to read as zeros";
+      return 1;
+    }
     out.assign(n, 0.0);
     return 0;
   }
@@ -657,11 +693,18 @@ int write_array(const std::string& path, const std::vector<Dataset>& sets, std::
 
 int read_array(const std::string& path, const char* dataset, std::vector<double>& out, int64_t& rows,
                int64_t& cols, std::string& err) {
-  if (extension(path) == "h5") return read_h5(path, strip_slash(dataset), out, rows, cols, err);
-  const int rc = read_text(path, out, err);
-  rows = (int64_t)out.size();
-  cols = 1;
-  return rc;
+  // the callers are C entry points: an allocation failure becomes an error
+  try {
+    if (extension(path) == "h5") return read_h5(path, strip_slash(dataset), out, rows, cols, err);
+    const int rc = read_text(path, out, err);
+    rows = (int64_t)out.size();
+    cols = 1;
+    return rc;
+  } catch (const std::exception& e) {
+    out.clear();
+    err = std::string("reading ") + path + ": " + e.what();
+    return 1;
+  }
 }
 
 std::string dataset_name(const char* name) { return strip_slash(name); }

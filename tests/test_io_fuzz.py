@@ -1,0 +1,86 @@
+"""Corrupted spin files: the HDF5 and text readers (llg_io.cu) must answer
+every file with a status code or with the values, never by crashing or
+by writing past the caller's array.  Valid files written by
+llg_write_array_file are corrupted by seeded byte flips, zeroed or
+saturated spans, truncations and repeated spans, then read twice (sizes
+first, then the values into an array with a guard region).  The loop runs
+in a child process so that a crash fails the test; no GPU is needed."""
+import ast
+import os
+import subprocess
+import sys
+import textwrap
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+CHILD = textwrap.dedent(r'''
+    import ctypes, os, random, sys, tempfile
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    from jams_gb300 import llg
+
+    L = llg.lib()
+    rng = random.Random(SEED)
+    tmp = tempfile.mkdtemp()
+    bases = []
+    for name, a in (("spins.h5", np.random.default_rng(1).normal(size=(100, 3))),
+                    ("flat.h5", np.arange(37, dtype=np.float64)),
+                    ("empty.h5", np.zeros((0, 3))),
+                    ("spins.txt", np.random.default_rng(2).normal(size=(20, 3)))):
+        p = os.path.join(tmp, name)
+        llg.write_array_file(p, a)
+        bases.append((p, open(p, "rb").read()))
+
+    def corrupt(b):
+        b = bytearray(b)
+        for _ in range(rng.randint(1, 6)):
+            if not b:
+                break
+            i = rng.randrange(len(b))
+            k = rng.randint(1, 16)
+            op = rng.randrange(6)
+            if op == 0:
+                b[i] ^= 1 << rng.randrange(8)
+            elif op == 1:
+                b[i:i + k] = bytes(len(b[i:i + k]))
+            elif op == 2:
+                b[i:i + k] = b"\xff" * len(b[i:i + k])
+            elif op == 3:
+                del b[i:]
+            elif op == 4:
+                b[i:i] = b[i:i + k] * rng.randint(1, 3)
+            else:
+                b[i] = rng.randrange(256)
+        return bytes(b)
+
+    guard = 512
+    counts = {}
+    rows, cols = ctypes.c_int64(), ctypes.c_int64()
+    for it in range(N):
+        path, data = bases[it % len(bases)]
+        bad = os.path.join(tmp, "bad" + os.path.splitext(path)[1])
+        with open(bad, "wb") as f:
+            f.write(corrupt(data))
+        rc = L.llg_read_array_file(bad.encode(), b"/spins", None, 0, ctypes.byref(rows), ctypes.byref(cols))
+        if rc == 0:
+            n = rows.value * cols.value
+            assert rows.value >= 0 and cols.value >= 0 and n <= 1 << 24, (rows.value, cols.value)
+            out = np.full(n + guard, 7.0)
+            rc = L.llg_read_array_file(bad.encode(), b"/spins", out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                       n, ctypes.byref(rows), ctypes.byref(cols))
+            assert (out[n:] == 7.0).all(), "wrote past the array"
+        if rc != 0:
+            assert L.llg_last_error(None), "error without a message"
+        counts[rc] = counts.get(rc, 0) + 1
+    print("codes", sorted(counts.items()))
+''')
+
+
+def test_corrupted_spin_files_are_answered_with_a_status():
+    n = 20000
+    code = "ROOT = %r\nN = %d\nSEED = 20261204\n" % (ROOT, n) + CHILD
+    res = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, (res.returncode, res.stdout[-2000:], res.stderr[-4000:])
+    codes = dict(ast.literal_eval(res.stdout.strip().split("codes ", 1)[1]))
+    assert sum(codes.values()) == n
+    assert len(codes) > 1   # some corruptions are detected, some leave a readable file
