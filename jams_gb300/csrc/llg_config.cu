@@ -256,19 +256,21 @@ class Parser {
       }
       const bool is_hex = low.size() > 2 && (low.rfind("0x", 0) == 0);
       const bool is_float = !is_hex && low.find_first_of(".e") != std::string::npos;
-      char* end = nullptr;
+      // `end` points into the string parsed, so each branch checks it while
+      // that string is alive
       if (is_float) {
         n.type = Node::Float;
+        char* end = nullptr;
         n.f = strtod(tok.c_str(), &end);
+        if (!end || *end != '\0') fail("bad number '" + tok + "'");
       } else {
         std::string digits = tok;
         while (!digits.empty() && (digits.back() == 'L' || digits.back() == 'l')) digits.pop_back();
         n.type = Node::Int;
+        char* end = nullptr;
         n.i = strtoll(digits.c_str(), &end, 0);
-        if (end && *end == '\0') return;
-        tok = digits;
+        if (!end || *end != '\0') fail("bad number '" + digits + "'");
       }
-      if (!end || *end != '\0') fail("bad number '" + tok + "'");
     }
   }
 };
