@@ -44,6 +44,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <sstream>
@@ -521,6 +522,74 @@ struct Interaction {
   std::array<double, 9> J{};
 };
 
+// A line the interaction-file reader skips (src/jams/helpers/utils.h:115-126):
+// fewer than two non-blank characters, or the first of them '#', or the
+// first two "//".
+bool interaction_line_is_comment(const std::string& line) {
+  char c[2];
+  int n = 0;
+  for (char ch : line)
+    if (!std::isspace((unsigned char)ch)) {
+      c[n++] = ch;
+      if (n == 2) break;
+    }
+  return n < 2 || c[0] == '#' || (c[0] == '/' && c[1] == '/');
+}
+
+// exc_file (src/jams/hamiltonian/exchange.cc:117-131), read as
+// discover_interaction_file_format and interactions_from_file
+// (src/jams/core/interactions.cc:127-246): the first data line fixes the
+// layout for the whole file, 6 columns for a scalar J or 14 for a 3x3
+// tensor, and its first two tokens, both integers (KKR: 1-based basis
+// sites) or both names (JAMS: material names).  Each data line is read
+// token by token; a line that does not read is an error.
+std::vector<Interaction> interactions_from_file(const std::string& path, const Model& m, bool& kkr) {
+  std::ifstream f(path);
+  if (!f) throw CfgError("exchange: failed to open exc_file " + path);
+  std::vector<std::string> lines;
+  for (std::string line; std::getline(f, line);) lines.push_back(line);
+  int ncols = 0;
+  for (const std::string& line : lines) {
+    if (interaction_line_is_comment(line)) continue;
+    std::istringstream is(line);
+    std::vector<std::string> tok;
+    for (std::string t; is >> t;) tok.push_back(t);
+    if (tok.size() != 6 && tok.size() != 14) throw CfgError("interaction file has an incorrect number of columns");
+    auto is_int = [](const std::string& s) { return s.find_first_not_of("0123456789") == std::string::npos; };
+    if (is_int(tok[0]) != is_int(tok[1])) throw CfgError("failed to discover interaction file format");
+    kkr = is_int(tok[0]);
+    ncols = (int)tok.size();
+    break;
+  }
+  if (ncols == 0) throw CfgError("failed to discover interaction file format");
+  std::vector<Interaction> in;
+  for (size_t k = 0; k < lines.size(); ++k) {
+    if (interaction_line_is_comment(lines[k])) continue;
+    std::istringstream is(lines[k]);
+    Interaction I;
+    if (kkr) {
+      is >> I.bi >> I.bj;
+      --I.bi;
+      --I.bj;
+    } else {
+      is >> I.ti >> I.tj;
+    }
+    is >> I.r[0] >> I.r[1] >> I.r[2];
+    if (ncols == 6) {
+      double J = 0.0;
+      is >> J;
+      I.J = {J, 0, 0, 0, J, 0, 0, 0, J};
+    } else {
+      for (int a = 0; a < 9; ++a) is >> I.J[a];
+    }
+    if (is.fail()) throw CfgError("failed to read line " + std::to_string(k + 1) + " of interaction file " + path);
+    if (kkr && (I.bi < 0 || I.bi >= (int)m.basis.size() || I.bj < 0 || I.bj >= (int)m.basis.size()))
+      throw CfgError("interaction basis index out of range");
+    in.push_back(I);
+  }
+  return in;
+}
+
 void build_exchange(Model& m, const Node& h, Model::Term& out) {
   const double conv = energy_unit(h);
   bool symops = true;
@@ -534,13 +603,17 @@ void build_exchange(Model& m, const Node& h, Model::Term& out) {
   if (const Node* n = h.find("coordinate_format")) coord = n->str();
   coord = lower(coord);
   if (coord != "cartesian" && coord != "fractional") throw CfgError("Unknown coordinate format " + coord);
-  if (h.find("exc_file")) throw CfgError("exchange: exc_file is not supported, give the interactions inline");
-  const Node& list = h.at("interactions");
-  if (list.type != Node::List || list.size() == 0) throw CfgError("exchange settings must be a list");
+  std::vector<Interaction> in;
+  bool kkr = false;
+  // exc_file first, as the reference checks it first; else the inline list
+  const Node* file = h.find("exc_file");
+  const Node no_list;
+  if (file) in = interactions_from_file(file->str(), m, kkr);
+  const Node& list = file ? no_list : h.at("interactions");
+  if (!file && (list.type != Node::List || list.size() == 0)) throw CfgError("exchange settings must be a list");
 
   // interactions_from_settings (src/jams/core/interactions.cc:221-257)
-  std::vector<Interaction> in;
-  const bool kkr = list.at(0).at(0).is_number();
+  if (!file) kkr = list.at(0).at(0).is_number();
   for (size_t k = 0; k < list.size(); ++k) {
     const Node& e = list.at(k);
     Interaction I;

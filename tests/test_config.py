@@ -166,3 +166,60 @@ def test_duplicate_site_pair_is_rejected_at_create(llg):
     w = W.sc_ferromagnet(L=(2, 4, 4))
     with pytest.raises(llg.LLGError, match="Multiple interactions"):
         llg.Solver(w, precision=llg.FP64)
+
+
+_INLINE = '''    interactions = (
+      ("Fe", "Fe", [0.5, 0.5, 0.5], 2.0),    // shell 1: 8 at a<111>/2
+      ("Fe", "Fe", [1.0, 0.0, 0.0], 1.2),    // shell 2: 6 at a<100>
+      ("Fe", "Fe", [1.0, 1.0, 0.0], -0.1)    // shell 3: 12 at a<110>
+    );
+'''
+
+
+def _with_exc_file(path):
+    text = C.bcc_three_shell(L=6)
+    assert text.count(_INLINE) == 1
+    return text.replace(_INLINE, '    exc_file = "%s";\n' % path)
+
+
+def test_exc_file_jams_and_kkr_formats_equal_the_inline_list(llg, tmp_path):
+    """exc_file (src/jams/core/interactions.cc:127-246): material names or
+    1-based basis sites, a scalar J (6 columns) or a 3x3 tensor (14), '#',
+    '//' and short lines skipped.  Both files describe the model of the
+    inline list."""
+    ref = llg.describe_config(C.bcc_three_shell(L=6))["terms"][0]
+    jams = tmp_path / "jams.txt"
+    jams.write_text("# bcc, three shells (meV)\n\nFe Fe 0.5 0.5 0.5 2.0\n  // shell 2\nFe Fe 1.0 0.0 0.0 1.2\n"
+                    "x\nFe Fe 1.0 1.0 0.0 -0.1\n")
+    kkr = tmp_path / "kkr.txt"
+    rows = []
+    for (i, j, r, J) in ((1, 2, "0.5 0.5 0.5", 2.0), (2, 1, "-0.5 -0.5 -0.5", 2.0), (1, 1, "1.0 0.0 0.0", 1.2),
+                         (2, 2, "1.0 0.0 0.0", 1.2), (1, 1, "1.0 1.0 0.0", -0.1), (2, 2, "1.0 1.0 0.0", -0.1)):
+        rows.append("%d %d %s %s" % (i, j, r, " ".join(repr(J if a % 4 == 0 else 0.0) for a in range(9))))
+    kkr.write_text("// i j rx ry rz Jxx ... Jzz\n" + "\n".join(rows) + "\n")
+    for path in (jams, kkr):
+        ex = llg.describe_config(_with_exc_file(path))["terms"][0]
+        got = sorted(zip(ex["bi"], ex["bj"], map(tuple, np.reshape(ex["T"], (-1, 3))),
+                         map(tuple, np.reshape(ex["J"], (-1, 9)))))
+        want = sorted(zip(ref["bi"], ref["bj"], map(tuple, np.reshape(ref["T"], (-1, 3))),
+                          map(tuple, np.reshape(ref["J"], (-1, 9)))))
+        assert got == want, path
+
+
+@pytest.mark.parametrize("content,needle", [
+    ("Fe Fe 0.5 0.5 0.5\n", "incorrect number of columns"),
+    ("Fe 1 0.5 0.5 0.5 2.0\n", "failed to discover"),
+    ("# only comments\n\n", "failed to discover"),
+    ("Fe Fe 0.5 0.5 0.5 2.0\nFe Fe 1.0 0.0 zero 1.2\n", "failed to read line 2"),
+    ("1 3 0.5 0.5 0.5 2.0\n", "basis index out of range"),
+])
+def test_exc_file_errors(llg, tmp_path, content, needle):
+    p = tmp_path / "bad.txt"
+    p.write_text(content)
+    with pytest.raises(llg.LLGError, match=needle):
+        llg.describe_config(_with_exc_file(p))
+
+
+def test_exc_file_missing(llg, tmp_path):
+    with pytest.raises(llg.LLGError, match="failed to open exc_file"):
+        llg.describe_config(_with_exc_file(tmp_path / "absent.txt"))
