@@ -63,3 +63,21 @@ def test_two_exchange_modules_run_the_tiled_kernels(llg):
     ea, eb = a.observables(0)[1], b.observables(0)[1]
     np.testing.assert_allclose(eb[0] + eb[1], ea[0], rtol=1e-12)
     np.testing.assert_allclose(eb[2:], ea[1:], rtol=1e-12)
+
+
+def test_exc_file_config_runs_like_the_inline_config(llg, tmp_path):
+    """The three bcc shells read from an exc_file (JAMS format) give the
+    inline config's FP64 trajectory bit for bit."""
+    inline = C.bcc_three_shell(L=6, T=300.0, steps=20, spin='"random"')
+    block = inline[inline.index("    interactions = ("):inline.index("    );\n", inline.index("    interactions = (")) + 7]
+    exc = tmp_path / "bcc3.txt"
+    exc.write_text("# type_i type_j rx ry rz J (meV)\nFe Fe 0.5 0.5 0.5 2.0\nFe Fe 1.0 0.0 0.0 1.2\n"
+                   "Fe Fe 1.0 1.0 0.0 -0.1\n")
+    from_file = inline.replace(block, '    exc_file = "%s";\n' % exc)
+    assert from_file != inline
+    a = llg.Solver.from_config(inline, precision=llg.FP64)
+    b = llg.Solver.from_config(from_file, precision=llg.FP64)
+    assert np.array_equal(a.get_state(0), b.get_state(0))
+    a.step(20)
+    b.step(20)
+    assert np.array_equal(a.get_state(0), b.get_state(0))
