@@ -294,15 +294,27 @@ def ref_lib():
         R.ref_fields.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         R.ref_energies.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         R.ref_destroy.restype = None
+        R.ref_seed.argtypes = [ctypes.c_uint64]
+        R.ref_seed.restype = None
+        R.ref_rk4_run.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        R.ref_term_fields.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         _ref = R
     return _ref
 
 
 class ReferenceSim:
-    """The reference's HeunLLGSolver (one global instance at a time)."""
+    """The reference's HeunLLGSolver (one global instance at a time).
 
-    def __init__(self, workload, replica: int = 0):
+    seed: seeds the reference's global pcg32 before the solver is made, so
+    that its own thermal noise (pcg32_k1024 + std::normal_distribution,
+    src/jams/solvers/cpu_llg_heun.cc:50-63) is reproducible.  rk4_run: the
+    reference's RK4 kernels built for the host, driven as
+    CudaRK4BaseSolver::run drives them (T = 0)."""
+
+    def __init__(self, workload, replica: int = 0, seed: Optional[int] = None):
         self.R = ref_lib()
+        if seed is not None:
+            self.R.ref_seed(int(seed))
         self.packed = _Packed(workload, replica, True)
         if self.R.ref_create(ctypes.byref(self.packed.model), float(workload.model.t_step)) != 0:
             raise RuntimeError(self.R.ref_last_error().decode())
@@ -314,11 +326,26 @@ class ReferenceSim:
         self.R.ref_run(_dp(s), int(nsteps))
         return s
 
+    def rk4_run(self, spins: np.ndarray, nsteps: int) -> np.ndarray:
+        s = np.ascontiguousarray(spins, dtype=np.float64).copy()
+        if self.R.ref_rk4_run(_dp(s), int(nsteps)) != 0:
+            raise RuntimeError(self.R.ref_last_error().decode())
+        return s
+
     def fields(self, spins: np.ndarray) -> np.ndarray:
         s = np.ascontiguousarray(spins, dtype=np.float64)
         h = np.empty_like(s)
         self.R.ref_fields(_dp(s), _dp(h))
         return h
+
+    def term_fields(self, spins: np.ndarray) -> np.ndarray:
+        """Each term's field_ (n_terms x N x 3, meV) at the solver time."""
+        s = np.ascontiguousarray(spins, dtype=np.float64)
+        out = np.empty((self.n_terms,) + s.shape)
+        for t in range(self.n_terms):
+            if self.R.ref_term_fields(_dp(s), t, _dp(out[t])) != 0:
+                raise RuntimeError("term %d" % t)
+        return out
 
     def energies(self, spins: np.ndarray) -> np.ndarray:
         s = np.ascontiguousarray(spins, dtype=np.float64)

@@ -243,10 +243,29 @@ Setting vec3(const double* v) {
   return a;
 }
 
-HeunLLGSolver* g_solver = nullptr;
+// The reference's CPU Heun solver with access to the solver clock (Solver's
+// protected iteration_ and time_), so that the RK4 driver below can set the
+// stage times as CudaRK4BaseSolver::run does while reusing the solver's
+// registered Hamiltonians and Solver::compute_fields.
+class HarnessSolver : public HeunLLGSolver {
+ public:
+  using HeunLLGSolver::HeunLLGSolver;
+  void set_clock(int iteration, double time) {
+    iteration_ = iteration;
+    time_ = time;
+  }
+};
+
+HarnessSolver* g_solver = nullptr;
 std::vector<Setting> g_keep;
 
 }  // namespace
+
+// the reference's RK4 kernels built for the host (ref_rk4_kernels.cc)
+void ref_host_llg_rk4_kernel(const double* s, double* k, const double* h, const double* noise, const double* gyro,
+                             const double* mus, const double* alpha, unsigned n);
+void ref_host_rk4_combine_normalise(double* s, const double* s_old, const double* k1, const double* k2,
+                                    const double* k3, const double* k4, double dt, unsigned n);
 
 extern "C" {
 
@@ -302,7 +321,7 @@ __attribute__((visibility("default"))) int ref_create(const orc_model* m, double
     solver_settings.add("t_step", Setting::number(t_step_seconds));
     solver_settings.add("t_max", Setting::number(1.0));
     solver_settings.add("gilbert_prefactor", Setting::boolean(m->gilbert_prefactor != 0));
-    g_solver = new HeunLLGSolver(solver_settings);
+    g_solver = new HarnessSolver(solver_settings);
 
     Setting physics_settings = group();
     physics_settings.add("module", Setting::string("empty"));
@@ -392,6 +411,63 @@ __attribute__((visibility("default"))) int ref_run(double* spins, int nsteps) {
   return 0;
 }
 
+// Seeds the reference's global generator (jams::instance().random_generator(),
+// pcg32), from which each HeunLLGSolver draws the seed of its own pcg32_k1024
+// noise generator at construction (src/jams/solvers/cpu_llg_heun.h:35): a
+// ref_create after ref_seed gives a reproducible thermal trajectory.
+__attribute__((visibility("default"))) void ref_seed(uint64_t seed) { jams::instance().random_generator().seed(seed); }
+
+// nsteps of CudaRK4BaseSolver::run (src/jams/solvers/cuda_rk4_base.cu:50-108)
+// with the CUDALLGRK4Solver kernels (cuda_llg_rk4.cu:16-32), at T = 0, on the
+// host: s_old = s; k1 from the fields at t0; s = s_old + dt/2 k1 at t0 + dt/2
+// (cublasDcopy then cublasDaxpy, written here as a k + s with two roundings,
+// as the oracle and the GPU FP64 form compute it; the library may fuse the
+// multiply-add); k2;
+// s = s_old + dt/2 k2; k3 at t0 + dt/2; s = s_old + dt k3; k4 at t0 + dt;
+// then the combination and the normalisation of post_step (one kernel of the
+// reference that evaluates both, see ref_rk4_kernels.cc).  The fields come
+// from the reference's CPU Hamiltonians through Solver::compute_fields (the
+// reference's GPU path sums the same terms with cuSPARSE and cuBLAS).  The
+// derivative, combination and normalisation are the reference's own kernels
+// (ref_rk4_kernels.cc).  The iteration and time advance as the solver's do.
+__attribute__((visibility("default"))) int ref_rk4_run(double* spins, int nsteps) {
+  if (!g_solver) return -1;
+  try {
+    if (g_solver->physics()->temperature() > 0.0) throw std::runtime_error("the RK4 driver runs at T = 0 only");
+    const int n = globals::num_spins, n3 = 3 * n;
+    std::vector<double> s_old(n3), k[4], zero(n3, 0.0);
+    for (auto& v : k) v.assign(n3, 0.0);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < 3; ++j) globals::s(i, j) = spins[3 * i + j];
+    const double dt = g_solver->time_step();
+    for (int step = 0; step < nsteps; ++step) {
+      const int it = g_solver->iteration();
+      const double t0 = g_solver->time();
+      for (int q = 0; q < n3; ++q) s_old[q] = globals::s.data()[q];
+      const double stage_dt[3] = {0.5 * dt, 0.5 * dt, dt};
+      for (int st = 0; st < 4; ++st) {
+        g_solver->compute_fields();
+        ref_host_llg_rk4_kernel(globals::s.data(), k[st].data(), globals::h.data(), zero.data(), globals::gyro.data(),
+                                globals::mus.data(), globals::alpha.data(), (unsigned)n);
+        if (st == 3) break;
+        g_solver->set_clock(it, t0 + stage_dt[st]);
+        double* s = globals::s.data();
+        for (int q = 0; q < n3; ++q) s[q] = s_old[q];
+        for (int q = 0; q < n3; ++q) s[q] = stage_dt[st] * k[st][q] + s[q];
+      }
+      ref_host_rk4_combine_normalise(globals::s.data(), s_old.data(), k[0].data(), k[1].data(), k[2].data(),
+                                     k[3].data(), dt, (unsigned)n);
+      g_solver->set_clock(it + 1, (it + 1) * dt);
+    }
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < 3; ++j) spins[3 * i + j] = globals::s(i, j);
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
 __attribute__((visibility("default"))) int ref_fields(const double* spins, double* h) {
   if (!g_solver) return -1;
   const int n = globals::num_spins;
@@ -400,6 +476,20 @@ __attribute__((visibility("default"))) int ref_fields(const double* spins, doubl
   g_solver->compute_fields();
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < 3; ++j) h[3 * i + j] = globals::h(i, j);
+  return 0;
+}
+
+// one term's field_ after its calculate_fields at the solver time, as a
+// Hamiltonian plugin leaves it (src/jams/core/hamiltonian.h:15-78)
+__attribute__((visibility("default"))) int ref_term_fields(const double* spins, int term, double* h) {
+  if (!g_solver || term < 0 || term >= (int)g_solver->hamiltonians().size()) return -1;
+  const int n = globals::num_spins;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < 3; ++j) globals::s(i, j) = spins[3 * i + j];
+  auto& hh = g_solver->hamiltonians()[term];
+  hh->calculate_fields(g_solver->time());
+  const double* f = hh->ptr_field();
+  for (int q = 0; q < 3 * n; ++q) h[q] = f[q];
   return 0;
 }
 

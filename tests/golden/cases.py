@@ -1,4 +1,4 @@
-"""The small seeded workloads behind the golden fixtures (all T = 0, Heun).
+"""The small seeded workloads behind the golden fixtures.
 
 cases(): the reference's exchange, anisotropy and field terms; the FP64 form
 equals these bit for bit.  dipole_cases(): with the dipole-dipole term (the
@@ -6,7 +6,11 @@ reference's dipole-bruteforce Hamiltonian); the FFT evaluation equals these
 within rounding, not bit for bit.  pulse_cases(): time-dependent applied
 fields (sinc and sinc-cos pulses) and zeeman dc / ac fields; their sin and cos
 come from the C library, so the fixtures pin the oracle bit for bit where
-they were made and the GPU form within 1e-12 elsewhere."""
+they were made and the GPU form within 1e-12 elsewhere.  long_cases(): 1000
+T = 0 steps, of the simple-cubic benchmark lattice at full size (Heun) and of
+a triangular DMI monolayer (RK4, the reference's RK4 kernels built for the
+host).  thermal_cases(): the reference's own finite-temperature Heun run,
+summarised as means and numerical standard errors of |M| and the energies."""
 from jams_gb300 import workloads as W
 
 
@@ -63,3 +67,50 @@ def pulse_cases():
         "sc4x5x6_sinc_cos_zeeman_ac": _sc_pulse(),
         "bcc4_sinc_zeeman_dc_ac": _bcc_pulse(),
     }
+
+
+def long_cases():
+    """name -> (workload, integrator label, steps kept): T = 0, random start.
+    The simple-cubic fixture keeps only the state after 1000 steps and a
+    SHA-256 digest of its seeded start (W.initial_state regenerates it)."""
+    tri = W.triangular_dmi_field_sweep(L=16, n_fields=1, T=0.0)
+    tri.replicas[0].B = (0.0, 0.0, 0.5)
+    return {
+        "sc32_heun_1000": (W.sc_ferromagnet(L=32), "heun", (1000,)),
+        "tri16_dmi_rk4_1000": (tri, "rk4", (1, 10, 100, 1000)),
+    }
+
+
+# bcc 10^3 x 2 (2000 spins) with the three-shell exchange and cubic
+# anisotropy of the bcc 64^3 benchmark (mean-field ordering temperature
+# about 85 K): 40 K in the ordered phase, 300 K in the paramagnetic phase.
+# Start +z; burn-in steps, then samples every `every` steps.
+THERMAL_SEED = 20261204
+
+
+def thermal_cases():
+    """name -> (workload, burn-in steps, steps between samples, samples)."""
+    return {
+        "thermal_bcc10_3shell_40K": (W.bcc_three_shell(L=10, T=40.0, start="+z"), 200000, 25, 8000),
+        "thermal_bcc10_3shell_300K": (W.bcc_three_shell(L=10, T=300.0, start="+z"), 20000, 25, 4000),
+    }
+
+
+def thermal_summary(abs_m, energies, n_spins):
+    """Means and numerical standard errors (Stats::spectral_density_zero,
+    src/jams/helpers/stats.cc:16-50) of |M| and of the energies per spin
+    (total, then per term) of a sampled run."""
+    import numpy as np
+
+    from jams_gb300 import stats
+
+    e = np.asarray(energies, dtype=np.float64) / n_spins
+    series = {"abs_m": np.asarray(abs_m, dtype=np.float64), "e_total": e.sum(axis=1)}
+    for t in range(e.shape[1]):
+        series["e_term%d" % t] = e[:, t]
+    out = {}
+    for k, x in series.items():
+        out[k + "_mean"] = float(x.mean())
+        out[k + "_nse"] = stats.num_std_err(x)
+        out[k + "_geweke"] = stats.geweke(x)[0]
+    return out

@@ -4,10 +4,12 @@ Runs the reference's own CPU Heun solver (HeunLLGSolver::run,
 src/jams/solvers/cpu_llg_heun.cc:45-148), its Solver::compute_fields and its
 Hamiltonian terms, compiled from the reference sources by
 oracle/Makefile.ref into oracle/_ref/libjams_ref.so.  This only works where the
-reference sources are present (the development container):
+reference sources are present (the development container; the Makefile finds
+them through $JAMS_REFERENCE_DIR or a checkout named "reference" beside
+this repository):
 
-    make -f oracle/Makefile.ref REF=/root/reference
-    python tests/golden/make_golden.py
+    make -f oracle/Makefile.ref
+    python tests/golden/make_golden.py [case ...]
 
 The dipole cases run the reference's dipole-bruteforce Hamiltonian
 (src/jams/hamiltonian/dipole_bruteforce.cc) compiled the same way, the pulse
@@ -15,14 +17,24 @@ cases its applied-field pulses and zeeman term (applied_field.cc, zeeman.cc);
 these also hold the fields and energies after the 100 steps, at the solver
 time 100 dt.
 
-Each fixture holds, for a small seeded case at T = 0: the initial spins, the
-total field and per-term energies of the reference at those spins, and the
-reference's spins after 1, 10 and 100 Heun steps.  The reference's thermal
-noise (pcg32 + std::normal_distribution) is not reproducible elsewhere, so
-fixtures are T = 0 only.
+Each T = 0 fixture holds, for a small seeded case: the initial spins, the
+total field, each term's field_ and the per-term energies of the reference
+at those spins, and the
+reference's spins after 1, 10 and 100 Heun steps.  The long cases hold the
+spins after up to 1000 steps: Heun on the simple-cubic benchmark lattice
+(32^3), and RK4 on a triangular DMI monolayer through the reference's RK4
+kernels built for the host (oracle/ref_rk4_kernels.cc).
+
+The thermal cases run the reference's Heun solver at T > 0 with its own
+noise (pcg32_k1024 + std::normal_distribution, cpu_llg_heun.cc:50-63),
+seeded through the reference's global generator so that the fixture can be
+made again.  They hold the means and numerical standard errors of |M| (the
+magnetisation monitor's normalisation by the summed moments) and of the
+energies per spin, sampled as tests/golden/cases.py states.
 """
 from __future__ import annotations
 
+import hashlib
 import os
 import sys
 
@@ -33,7 +45,8 @@ sys.path.insert(0, ROOT)
 
 from jams_gb300 import workloads as W  # noqa: E402
 from oracle import oracle as O  # noqa: E402
-from tests.golden.cases import cases, dipole_cases, pulse_cases  # noqa: E402
+from tests.golden.cases import (THERMAL_SEED, cases, dipole_cases, long_cases, pulse_cases,  # noqa: E402
+                                thermal_cases, thermal_summary)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -48,7 +61,7 @@ def main():
             continue
         s0 = W.initial_state(w, 0)
         ref = O.ReferenceSim(w)
-        out = {"s0": s0, "fields": ref.fields(s0), "energies": ref.energies(s0)}
+        out = {"s0": s0, "fields": ref.fields(s0), "energies": ref.energies(s0), "term_fields": ref.term_fields(s0)}
         s = s0
         done = 0
         for k in (1, 10, 100):
@@ -60,6 +73,36 @@ def main():
             out["energies100"] = ref.energies(s)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, {k: v.shape for k, v in out.items()})
+    for name, (w, integ, keep) in long_cases().items():
+        if only and name not in only:
+            continue
+        s0 = W.initial_state(w, 0)
+        ref = O.ReferenceSim(w)
+        out = {"s0": s0} if s0.size <= 3 * 4096 else {"s0_sha256": hashlib.sha256(s0.tobytes()).hexdigest()}
+        s, done = s0, 0
+        for k in keep:
+            s = ref.rk4_run(s, k - done) if integ == "rk4" else ref.run(s, k - done)
+            done = k
+            out["s%d" % k] = s
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, {k: getattr(v, "shape", v) for k, v in out.items()})
+    for name, (w, burn, every, nsamp) in thermal_cases().items():
+        if only and name not in only:
+            continue
+        ref = O.ReferenceSim(w, seed=THERMAL_SEED)
+        s = ref.run(W.initial_state(w, 0), burn)
+        mus = np.tile(w.model.mus, w.spins_per_replica[0] // w.model.nb)
+        abs_m, energies = [], []
+        for _ in range(nsamp):
+            s = ref.run(s, every)
+            m = (mus[:, None] * s).sum(axis=0) / mus.sum()
+            abs_m.append(float(np.linalg.norm(m)))
+            energies.append(ref.energies(s))
+        summ = thermal_summary(abs_m, energies, len(s))
+        out = {"temperature": w.replicas[0].temperature, "L": np.array(w.replicas[0].L), "burn_in": burn,
+               "every": every, "samples": nsamp, "seed": THERMAL_SEED, **summ}
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, {k: float(v) for k, v in summ.items()})
 
 
 if __name__ == "__main__":
