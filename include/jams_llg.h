@@ -226,6 +226,19 @@ int llg_set_field(llg_handle *h, int32_t replica, const double B[3]);
    order (CudaSolver::compute_fields, src/jams/cuda/cuda_solver.cc:11-26). */
 int llg_fields(llg_handle *h, int32_t replica, double *h_host);
 
+/* The field of one term (index into the descriptor's term list, or the
+   config's Hamiltonian order) at the current spins and solver time, meV,
+   N x 3 in site order: what Hamiltonian::calculate_fields(t) leaves in that
+   term's field_ (src/jams/core/hamiltonian.h:15-78; e.g.
+   SparseInteractionHamiltonian::calculate_fields,
+   src/jams/hamiltonian/sparse_interaction.cc:36-45).  The FP64 form gives
+   the reference's values bit for bit; the FP32C form computes the term
+   from its FP32 state.  The _device variant writes to device memory (a
+   Hamiltonian's dev_ptr_field()) on the handle's stream and returns when
+   the copy is done. */
+int llg_term_fields(llg_handle *h, int32_t replica, int32_t term, double *h_host);
+int llg_term_fields_device(llg_handle *h, int32_t replica, int32_t term, double *h_dev);
+
 /* FP64 on-device reductions of one replica: m4 = (Mx, My, Mz, |M|) with
    M = sum mu_s S / sum mu_s (src/jams/monitors/magnetisation.cc:77-104);
    e_terms[n_terms] = total energy of each term in meV
@@ -294,14 +307,17 @@ int llg_autotune(llg_handle *h, int32_t trial_steps, int32_t use_cache);
    doubles, basis site of spin i = i % nb, mu_s per basis site in mus[nb]),
    written to m4_dev (4 doubles of device memory) on cuda_stream - without
    allocating anything.  It exists for callers that cannot call cudaMalloc
-   when they need the value: code running during stream capture, host loops
-   that must not synchronise the device, memory owned by an external pool.
-   Its reduction scratch is a fixed 32 KiB device array inside the library
-   (held on every GPU that loads it until exit); n_spins above 2^30 or not a
-   multiple of nb is rejected with LLG_ERR_BAD_DESC.  The first call on a
-   device looks up that array's device address; make that first call before
-   any stream capture.  All calls share the array: calls that overlap on the
-   GPU race.  Errors are reported through llg_last_error(NULL). */
+   when they need the value: host loops that must not synchronise the device
+   (cudaMalloc and cudaFree can), and callers whose device memory belongs to
+   an external pool or arena.  Its reduction scratch is a fixed 32 KiB
+   device array inside the library (held on every GPU that loads it until
+   exit); n_spins above 2^30 or not a multiple of nb, nb outside [1, 4] and
+   a mu_s that is not positive and finite are rejected with
+   LLG_ERR_BAD_DESC.  The first call on a device looks up that array's
+   device address (set-up done once per device, with the device current);
+   make that first call before any stream capture, and do not call
+   cudaDeviceReset after it.  All calls share the array: calls that overlap
+   on the GPU race.  Errors are reported through llg_last_error(NULL). */
 int llg_magnetisation_noalloc(const double *spins_dev, int64_t n_spins, int32_t nb, const double *mus,
                               double *m4_dev, void *cuda_stream);
 

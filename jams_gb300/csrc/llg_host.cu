@@ -1430,6 +1430,47 @@ int llg_fields(llg_handle* h, int32_t replica, double* h_host) {
   return 0;
 }
 
+// one term's field at the current state into `out` (host or device memory)
+static int term_fields(llg_handle* h, int32_t replica, int32_t term, double* out, bool device_out) {
+  if (!h) return tls_fail(LLG_ERR_BAD_DESC, "null handle");
+  if (replica < 0 || replica >= (int32_t)h->reps.size() || !out)
+    return h->fail(LLG_ERR_BAD_DESC, "replica %d out of range", replica);
+  if (term < 0 || term >= h->nterms) return h->fail(LLG_ERR_BAD_DESC, "term %d outside [0, %d)", term, h->nterms);
+  cudaSetDevice(h->device);
+  int rc = sync_replicas(h);
+  if (rc) return rc;
+  const ReplicaDev& R = h->reps[replica];
+  const dim3 grid((unsigned)h->P.ntiles);
+  const int sb = state_buffer(h);
+  rc = upload_pulse_now(h);   // fields at the solver time
+  if (rc) return rc;
+  const Params P = launch_params(h, h->state[sb].p, 0);
+  if (!h->async_err.empty()) {
+    const std::string e = h->async_err;
+    h->async_err.clear();
+    return h->fail(LLG_ERR_CUDA, "%s", e.c_str());
+  }
+  if (h->fp64)
+    term_fields_f64<<<grid, kBlock, 0, h->stream>>>(P, buf<double>(h, sb), h->d_scratch.p, replica, term);
+  else
+    term_fields_f32<<<grid, kBlock, 0, h->stream>>>(P, buf<float>(h, sb), h->d_scratch.p, replica, term);
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "term fields kernel");
+  ce = cudaMemcpyAsync(out, h->d_scratch.p, (size_t)R.n * 3 * sizeof(double),
+                       device_out ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "copying term fields");
+  return 0;
+}
+
+int llg_term_fields(llg_handle* h, int32_t replica, int32_t term, double* h_host) {
+  return term_fields(h, replica, term, h_host, false);
+}
+
+int llg_term_fields_device(llg_handle* h, int32_t replica, int32_t term, double* h_dev) {
+  return term_fields(h, replica, term, h_dev, true);
+}
+
 // the replica's observable sums in the observe kernel's layout: mu_s S and
 // mu_s (0..3), the energy of every term (4..), mu_s S and mu_s per basis site
 // (4 + nterms + 4 b ..)

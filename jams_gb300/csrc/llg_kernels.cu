@@ -151,13 +151,15 @@ __device__ __forceinline__ void exchange_f32(const Params& P, int t, const Repli
 }
 
 // total field (meV) of all terms at spin s, compensated, FP32; pf: the time
-// factors of the stage (null: no time-dependent field)
+// factors of the stage (null: no time-dependent field); only >= 0: the field
+// of that term alone
 __device__ __forceinline__ void field_f32(const Params& P, const ReplicaDev& R, Site st, int64_t gi,
                                           const Planes<const float>& S, const float s[3], float h[3],
-                                          const float* hd, const float* pf) {
+                                          const float* hd, const float* pf, int only = -1) {
   float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
   const int b = st.b;
   for (int t = 0; t < P.nterms; ++t) {
+    if (only >= 0 && t != only) continue;
     const TermDev& T = P.term[t];
     switch (T.kind) {
       case kExchange:
@@ -780,6 +782,44 @@ __global__ void __launch_bounds__(kBlock) fields_f64(const __grid_constant__ Par
   const double s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
   double h[3];
   field_f64(P, R, st, me.gi, S, s, h, P.hdip64, P.pulse_now64);
+  out[3 * (int64_t)me.i] = h[0];
+  out[3 * (int64_t)me.i + 1] = h[1];
+  out[3 * (int64_t)me.i + 2] = h[2];
+}
+
+// the field (meV) of term `term` alone, as the reference's
+// Hamiltonian::calculate_fields leaves it in field_ (src/jams/core/
+// hamiltonian.h:15-78): FP64 in the reference's association order, FP32C
+// from the FP32 state with the FP32 term arithmetic; AoS N x 3 doubles
+__global__ void __launch_bounds__(kBlock) term_fields_f64(const __grid_constant__ Params P,
+                                                         const double* __restrict__ s0, double* __restrict__ out,
+                                                         int replica, int term) {
+  const ReplicaDev* Rp;
+  const Me me = whoami(P, Rp);
+  if (!me.active || me.r != replica) return;
+  const ReplicaDev& R = *Rp;
+  const Site st = locate(R, P.nb, me.i);
+  const Planes<const double> S = planes(s0, P.npad);
+  const double s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
+  double f[3];
+  term_field_f64(P, P.term[term], R, st, me.gi, S, s, f, P.hdip64, P.pulse_now64);
+  out[3 * (int64_t)me.i] = f[0];
+  out[3 * (int64_t)me.i + 1] = f[1];
+  out[3 * (int64_t)me.i + 2] = f[2];
+}
+
+__global__ void __launch_bounds__(kBlock) term_fields_f32(const __grid_constant__ Params P,
+                                                         const float* __restrict__ s0, double* __restrict__ out,
+                                                         int replica, int term) {
+  const ReplicaDev* Rp;
+  const Me me = whoami(P, Rp);
+  if (!me.active || me.r != replica) return;
+  const ReplicaDev& R = *Rp;
+  const Site st = locate(R, P.nb, me.i);
+  const Planes<const float> S = planes(s0, P.npad);
+  const float s[3] = {S.x[me.gi], S.y[me.gi], S.z[me.gi]};
+  float h[3];
+  field_f32(P, R, st, me.gi, S, s, h, P.hdip32, P.pulse_now32, term);
   out[3 * (int64_t)me.i] = h[0];
   out[3 * (int64_t)me.i + 1] = h[1];
   out[3 * (int64_t)me.i + 2] = h[2];

@@ -33,6 +33,10 @@ __global__ void fields_f32(const __grid_constant__ Params P, const float* __rest
                            double* __restrict__ out, int replica);
 __global__ void fields_f64(const __grid_constant__ Params P, const double* __restrict__ s0,
                            double* __restrict__ out, int replica);
+__global__ void term_fields_f32(const __grid_constant__ Params P, const float* __restrict__ s0,
+                                double* __restrict__ out, int replica, int term);
+__global__ void term_fields_f64(const __grid_constant__ Params P, const double* __restrict__ s0,
+                                double* __restrict__ out, int replica, int term);
 
 void launch_rk4_f32(int stage, unsigned grid, cudaStream_t st, const Params& P, const float* s0, const float* sin,
                     float* acc, float* sout, uint32_t k);

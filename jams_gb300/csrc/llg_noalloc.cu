@@ -2,20 +2,22 @@
 // without allocating any memory.
 //
 // Who needs it: code that must not call cudaMalloc/cudaFree at the moment it
-// wants the magnetisation - a monitor running while a stream is being
-// captured into a CUDA graph (allocation is not capturable), a host loop that
-// must not synchronise the device (cudaMalloc/cudaFree can), or a caller whose
-// device memory is owned by an external pool that forbids other allocations.
-// The regular path (llg_observables) keeps its reduction partials in memory
-// the handle allocated; this entry point uses the same two-pass block
-// reduction with its partials in a fixed, file-scope device array instead.
+// wants the magnetisation - a host loop that must not synchronise the device
+// (cudaMalloc and cudaFree can), or a caller whose device memory is owned by
+// an external pool or arena that forbids other allocations.  The regular
+// path (llg_observables) keeps its reduction partials in memory the handle
+// allocated; this entry point uses the same two-pass block reduction with
+// its partials in a fixed, file-scope device array instead.
 //
 // Scratch: kNoAllocMaxBlocks x 4 doubles (32 KiB) of device memory, held by
 // every GPU that loads this library until the process exits.  Every call on
 // a device shares it and it keeps the previous call's contents; the first
 // pass writes every slot the second pass reads, so nothing needs clearing.
 // Two calls whose kernels overlap on the GPU (different streams without
-// ordering) race on the array and give wrong results.
+// ordering) race on the array and give wrong results.  The array's device
+// address is looked up once per device and kept: a cudaDeviceReset after the
+// first call on a device is not supported (the reloaded module may put the
+// array elsewhere).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -121,7 +123,8 @@ extern "C" int llg_magnetisation_noalloc(const double* spins_dev, int64_t n_spin
   }
   Mus m{};
   for (int b = 0; b < nb; ++b) {
-    if (!(mus[b] > 0.0)) return fail(LLG_ERR_BAD_DESC, "llg_magnetisation_noalloc: mu_s must be positive");
+    if (!(std::isfinite(mus[b]) && mus[b] > 0.0))
+      return fail(LLG_ERR_BAD_DESC, "llg_magnetisation_noalloc: mu_s must be positive and finite");
     m.v[b] = mus[b];
   }
   int dev = 0;
@@ -144,6 +147,10 @@ extern "C" int llg_magnetisation_noalloc(const double* spins_dev, int64_t n_spin
   const int64_t want = (n_spins + kNoAllocBlock - 1) / kNoAllocBlock;
   const int nblocks = (int)(want < kNoAllocMaxBlocks ? want : kNoAllocMaxBlocks);
   cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  // an error left pending by earlier, unrelated work is cleared here, so that
+  // the check after the launches reports only these launches (an error that
+  // corrupted the context persists and is reported there)
+  (void)cudaGetLastError();
   noalloc_partials<<<nblocks, kNoAllocBlock, 0, st>>>(spins_dev, n_spins, nb, m, scratch);
   noalloc_finish<<<1, kNoAllocBlock, 0, st>>>(scratch, nblocks, m4_dev);
   ce = cudaGetLastError();

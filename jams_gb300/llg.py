@@ -37,7 +37,8 @@ EXPORTED = [
     "llg_profile_stages", "llg_kernel_info", "llg_set_tuning", "llg_autotune", "llg_magnetisation_noalloc",
     "llg_create_from_config", "llg_config_describe", "llg_max_steps",
     "llg_write_array_file", "llg_read_array_file", "llg_write_spins", "llg_read_spins",
-    "llg_save_checkpoint", "llg_load_checkpoint", "llg_magnetisation_groups",
+    "llg_save_checkpoint", "llg_load_checkpoint", "llg_magnetisation_groups", "llg_term_fields",
+    "llg_term_fields_device",
 ]
 
 
@@ -112,6 +113,8 @@ def lib(checked: bool = False):
         L.llg_set_temperature.argtypes = [vp, i32, ctypes.c_double]
         L.llg_set_field.argtypes = [vp, i32, dp]
         L.llg_fields.argtypes = [vp, i32, dp]
+        L.llg_term_fields.argtypes = [vp, i32, i32, dp]
+        L.llg_term_fields_device.argtypes = [vp, i32, i32, vp]
         L.llg_observables.argtypes = [vp, i32, dp, dp]
         L.llg_magnetisation_groups.argtypes = [vp, i32, ctypes.POINTER(i32), i32, i32, dp]
         L.llg_topological_charge.argtypes = [vp, i32, dp]
@@ -252,7 +255,7 @@ def build_desc(workload: W.Workload, precision: int = FP32C, device: int = 0, st
     d.integrator = int(m.integrator)
     d.precision = int(precision)
     d.rk4_normalise_stages = int(bool(rk4_normalise_stages))
-    d.seed = int(workload.seed)
+    d.seed = int(workload.seed if workload.noise_seed is None else workload.noise_seed)
     d.n_replicas = len(workload.replicas)
     d.replicas = ctypes.cast(reps, ctypes.POINTER(LlgReplica))
     d.device = int(device)
@@ -374,6 +377,12 @@ class Solver:
     def fields(self, replica: int = 0) -> np.ndarray:
         out = np.empty((self.num_spins(replica), 3))
         self._check(self.L.llg_fields(self.h, replica, _dp(out)))
+        return out
+
+    def term_fields(self, term: int, replica: int = 0) -> np.ndarray:
+        """The field (meV, N x 3) of one Hamiltonian term alone."""
+        out = np.empty((self.num_spins(replica), 3))
+        self._check(self.L.llg_term_fields(self.h, replica, term, _dp(out)))
         return out
 
     def observables(self, replica: int = 0):

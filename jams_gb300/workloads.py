@@ -118,6 +118,11 @@ class Workload:
     seed: int = 1
     start: str = "random"  # "random" or "+z"
     description: str = ""
+    # a subset of a larger replica list (one rank's share): the original
+    # index of each replica (its start state), and the noise key of this
+    # share, distinct per share (None: the full list, keyed by seed)
+    replica_ids: Optional[List[int]] = None
+    noise_seed: Optional[int] = None
 
     @property
     def spins_per_replica(self) -> List[int]:
@@ -450,4 +455,5 @@ def initial_state(w: Workload, replica: int) -> np.ndarray:
         s = np.zeros((n, 3))
         s[:, 2] = 1.0
         return s
-    return random_sphere(n, w.seed * 7919 + replica)
+    rid = w.replica_ids[replica] if w.replica_ids is not None else replica
+    return random_sphere(n, w.seed * 7919 + rid)

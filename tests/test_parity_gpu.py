@@ -41,6 +41,30 @@ def test_fp64_equals_reference_golden_vectors(llg, name):
     s.synchronize()
 
 
+@pytest.mark.parametrize("name", sorted(cases().keys()))
+def test_term_fields_equal_the_reference_hamiltonians_fields(llg, name):
+    """llg_term_fields: each term's field as the reference's
+    Hamiltonian::calculate_fields leaves it in field_ (FP64: bit for bit;
+    FP32C: within 2e-6 of the field scale); the terms add up to llg_fields."""
+    w = cases()[name]
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    ref = g["term_fields"]
+    for prec in (llg.FP64, llg.FP32C):
+        s = solver(llg, w, prec)
+        s.set_state(g["s0"])
+        got = np.stack([s.term_fields(t, 0) for t in range(len(w.model.terms))])
+        if prec == llg.FP64:
+            assert np.array_equal(got, ref)
+            total = got[0].copy()
+            for t in range(1, len(got)):
+                total = total + got[t]
+            assert np.array_equal(total, s.fields(0))
+        else:
+            scale = np.abs(ref).max()
+            assert np.abs(got - ref).max() <= 2e-6 * scale
+        s.close()
+
+
 @pytest.mark.parametrize("T", [0.0, 300.0])
 def test_fp64_heun_bcc_equals_oracle(llg, oracle, T):
     w = W.bcc_three_shell(L=8, T=T, start="random")
