@@ -1,17 +1,26 @@
 #!/usr/bin/env python3
-"""LLG spin-steps/s on one GB300.
+"""LLG spin-steps/s on one GB300: the FP32C and FP64 forms and the fraction
+of HBM bandwidth the dominant stage kernel reaches.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
                     [--precision fp32c|fp64] [--impl ours|reference]
 
 A step is one stochastic-LLG time step (Heun: predictor + corrector, RK4:
 four stages) over every spin of the workload.  Default workload: bcc,
-2-site conventional basis, 64^3 cells (524,288 spins), isotropic exchange
-to the third shell, cubic anisotropy, T = 300 K thermal field, Heun,
-FP32 spins with compensated neighbour sums (the benchmark's FP32 form).
+2-site conventional basis, 256^3 cells (33,554,432 spins, 403 MB per FP32
+state vector: larger than L2), nearest-neighbour exchange J = 1 meV,
+uniaxial K1 = 0.1 meV, B = 1 T, T = 500 K thermal field, Heun dt = 0.5 fs,
+FP32 spins with compensated neighbour sums (the FP32C form).  The same line
+carries, each as an object of its own:
+  fp64         the FP64 form on the same workload (K capped at 100 steps) and
+               the FP32C / FP64 ratio;
+  three_shell  the three-shell + cubic reading of the same 256^3 lattice;
+  config2      bcc 64^3 x 2, three shells + cubic, 300 K (L2-resident);
+  accuracy     max |dS|, d|M|, dE of FP32C against FP64 after 1000 T = 0
+               steps at the workload's own size.
 
 Timing: W untimed steps, then K timed steps (K defaults to the workload's
-own run length: 20,000 steps for the default), each bracketed by CUDA events
+own run length: 2000 steps for the default), each bracketed by CUDA events
 on the solver's stream with an L2 flush (a 256 MiB write) between steps, a
 barrier + synchronize on both sides, max over ranks.  value = spins x K /
 sum of step times.  e2e: the same steps through the C ABI with the FP64
@@ -20,11 +29,14 @@ roofline: the dominant stage kernel's algorithmic bytes per launch / its
 mean CUDA-event duration, against the measured HBM copy bandwidth.
 cpu_baseline / --impl reference: the oracle's restatement of the
 reference's CPU Heun path (CSR SpMV, per-term field arrays, serial noise
-draw as the reference does) on all host cores.
+draw as the reference does) on all host cores, a bounded number of steps
+of the full lattice.
 
-Several GPUs (torchrun, one process per GPU): replicas only.  Each rank
-integrates its own independent copy of the workload (seed offset by the
-rank); value = all ranks' spin-steps / the slowest rank's time.
+Several GPUs (torchrun, one process per GPU), no collective on the data
+path.  A replica list (temperature or field sweep) is split over the ranks,
+balanced by spin count; a single-replica workload runs as an independent
+copy per rank (seed offset by the rank).  value = all ranks' spin-steps /
+the slowest rank's time.
 """
 from __future__ import annotations
 
@@ -52,6 +64,13 @@ STAGE_BYTES = {
     ("rk4", "fp32c"): [36, 60, 60, 48],
     ("rk4", "fp64"): [72, 120, 120, 96],
 }
+# BASELINE metric: spin-steps/s of the FP32C and FP64 forms and the HBM
+# fraction, on one GPU
+METRIC = "LLG spin-steps/s on 1 GB300: FP32 vs FP64 form at \u22641e-5 max|\u0394S|; % of HBM peak"
+# the default line also carries these workloads, each as an object of its own
+SECONDARY = {"bcc256_nn": {"three_shell": "bcc256_3shell", "config2": "bcc64_3shell"}}
+DEFAULT_WORKLOAD = "bcc256_nn"
+
 STAGE_NAMES = {"heun": ["heun_predict", "heun_correct"], "rk4": ["rk4_stage1", "rk4_stage2", "rk4_stage3",
                                                                  "rk4_stage4"]}
 
@@ -124,15 +143,19 @@ def parse(argv=None):
     p.add_argument("--steps", type=int, default=None,
                    help="timed steps (default: the workload's own run length, e.g. 20000 for bcc64_3shell)")
     p.add_argument("--warmup", type=int, default=20)
-    p.add_argument("--workload", default="bcc64_3shell", choices=sorted(WORKLOADS))
+    p.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-accuracy", action="store_true", help="skip the FP32C-vs-FP64 accuracy check")
+    p.add_argument("--accuracy-cap", type=int, default=0,
+                   help="cells per axis of the accuracy check's lattice (0: the workload's own size)")
+    p.add_argument("--no-extra", action="store_true",
+                   help="skip the FP64-form, three-shell and bcc 64^3 objects of the default line")
     p.add_argument("--ref-gpu", default="auto", choices=["auto", "on", "off"],
                    help="time the restated reference GPU path (baseline/refgpu.cu) on replica 0: auto = single-replica "
-                        "Heun workloads up to 4.2 M spins")
+                        "Heun workloads whose int32 CSR fits (up to 40 M spins)")
     p.add_argument("--profile-steps", type=int, default=50)
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--tuning", default="", help="planes_per_cta,flags,occupancy instead of autotuning (flags: 1 stored rhs, 2 narrow tile, "
@@ -180,18 +203,57 @@ def init_ranks(world: int, local: int, backend: str = "nccl"):
         dist.init_process_group(backend)
 
 
-def rank_workload(name: str, rank: int):
-    """The workload of one rank: the named configuration with the seed offset
-    by the rank, so every rank integrates its own independent replicas
-    (distinct noise streams and starts) of the same size: weak scaling."""
+def rank_workload(name: str, rank: int, world: int = 1):
+    """The workload of one rank.  A replica list (temperature or field sweep)
+    is split over the ranks: rank r takes a disjoint subset, balanced by spin
+    count (split_replicas), with the original replicas' starts and its own
+    noise key.  A single-replica workload is not split: every
+    rank integrates its own independent copy (seed offset by the rank), i.e.
+    weak scaling."""
     w = WORKLOADS[name]()
-    w.seed = w.seed + rank
+    if world > 1 and len(w.replicas) > 1:
+        parts = split_replicas([int(np.prod(r.L)) * w.model.nb for r in w.replicas], world)
+        w.replicas = [w.replicas[i] for i in parts[rank]]
+        w.replica_ids = parts[rank]          # starts of the original replicas
+        w.noise_seed = w.seed * 1000003 + rank + 1   # noise streams distinct across ranks
+    else:
+        w.seed = w.seed + rank
     return w
 
 
-def job_rate(spins_per_rank: int, world: int, steps: int, seconds: float) -> float:
-    """Whole-job spin-steps/s: every rank's spins over the slowest rank's time."""
-    return world * spins_per_rank * steps / seconds
+def split_replicas(spins, world: int):
+    """Disjoint subsets of replica indices, one per rank, that together cover
+    every replica and balance the spins: largest replica first, each to the
+    rank with the fewest spins so far (ties to the lower rank).  Each
+    subset is returned in ascending replica order.  With at least as many
+    replicas as ranks no rank is empty, and the largest rank total exceeds
+    the smallest by at most one replica's spins."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    order = sorted(range(len(spins)), key=lambda i: (-spins[i], i))
+    load = [0] * world
+    parts = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        parts[r].append(i)
+        load[r] += spins[i]
+    return [sorted(p) for p in parts]
+
+
+def job_rate(spins_all_ranks: int, steps: int, seconds: float) -> float:
+    """Whole-job spin-steps/s: the spins of every rank over the slowest rank's time."""
+    return spins_all_ranks * steps / seconds
+
+
+def sum_over_ranks(x: float, world: int, device=None) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
 
 
 def gather_scalars(values, world: int, device=None):
@@ -202,10 +264,9 @@ def gather_scalars(values, world: int, device=None):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor(list(values), dtype=torch.float64, device=device)
-    out = [torch.empty_like(t) for _ in range(world)]
-    dist.all_gather(out, t)
-    return [o.cpu().tolist() for o in out]
+    out = [None] * world
+    dist.all_gather_object(out, [float(v) for v in values])   # ranks may hold different replica counts
+    return out
 
 
 # ------------------------------------------------------------------ clocks --
@@ -312,13 +373,15 @@ def run_reference(args, rank, world):
     value = sim.n * k / dt
 
     line = {
-        "metric": "LLG spin-steps/s", "value": value, "unit": "spin-steps/s", "impl": "reference",
+        "metric": METRIC, "value": value, "unit": "spin-steps/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": k, "warmup": args.warmup, "ms_per_step": 1e3 * dt / k,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": args.workload, "spins": sim.n, "description": w.description,
-                                         "replicas_timed": 1},
+        "data": "synthetic (seeded spins, the configuration's Hamiltonian)",
+        "config": workload_config(args.workload, w, sum(w.spins_per_replica)),
         "cpu_baseline": {"value": value, "unit": "spin-steps/s", "cores": threads, "kind": "port",
-                         "sample": "%d Heun steps of replica 0 (%d spins), full lattice" % (k, sim.n)},
+                         "sample": "%d %s steps of replica 0 (%d spins, the full lattice) after %d warm-up steps, "
+                                   "OpenMP on all host cores, noise drawn serially as the reference draws it"
+                                   % (k, "RK4" if w.model.integrator == W.RK4 else "Heun", sim.n, args.warmup)},
         "e2e": {"value": value, "unit": "spin-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -337,18 +400,20 @@ def tiled_stem(name: str):
     return tuple(args[:3] + [args[4] if len(args) == 7 else args[3]])
 
 
-def accuracy_vs_fp64(w, steps=1000, cap=32):
+def accuracy_vs_fp64(w, steps=1000, cap=0):
     """max |dS|, d|M| and dE of the FP32C form against the FP64 form (which
     equals the oracle, and through it the reference's CPU solver, bit for
-    bit) after `steps` T = 0 steps.  The workload's Hamiltonian and integrator on
-    replica 0 with at most `cap` cells per axis and a random start."""
+    bit) after `steps` T = 0 steps.  The workload's Hamiltonian and integrator
+    on replica 0 (at most `cap` cells per axis when cap > 0, else its own
+    size) with a random start."""
     import copy
 
     from jams_gb300 import llg
 
     w2 = copy.deepcopy(w)
     r0 = w2.replicas[0]
-    r0.L = tuple(min(int(l), cap) for l in r0.L)
+    if cap > 0:
+        r0.L = tuple(min(int(l), cap) for l in r0.L)
     r0.temperature = 0.0
     w2.replicas = [r0]
     w2.start = "random"
@@ -385,8 +450,10 @@ def reference_gpu_rate(args, w):
         why = "the reference GPU path restated here is Heun"
     elif any(t.kind not in supported or t.pulse != W.PULSE_STATIC for t in w.model.terms):
         why = "terms outside the restatement (exchange, uniaxial, cubic, static field)"
-    elif args.ref_gpu == "auto" and (len(w.replicas) > 1 or n > (1 << 22)):
-        why = "skipped by default above 4.2 M spins or for several replicas (--ref-gpu on)"
+    elif args.ref_gpu == "auto" and (len(w.replicas) > 1 or n > 40_000_000):
+        why = "skipped by default above 40 M spins or for several replicas (--ref-gpu on)"
+    elif sum(3 * len(t.bi) for t in w.model.terms if t.kind == W.TERM_EXCHANGE) * n // w.model.nb >= 2 ** 31:
+        why = "the reference's CSR needs more than 2^31 stored values (int32 indices)"
     if why:
         return {"unavailable": why}
     try:
@@ -428,6 +495,126 @@ def traffic_from_profiles(workload: str, kernel: str, precision: str):
         return None
 
 
+def workload_config(name: str, w, n_spins: int) -> dict:
+    """The `config` object of a bench line: the same keys and values in both
+    arms (this library and --impl reference)."""
+    vec_mb = n_spins * 12 / 1e6
+    l2 = ("state larger than the 129 MB L2 (%.0f MB per FP32 state vector); the GPU arm also flushes L2 between "
+          "timed steps (256 MiB write)" % vec_mb) if vec_mb > 129 else \
+        ("state smaller than L2 (%.1f MB per FP32 state vector): the GPU arm flushes L2 between timed steps "
+         "(256 MiB write)" % vec_mb)
+    return {"workload": name, "description": w.description, "spins": int(n_spins), "replicas": len(w.replicas),
+            "l2": l2}
+
+
+def load_peak():
+    """HBM copy bandwidth (GB/s) and where it came from."""
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        if peaks.get("hbm_gbs"):
+            return float(peaks["hbm_gbs"]), "measured"
+    except (OSError, ValueError):
+        pass
+    return 6800.0, "fallback"
+
+
+def make_solver(llg, w, prec, local, stream, tuning_arg: str = "", tune: bool = True):
+    sol = llg.Solver(w, precision=prec, device=local)
+    sol.set_stream(stream.cuda_stream)
+    for r in range(len(w.replicas)):
+        sol.set_state(W.initial_state(w, r), r)
+    if tuning_arg:
+        tx, fl, oc = (int(v) for v in tuning_arg.split(","))
+        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2), bool(fl & 4))
+        tuning = sol.kernel_info()
+    else:
+        # the choice is cached per lattice shape ($JAMS_LLG_TUNE_CACHE), so a
+        # second run of the same command launches no trial kernels
+        tuning = sol.autotune(trial_steps=10, use_cache=True) if tune else sol.kernel_info()
+    return sol, tuning
+
+
+def timed_steps(torch, sol, steps: int, warmup: int, flush, stream, world: int, local: int, clocks=None):
+    """W untimed steps, then K single steps each bracketed by CUDA events on
+    the solver's stream, L2 flushed before each; barrier + synchronize on
+    both sides; max over ranks.  Returns (total ms, launches, wall s)."""
+    for _ in range(warmup):
+        sol.step(1)
+    torch.cuda.synchronize()
+    if clocks is not None:
+        clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    launches = 0
+    t_wall = time.perf_counter()
+    for k in range(steps):
+        flush.fill_(float(k))
+        evs[k][0].record(stream)
+        sol.step(1)
+        evs[k][1].record(stream)
+        launches += sol.last_launch_count
+    torch.cuda.synchronize()
+    barrier(world)
+    t_wall = time.perf_counter() - t_wall
+    total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs), world, torch.device("cuda", local))
+    sol.synchronize()
+    return total_ms, launches, t_wall
+
+
+def stage_roofline(sol, w, name: str, precision: str, tuning: dict, flush, profile_steps: int, ms_per_step: float,
+                   n_spins: int):
+    """Per-stage kernel durations (CUDA events on the solver's stream, L2
+    flushed before each step) and the roofline of the dominant stage kernel:
+    its algorithmic bytes per launch / its mean duration, against the HBM
+    copy bandwidth.  Returns (roofline, per-stage dipole ms)."""
+    integ = "heun" if w.model.integrator == W.HEUN else "rk4"
+    ns = len(STAGE_BYTES[(integ, precision)])
+    stage_ms = np.zeros(ns)
+    dip_ms = np.zeros(ns)
+    for _ in range(profile_steps):
+        flush.fill_(1.0)
+        k_ms, d_ms = sol.profile_stages(1, dipole=True)
+        stage_ms += k_ms
+        dip_ms += d_ms
+    stage_ms /= profile_steps
+    dip_ms /= profile_steps
+    dom = int(np.argmax(stage_ms))
+    bytes_per_launch = STAGE_BYTES[(integ, precision)][dom] * n_spins
+    achieved = bytes_per_launch / (stage_ms[dom] * 1e-3) / 1e9
+    peak, peak_src = load_peak()
+    has_dipole = any(t.kind == W.TERM_DIPOLE for t in w.model.terms)
+    kname = kernel_name(tuning, integ, dom, precision, has_dipole)
+    traffic = traffic_from_profiles(name, kname, precision)
+    step_bytes = sum(STAGE_BYTES[(integ, precision)])
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": kname, "stage": STAGE_NAMES[integ][dom], "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": int(bytes_per_launch),
+                "stage_ms": [float(x) for x in stage_ms],
+                "algorithmic_bytes_per_spin_step": int(step_bytes),
+                "step_frac": (step_bytes * n_spins / (ms_per_step * 1e-3) / 1e9) / peak}
+    return roofline, dip_ms
+
+
+def secondary_form(torch, llg, args, name: str, precision: str, local: int, stream, flush, steps: int,
+                   warmup: int):
+    """One more workload or precision in the same line: value, ms per step,
+    roofline of its dominant kernel, clocks and the kernels it ran."""
+    w = WORKLOADS[name]()
+    prec = llg.FP32C if precision == "fp32c" else llg.FP64
+    sol, tuning = make_solver(llg, w, prec, local, stream, tune=not args.no_tune)
+    n_spins = sol.num_spins(-1)
+    clocks = ClockSampler(local)
+    total_ms, launches, _ = timed_steps(torch, sol, steps, warmup, flush, stream, 1, local, clocks)
+    clk = clocks.stop()
+    ms = total_ms / steps
+    roof, _ = stage_roofline(sol, w, name, precision, tuning, flush, max(5, args.profile_steps // 5), ms, n_spins)
+    sol.close()
+    return {"workload": name, "description": w.description, "spins": int(n_spins), "precision": precision,
+            "value": n_spins * steps / (total_ms * 1e-3), "unit": "spin-steps/s", "steps": steps, "warmup": warmup,
+            "ms_per_step": ms, "gpu_launches": launches, "roofline": roof, "clocks": clk, "kernels": tuning}
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -442,95 +629,36 @@ def main():
     from jams_gb300 import llg
 
     B.build()
-    w = rank_workload(args.workload, rank)
+    w = rank_workload(args.workload, rank, world)
     if args.steps is None:
         args.steps = w.steps
     prec = llg.FP32C if args.precision == "fp32c" else llg.FP64
     integ = "heun" if w.model.integrator == W.HEUN else "rk4"
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)  # torch work (L2 flush, events) and the solver share one stream
-    sol = llg.Solver(w, precision=prec, device=local)
-    sol.set_stream(stream.cuda_stream)
-    for r in range(len(w.replicas)):
-        sol.set_state(W.initial_state(w, r), r)
-    n_spins = sol.num_spins(-1)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    if args.tuning:
-        tx, fl, oc = (int(v) for v in args.tuning.split(","))
-        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2), bool(fl & 4))
-        tuning = sol.kernel_info()
-    else:
-        # the choice is cached per lattice shape ($JAMS_LLG_TUNE_CACHE), so a
-        # second run of the same command launches no trial kernels
-        tuning = sol.autotune(trial_steps=10, use_cache=True) if not args.no_tune else sol.kernel_info()
-
-    # warm-up (also builds nothing lazily: single steps use direct launches)
-    for _ in range(args.warmup):
-        sol.step(1)
-    torch.cuda.synchronize()
+    sol, tuning = make_solver(llg, w, prec, local, stream, args.tuning, not args.no_tune)
+    n_spins = sol.num_spins(-1)
+    spins_all = int(sum_over_ranks(float(n_spins), world, torch.device("cuda", local)))
 
     # ---- timed region: K steps, L2 flushed between steps
     clocks = ClockSampler(local)
-    clocks.start()
-    barrier(world)
-    torch.cuda.synchronize()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    launches = 0
-    t_wall = time.perf_counter()
-    for k in range(args.steps):
-        flush.fill_(float(k))
-        evs[k][0].record(stream)
-        sol.step(1)
-        evs[k][1].record(stream)
-        launches += sol.last_launch_count
-    torch.cuda.synchronize()
-    barrier(world)
-    t_wall = time.perf_counter() - t_wall
+    total_ms, launches, t_wall = timed_steps(torch, sol, args.steps, args.warmup, flush, stream, world, local, clocks)
     clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = max_over_ranks(sum(step_ms), world, torch.device("cuda", local))
     ms_per_step = total_ms / args.steps
-    value = job_rate(n_spins, world, args.steps, total_ms * 1e-3)
-    sol.synchronize()
+    value = job_rate(spins_all, args.steps, total_ms * 1e-3)
 
-    # ---- per-stage kernel durations (same flush between steps)
+    # ---- per-stage kernel durations and the roofline of the dominant one
+    roofline, dip_ms = stage_roofline(sol, w, args.workload, args.precision, tuning, flush, args.profile_steps,
+                                      ms_per_step, n_spins)
     ns = len(STAGE_BYTES[(integ, args.precision)])
-    stage_ms = np.zeros(ns)
-    dip_ms = np.zeros(ns)
-    for _ in range(args.profile_steps):
-        flush.fill_(1.0)
-        k_ms, d_ms = sol.profile_stages(1, dipole=True)
-        stage_ms += k_ms
-        dip_ms += d_ms
-    stage_ms /= args.profile_steps
-    dip_ms /= args.profile_steps
-    dom = int(np.argmax(stage_ms))
-    bytes_per_launch = STAGE_BYTES[(integ, args.precision)][dom] * n_spins
-    achieved = bytes_per_launch / (stage_ms[dom] * 1e-3) / 1e9
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    peak = peaks.get("hbm_gbs")
-    peak_src = "measured" if peak else "fallback"
-    peak = peak or 6800.0
-    has_dipole = any(t.kind == W.TERM_DIPOLE for t in w.model.terms)
-    kname = kernel_name(tuning, integ, dom, args.precision, has_dipole)
-    traffic = traffic_from_profiles(args.workload, kname, args.precision)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": kname, "stage": STAGE_NAMES[integ][dom], "peak_source": peak_src,
-                "stage_ms": [float(x) for x in stage_ms],
-                "algorithmic_bytes_per_spin_step": int(sum(STAGE_BYTES[(integ, args.precision)])),
-                "step_frac": (sum(STAGE_BYTES[(integ, args.precision)]) * n_spins / (ms_per_step * 1e-3) / 1e9)
-                / peak}
 
     # ---- dipole term: FFT convolution before every stage (cuFFT transforms
     # and this library's scatter / k-space product / gather kernels)
     dipole = None
     if any(t.kind == W.TERM_DIPOLE for t in w.model.terms):
         dipole = {"ms_per_evaluation": float(dip_ms.mean()), "evaluations_per_step": ns,
-                  "share_of_stage_time": float(dip_ms.sum() / (dip_ms.sum() + stage_ms.sum())),
+                  "share_of_stage_time": float(dip_ms.sum() / (dip_ms.sum() + np.sum(roofline["stage_ms"]))),
                   "r_cutoff": next(t.r_cutoff for t in w.model.terms if t.kind == W.TERM_DIPOLE)}
 
     # ---- steady state without flush: blocks of 100 steps as CUDA graphs
@@ -551,106 +679,127 @@ def main():
     # ---- e2e through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
-        host = torch.empty((n_spins, 3), dtype=torch.float64, pin_memory=True)
-        host_np = host.numpy()
-        host_np[:] = sol.get_state(-1)
-        ke = max(10, min(200, args.steps // 10))
-        for _ in range(3):
-            sol.set_state(host_np, -1)
-            sol.step(1)
-            sol.get_state(-1, out=host_np)
-        torch.cuda.synchronize()
-        barrier(world)
-        t_set = t_step = t_get = 0.0
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            a = time.perf_counter()
-            sol.set_state(host_np, -1)
-            b = time.perf_counter()
-            sol.step(1)
-            sol.synchronize()
-            c = time.perf_counter()
-            sol.get_state(-1, out=host_np)
-            t_set += b - a
-            t_step += c - b
-            t_get += time.perf_counter() - c
-        dt = time.perf_counter() - t0
-        dt = max_over_ranks(dt, world, torch.device("cuda", local))
-        # the host link: pinned copies of the state's size, each direction
-        dev = torch.empty_like(host, device="cuda")
-        link = {}
-        for name, dst, src in (("h2d", dev, host), ("d2h", host, dev)):
-            dst.copy_(src)
-            torch.cuda.synchronize()
-            t1 = time.perf_counter()
-            for _ in range(20):
-                dst.copy_(src)
-            torch.cuda.synchronize()
-            link[name] = n_spins * 24 * 20 / (time.perf_counter() - t1) / 1e9
-        # both directions at once (two streams): what each direction keeps
-        # when the link is shared; the set / step / get loop cannot use it,
-        # since each step's input is the previous step's result
-        host2 = torch.empty_like(host, pin_memory=True)
-        dev2 = torch.empty_like(dev)
-        s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        for _ in range(20):
-            with torch.cuda.stream(s_in):
-                dev.copy_(host, non_blocking=True)
-            with torch.cuda.stream(s_out):
-                host2.copy_(dev2, non_blocking=True)
-        torch.cuda.synchronize()
-        link["duplex_each_way"] = n_spins * 24 * 20 / (time.perf_counter() - t1) / 1e9
-        del host2, dev2
-        floor_s = n_spins * 24 * (1.0 / link["h2d"] + 1.0 / link["d2h"]) / 1e9 + ms_per_step * 1e-3
-        e2e = {"value": job_rate(n_spins, world, ke, dt), "unit": "spin-steps/s", "h2d_bytes_per_step": n_spins * 24,
-               "d2h_bytes_per_step": n_spins * 24, "steps": ke,
-               "us_per_step": {"set_state": 1e6 * t_set / ke, "step": 1e6 * t_step / ke, "get_state": 1e6 * t_get / ke},
-               "host_link_gbs": link,
-               "link_floor_value": job_rate(n_spins, world, 1, floor_s)}
+        e2e = measure_e2e(torch, sol, n_spins, spins_all, args.steps, world, local, ms_per_step)
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rate, cores, n_steps, n_rep = cpu_port_rate(w)
         cpu = {"value": rate, "unit": "spin-steps/s", "cores": cores, "kind": "port",
-               "sample": "%d Heun/RK4 steps of replica 0 (%d spins), oracle restatement of the reference CPU path"
-                         % (n_steps, n_rep)}
+               "sample": "%d Heun/RK4 steps of replica 0 (%d spins, the full lattice), oracle restatement of the "
+                         "reference CPU path, OpenMP on all host cores" % (n_steps, n_rep)}
 
     ref_gpu = None
     accuracy = None
     if rank == 0 and world == 1:
         ref_gpu = reference_gpu_rate(args, w)
         if args.precision == "fp32c" and not args.no_accuracy:
-            accuracy = accuracy_vs_fp64(w)
+            accuracy = accuracy_vs_fp64(w, cap=args.accuracy_cap)
 
     # |M| of every replica of every rank at the end of the run
     mags = [float(sol.observables(r)[0][3]) for r in range(len(w.replicas))]
     mags = gather_scalars(mags, world, torch.device("cuda", local))
+    sol.close()
+
+    # ---- the rest of the metric, in the same line (rank 0, N = 1): the FP64
+    # form on this workload, the three-shell reading of the 256^3 lattice and
+    # the L2-resident bcc 64^3 headline configuration
+    forms = {}
+    if rank == 0 and world == 1 and not args.no_extra:
+        ks = min(args.steps, 100)
+        if args.precision == "fp32c":
+            f64 = secondary_form(torch, llg, args, args.workload, "fp64", local, stream, flush, ks,
+                                 min(args.warmup, 5))
+            f64["fp32c_over_fp64"] = (n_spins * args.steps / (total_ms * 1e-3)) / f64["value"]
+            forms["fp64"] = f64
+        for key, name in SECONDARY.get(args.workload, {}).items():
+            forms[key] = secondary_form(torch, llg, args, name, "fp32c", local, stream, flush, args.steps,
+                                        args.warmup)
 
     line = {
-        "metric": "LLG spin-steps/s", "value": value, "unit": "spin-steps/s", "n_gpus": world,
+        "metric": METRIC, "value": value, "unit": "spin-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32c" else "f64",
-        "data": "synthetic",
-        "config": {"workload": args.workload, "description": w.description, "spins": n_spins,
-                   "replicas": len(w.replicas), "precision": args.precision, "integrator": integ,
-                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas" if world > 1
-                   else "single GPU", "kernels": tuning},
+        "scaling": "strong" if (world > 1 and len(WORKLOADS[args.workload]().replicas) > 1) else "weak",
+        "vs_baseline": None, "dtype": "f32" if args.precision == "fp32c" else "f64",
+        "data": "synthetic (seeded spins, the configuration's Hamiltonian)",
+        "config": workload_config(args.workload, WORKLOADS[args.workload](), spins_all),
+        "solver": {"precision": args.precision, "integrator": integ, "kernels": tuning,
+                   "parallelism": ("replica list split over %d ranks" % world) if world > 1 else "single GPU"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         "steady_state_graph": steady, "wall_s_timed_region": t_wall,
         "final_abs_m": {"mean": float(np.mean([m for r in mags for m in r])), "ranks": len(mags)},
         "dipole": dipole, "reference_gpu": ref_gpu, "accuracy": accuracy,
     }
+    line.update(forms)
     if rank == 0:
         print(json.dumps(line))
-    sol.close()
     if world > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
     return 0
+
+
+def measure_e2e(torch, sol, n_spins: int, spins_all: int, steps: int, world: int, local: int, ms_per_step: float):
+    """The same steps through the C ABI with host buffers: every step copies
+    the FP64 state from pinned host memory, steps, and copies it back."""
+    host = torch.empty((n_spins, 3), dtype=torch.float64, pin_memory=True)
+    host_np = host.numpy()
+    host_np[:] = sol.get_state(-1)
+    ke = max(10, min(200, steps // 10))
+    for _ in range(3):
+        sol.set_state(host_np, -1)
+        sol.step(1)
+        sol.get_state(-1, out=host_np)
+    torch.cuda.synchronize()
+    barrier(world)
+    t_set = t_step = t_get = 0.0
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        a = time.perf_counter()
+        sol.set_state(host_np, -1)
+        b = time.perf_counter()
+        sol.step(1)
+        sol.synchronize()
+        c = time.perf_counter()
+        sol.get_state(-1, out=host_np)
+        t_set += b - a
+        t_step += c - b
+        t_get += time.perf_counter() - c
+    dt = time.perf_counter() - t0
+    dt = max_over_ranks(dt, world, torch.device("cuda", local))
+    # the host link: pinned copies of the state's size, each direction
+    dev = torch.empty_like(host, device="cuda")
+    link = {}
+    for name, dst, src in (("h2d", dev, host), ("d2h", host, dev)):
+        dst.copy_(src)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(20):
+            dst.copy_(src)
+        torch.cuda.synchronize()
+        link[name] = n_spins * 24 * 20 / (time.perf_counter() - t1) / 1e9
+    # both directions at once (two streams): what each direction keeps when
+    # the link is shared; the set / step / get loop cannot use it, since each
+    # step's input is the previous step's result
+    host2 = torch.empty_like(host, pin_memory=True)
+    dev2 = torch.empty_like(dev)
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(20):
+        with torch.cuda.stream(s_in):
+            dev.copy_(host, non_blocking=True)
+        with torch.cuda.stream(s_out):
+            host2.copy_(dev2, non_blocking=True)
+    torch.cuda.synchronize()
+    link["duplex_each_way"] = n_spins * 24 * 20 / (time.perf_counter() - t1) / 1e9
+    del host2, dev2
+    floor_s = n_spins * 24 * (1.0 / link["h2d"] + 1.0 / link["d2h"]) / 1e9 + ms_per_step * 1e-3
+    return {"value": job_rate(spins_all, ke, dt), "unit": "spin-steps/s", "h2d_bytes_per_step": n_spins * 24,
+            "d2h_bytes_per_step": n_spins * 24, "steps": ke,
+            "us_per_step": {"set_state": 1e6 * t_set / ke, "step": 1e6 * t_step / ke, "get_state": 1e6 * t_get / ke},
+            "host_link_gbs": link, "link_floor_value": job_rate(spins_all, 1, floor_s)}
 
 
 if __name__ == "__main__":
