@@ -71,6 +71,8 @@ METRIC = "LLG spin-steps/s on 1 GB300: FP32 vs FP64 form at \u22641e-5 max|\u039
 SECONDARY = {"bcc256_nn": {"three_shell": "bcc256_3shell", "config2": "bcc64_3shell"}}
 DEFAULT_WORKLOAD = "bcc256_nn"
 
+# the fused Heun step (one kernel per step, FP32C): read s0, write s1
+FUSED_STEP_BYTES = 24
 STAGE_NAMES = {"heun": ["heun_predict", "heun_correct"], "rk4": ["rk4_stage1", "rk4_stage2", "rk4_stage3",
                                                                  "rk4_stage4"]}
 
@@ -121,6 +123,10 @@ def kernel_name(info: dict, integ: str, stage: int, precision: str, dipole: bool
     if info.get("family", "generic") != "generic" and precision == "fp32c":
         fam = {"sc": "FamSC", "bcc": "FamBCC", "bcc3": "FamBCC3", "triangular": "FamTRI", "fcc": "FamFCC",
                "fcc2": "FamFCC2"}[info["family"]]
+        if info.get("fused"):
+            nt = 32 * info["tile_y"] * {"fcc": 4, "fcc2": 4, "bcc": 2, "bcc3": 2}.get(info["family"], 1)
+            minb = max(1, (256 * (4 if info["occupancy"] >= 4 else 2)) // nt)
+            return "fused_heun<%s, %d, %d>" % (fam, info["tile_y"], minb)
         if integ == "heun":
             st = 0 if stage == 0 else (2 if info["store_rhs"] else 1)
         else:
@@ -159,7 +165,7 @@ def parse(argv=None):
     p.add_argument("--profile-steps", type=int, default=50)
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--tuning", default="", help="planes_per_cta,flags,occupancy instead of autotuning (flags: 1 stored rhs, 2 narrow tile, "
-                        "4 two rows per thread)")
+                        "4 two rows per thread, 8 the fused Heun step)")
     return p.parse_args(argv)
 
 
@@ -525,7 +531,7 @@ def make_solver(llg, w, prec, local, stream, tuning_arg: str = "", tune: bool = 
         sol.set_state(W.initial_state(w, r), r)
     if tuning_arg:
         tx, fl, oc = (int(v) for v in tuning_arg.split(","))
-        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2), bool(fl & 4))
+        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2), bool(fl & 4), bool(fl & 8))
         tuning = sol.kernel_info()
     else:
         # the choice is cached per lattice shape ($JAMS_LLG_TUNE_CACHE), so a
@@ -580,19 +586,25 @@ def stage_roofline(sol, w, name: str, precision: str, tuning: dict, flush, profi
     stage_ms /= profile_steps
     dip_ms /= profile_steps
     dom = int(np.argmax(stage_ms))
-    bytes_per_launch = STAGE_BYTES[(integ, precision)][dom] * n_spins
+    fused = bool(tuning.get("fused")) and precision == "fp32c"
+    # the fused Heun step is one launch: it reads s0 and writes s1 (24 B per
+    # spin); the two-pass form's 60 B per spin-step is kept for comparison
+    step_bytes = FUSED_STEP_BYTES if fused else sum(STAGE_BYTES[(integ, precision)])
+    bytes_per_launch = (FUSED_STEP_BYTES if fused else STAGE_BYTES[(integ, precision)][dom]) * n_spins
     achieved = bytes_per_launch / (stage_ms[dom] * 1e-3) / 1e9
     peak, peak_src = load_peak()
     has_dipole = any(t.kind == W.TERM_DIPOLE for t in w.model.terms)
     kname = kernel_name(tuning, integ, dom, precision, has_dipole)
     traffic = traffic_from_profiles(name, kname, precision)
-    step_bytes = sum(STAGE_BYTES[(integ, precision)])
+    two_pass = sum(STAGE_BYTES[(integ, precision)])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": kname, "stage": STAGE_NAMES[integ][dom], "peak_source": peak_src,
-                "algorithmic_bytes_per_launch": int(bytes_per_launch),
+                "traffic": traffic, "kernel": kname, "stage": "heun_step (fused)" if fused else STAGE_NAMES[integ][dom],
+                "peak_source": peak_src, "algorithmic_bytes_per_launch": int(bytes_per_launch),
                 "stage_ms": [float(x) for x in stage_ms],
                 "algorithmic_bytes_per_spin_step": int(step_bytes),
-                "step_frac": (step_bytes * n_spins / (ms_per_step * 1e-3) / 1e9) / peak}
+                "step_frac": (step_bytes * n_spins / (ms_per_step * 1e-3) / 1e9) / peak,
+                "two_pass_bytes_per_spin_step": int(two_pass),
+                "two_pass_equivalent_frac": (two_pass * n_spins / (ms_per_step * 1e-3) / 1e9) / peak}
     return roofline, dip_ms
 
 

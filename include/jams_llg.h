@@ -281,8 +281,9 @@ int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
    the corrector (else the corrector recomputes it), info[3..4] CTA tile
    (cells along the contiguous axis, rows), info[5] 1 for FP64, info[6] the
    occupancy variant (CTAs per SM the tiled kernels were compiled for),
-   info[7] rows computed per thread (1 or 2; 0 without tiled kernels).
-   info holds 8 values. */
+   info[7] rows computed per thread (1 or 2; 0 without tiled kernels),
+   info[8] 1 when each Heun step is one fused kernel (predictor and
+   corrector in one sweep).  info holds 9 values. */
 int llg_kernel_info(const llg_handle *h, int32_t *info);
 
 /* Tiling choice of the tiled FP32 kernels (no effect on other kernels):
@@ -291,8 +292,13 @@ int llg_kernel_info(const llg_handle *h, int32_t *info);
    predictor stores rhs(s0); bit 1: the narrow tile (half the rows, twice
    the CTAs, for lattices too small to fill the GPU); bit 2: two rows per
    thread (wide tile of sc, bcc and fcc lattices, no dipole term; occupancy
-   2 only); flags >> 4: occupancy variant, 2 (<= 128 registers), 3
-   (<= 80) or 4 (<= 64). */
+   2 only); bit 3: the fused Heun step, one kernel per step that computes
+   the predictor of its tile and a one-reach halo in shared memory and the
+   corrector in the same sweep (sc, bcc and fcc lattices, no dipole term;
+   bits 0 and 2 clear; bit 1 picks its narrow tile); flags >> 4: occupancy
+   variant, 2 (<= 128 registers), 3 (<= 80) or 4 (<= 64); for the fused
+   step 2 or 4 x 256 resident threads per SM.  Every choice gives the same
+   results bit for bit. */
 int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t flags);
 
 /* Times every tiling candidate (planes per CTA 2..64, stored or recomputed

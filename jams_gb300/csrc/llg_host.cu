@@ -164,6 +164,9 @@ struct llg_handle {
   int occupancy = 2;         // tiled kernels compiled for >= 2, 3 or 4 CTAs per SM
   int tz = 0, ty = 0;
   int rpt = 1;               // rows per thread of the tiled kernels (1 or 2)
+  uint64_t model_hash = 0;   // the descriptor's Hamiltonian and material parameters (checkpoint fingerprint)
+  bool fused = false;        // Heun: one fused step kernel (predictor over tile + halo in shared memory)
+  bool fused_wide = true;    // its wide tile (fused_rows)
   TiledParams TP{};
   DevBuf<int4> d_tiles4;
   // dipole-dipole term: FFT convolution state and the field planes of the
@@ -401,6 +404,80 @@ int build_tiles4(llg_handle* h) {
 void drop_graphs(llg_handle* h) {
   for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
   h->graphs.clear();
+}
+
+// FNV-1a over the values that define a model's physics besides the lattice
+// sizes: materials, periodicity, dt convention, and every term's parameters
+// (interaction templates, anisotropy constants and axes, fields, pulses,
+// dipole geometry), in term order
+struct ModelHasher {
+  uint64_t h = 1469598103934665603ull;
+  void bytes(const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+  }
+  template <class T>
+  void val(T v) { bytes(&v, sizeof v); }
+  template <class T>
+  void arr(const T* p, size_t n) {
+    val((uint64_t)(p ? n : 0));
+    if (p && n) bytes(p, n * sizeof(T));
+  }
+};
+
+uint64_t model_hash(const llg_desc* d) {
+  ModelHasher m;
+  m.val(d->nb);
+  m.arr(d->periodic, 3);
+  m.arr(d->mus, (size_t)d->nb);
+  m.arr(d->gyro, (size_t)d->nb);
+  m.arr(d->alpha, (size_t)d->nb);
+  m.val(d->gilbert_prefactor);
+  m.val(d->rk4_normalise_stages);
+  m.val(d->n_terms);
+  for (int t = 0; t < d->n_terms; ++t) {
+    const llg_term& T = d->terms[t];
+    const size_t nb = (size_t)d->nb;
+    m.val(T.kind);
+    m.val(T.order);
+    switch (T.kind) {
+      case LLG_TERM_EXCHANGE: {
+        const size_t ni = T.n_int > 0 ? (size_t)T.n_int : 0;
+        m.arr(T.bi, ni);
+        m.arr(T.bj, ni);
+        m.arr(T.T, 3 * ni);
+        m.arr(T.J, 9 * ni);
+        break;
+      }
+      case LLG_TERM_UNIAXIAL:
+      case LLG_TERM_CUBIC:
+        m.arr(T.K, nb);
+        m.arr(T.axis, nb * (T.kind == LLG_TERM_CUBIC ? 9 : 3));
+        break;
+      case LLG_TERM_APPLIED_FIELD:
+        m.arr(T.B, 3);
+        m.val(T.pulse);
+        m.val(T.time_center);
+        m.val(T.freq_bandwidth);
+        m.val(T.freq_center);
+        break;
+      case LLG_TERM_DIPOLE:
+        m.val(T.r_cutoff);
+        m.val(T.distance_tolerance);
+        m.val(T.lattice_parameter);
+        m.arr(T.lattice_vectors, 9);
+        m.arr(T.positions, 3 * nb);
+        break;
+      case LLG_TERM_ZEEMAN:
+        m.arr(T.dc_field, 3 * nb);
+        m.arr(T.ac_field, 3 * nb);
+        if (T.ac_field) m.arr(T.ac_frequency, nb);
+        break;
+      default:
+        break;
+    }
+  }
+  return m.h;
 }
 
 int build(llg_handle* h, const llg_desc* d) {
@@ -1059,6 +1136,15 @@ bool launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
   if (h->tiled) {
     const unsigned g4 = (unsigned)h->TP.ntiles;
     float* aux = reinterpret_cast<float*>(h->aux.p);
+    if (h->fused) {
+      // the whole step in the launch of stage 0; stage 1 has nothing to do
+      if (stage == 0) {
+        const cudaError_t e = launch_fused(h->family, h->fused_wide, h->occupancy, g4, st, P, h->TP,
+                                           buf<float>(h, cur), buf<float>(h, 2 - cur), ks, advance);
+        if (e != cudaSuccess && h->async_err.empty()) h->async_err = std::string("fused step: ") + cudaGetErrorString(e);
+      }
+      return true;
+    }
     if (h->integrator == LLG_HEUN) {
       float* s0 = buf<float>(h, cur);
       float* sp = buf<float>(h, 1);
@@ -1127,6 +1213,14 @@ int next_buffer(const llg_handle* h, int cur) {
 int64_t enqueue_steps(llg_handle* h, int nsteps, int cur) {
   const int ns = num_stages(h);
   bool advanced = false;
+  if (h->fused) {
+    // one launch per step; the last advances the noise step counter
+    for (int k = 0; k < nsteps; ++k) {
+      launch_stage(h, 0, (uint32_t)k, cur, nullptr, k == nsteps - 1 ? (uint32_t)nsteps : 0u);
+      cur = next_buffer(h, cur);
+    }
+    return nsteps;
+  }
   for (int k = 0; k < nsteps; ++k) {
     for (int stg = 0; stg < ns; ++stg) {
       const bool last = k == nsteps - 1 && stg == ns - 1;
@@ -1153,6 +1247,7 @@ int llg_create(const llg_desc* desc, llg_handle** out) {
   llg_handle* h = new (std::nothrow) llg_handle();
   if (!h) return tls_fail(LLG_ERR_OOM, "host allocation failed");
   int rc = build(h, desc);
+  if (rc == 0) h->model_hash = model_hash(desc);
   if (rc == 0) rc = sync_replicas(h);
   if (rc == 0) {
     // all spins +z
@@ -1285,7 +1380,9 @@ static int step_blocks(llg_handle* h, int32_t nsteps) {
   constexpr size_t kMaxGraphs = 64;
   while (remaining > 0) {
     const int n = remaining >= K && K > 1 ? K : remaining;
-    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX + 8192 * h->ty + 131072 * h->rpt, n};
+    GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX + 8192 * h->ty +
+                     131072 * h->rpt + 524288 * (h->fused ? 1 : 0),
+                 n};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end() && (n == K || h->graphs.size() < kMaxGraphs)) {
       cudaGraph_t g;
@@ -1303,7 +1400,9 @@ static int step_blocks(llg_handle* h, int32_t nsteps) {
     if (it != h->graphs.end()) {
       cudaError_t ce = cudaGraphLaunch(it->second, h->stream);
       if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaGraphLaunch");
-      h->last_launches += (int64_t)n * (h->integrator == LLG_HEUN ? 2 : 4) + (h->tiled ? 0 : 1);
+      // per step: one fused kernel, or one kernel per stage; the other
+      // kernels' blocks end with the step-counter kernel
+      h->last_launches += (int64_t)n * (h->fused ? 1 : num_stages(h)) + (h->tiled ? 0 : 1);
     } else {
       h->last_launches += enqueue_steps(h, n, h->cur);
     }
@@ -1590,6 +1689,7 @@ int llg_kernel_info(const llg_handle* h, int32_t* info) {
   info[5] = h->fp64 ? 1 : 0;
   info[6] = h->occupancy;
   info[7] = h->tiled ? h->rpt : 0;
+  info[8] = h->fused ? 1 : 0;
   return 0;
 }
 
@@ -1597,7 +1697,7 @@ static std::string tuning_key(const llg_handle* h) {
   cudaDeviceProp prop;
   cudaGetDeviceProperties(&prop, h->device);
   std::string k = std::string(prop.name) + "|fam" + std::to_string(h->family) + "|int" +
-                  std::to_string(h->integrator) + "|nb" + std::to_string(h->nb) + "|nt" + std::to_string(h->nterms) + "|k2";
+                  std::to_string(h->integrator) + "|nb" + std::to_string(h->nb) + "|nt" + std::to_string(h->nterms) + "|k3";
   for (auto& R : h->reps)
     k += "|" + std::to_string(R.L[0]) + "x" + std::to_string(R.L[1]) + "x" + std::to_string(R.L[2]) +
          (R.thermal ? "T" : "0");
@@ -1659,6 +1759,14 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
   if (pair && (!pair_rows_supported(h->family) || h->dipole || (store_rhs & 2)))
     return h->fail(LLG_ERR_BAD_DESC, "two rows per thread: only for the wide tile of sc, bcc and fcc lattices "
                                      "without a dipole term");
+  // bit 3: the fused Heun step (bit 1 then picks its narrow tile; bits 0
+  // and 2 do not apply)
+  const bool fused = (store_rhs & 8) != 0;
+  if (fused && (h->integrator != LLG_HEUN || !fused_supported(h->family) || h->dipole || (store_rhs & 5)))
+    return h->fail(LLG_ERR_BAD_DESC, "fused step: Heun on sc, bcc or fcc lattices without a dipole term, "
+                                     "without stored rhs or two rows per thread");
+  h->fused = fused;
+  h->fused_wide = (store_rhs & 2) == 0;
   h->store_mode = (store_rhs & 1) != 0 && h->integrator == LLG_HEUN;
   const int occ = store_rhs >> 4;
   h->occupancy = occ >= 4 ? 4 : (occ == 3 ? 3 : 2);
@@ -1667,7 +1775,8 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
   // bit 1: the narrow tile (half the rows, twice the CTAs)
   int wide_tz = 0, wide_ty = 0;
   tiled_geometry(h->family, &wide_tz, &wide_ty);
-  const int ty = (store_rhs & 2) ? narrow_tile_rows(h->family) : wide_ty;
+  const int ty = fused ? fused_rows(h->family, h->fused_wide)
+                       : ((store_rhs & 2) ? narrow_tile_rows(h->family) : wide_ty);
   const bool retile = ty != h->ty;
   h->ty = ty;
   if (planes_per_cta != h->TP.TX || retile) {
@@ -1769,14 +1878,24 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
             if (h->integrator == LLG_HEUN) cands.push_back({t, 5 | (occ << 4)});
           }
         }
+  // the fused Heun step: wide or narrow tile, occupancy 2 or 4 (x 256 threads)
+  if (h->integrator == LLG_HEUN && fused_supported(h->family) && !h->dipole)
+    for (int t : {2, 4, 8, 16, 32, 64})
+      if (t <= std::max(2, maxL))
+        for (int occ : {2, 4})
+          for (int narrow : {0, 2}) {
+            if (narrow && fused_rows(h->family, false) == fused_rows(h->family, true)) continue;
+            cands.push_back({t, 8 | narrow | (occ << 4)});
+          }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
   int wide_tz0 = 0, wide_ty0 = 0;
   tiled_geometry(h->family, &wide_tz0, &wide_ty0);
-  std::pair<int, int> choice = {h->TP.TX, (h->store_mode ? 1 : 0) | (h->ty != wide_ty0 ? 2 : 0) |
-                                              (h->rpt == 2 ? 4 : 0) | (h->occupancy << 4)};
+  std::pair<int, int> choice = {h->TP.TX, h->fused ? (8 | (h->fused_wide ? 0 : 2) | (h->occupancy << 4))
+                                                   : ((h->store_mode ? 1 : 0) | (h->ty != wide_ty0 ? 2 : 0) |
+                                                      (h->rpt == 2 ? 4 : 0) | (h->occupancy << 4))};
   // each trial runs as llg_step runs steps: one CUDA graph of trial_steps
   // steps (captured and run once untimed, then timed)
   const int spg0 = h->steps_per_graph;
@@ -1825,7 +1944,7 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
 namespace {
 
 constexpr char kCkptMagic[8] = {'J', 'L', 'L', 'G', 'C', 'K', 'P', 'T'};
-constexpr uint32_t kCkptVersion = 1;
+constexpr uint32_t kCkptVersion = 2;   // 2: the fingerprint holds the model hash
 
 struct Bytes {
   std::vector<uint8_t> b;
@@ -1872,6 +1991,7 @@ uint64_t fnv1a(const uint8_t* p, size_t n) {
 
 // header fields that must match between the writing and the loading solver
 void ckpt_fingerprint(const llg_handle* h, Bytes& o) {
+  o.u64(h->model_hash);
   o.u32(h->fp64 ? LLG_FP64 : LLG_FP32C);
   o.u32(h->integrator);
   o.u32(h->nb);
@@ -2004,8 +2124,8 @@ int llg_load_checkpoint(llg_handle* h, const char* path) {
   ckpt_fingerprint(h, fp);
   if (rd.p + fp.b.size() > b.size() || std::memcmp(&b[rd.p], fp.b.data(), fp.b.size()) != 0)
     return h->fail(LLG_ERR_BAD_DESC,
-                   "checkpoint %s was written by a different model (replicas, sizes, basis, precision, "
-                   "integrator, dt or seed differ)",
+                   "checkpoint %s was written by a different model (Hamiltonian terms or their parameters, "
+                   "materials, replicas, sizes, basis, precision, integrator, dt or seed differ)",
                    path);
   rd.p += fp.b.size();
   const int64_t iteration = (int64_t)rd.un(8);
@@ -2017,11 +2137,23 @@ int llg_load_checkpoint(llg_handle* h, const char* path) {
   size_t need = 0;
   for (const ReplicaDev& R : h->reps) need += (size_t)R.n * 3 * 8;
   if (!rd.ok || rd.p + need + 8 != b.size()) return h->fail(LLG_ERR_IO, "checkpoint %s: truncated", path);
-  std::vector<double> s;
+  // everything is read and checked before anything is applied
   for (size_t r = 0; r < h->reps.size(); ++r) {
-    s.resize((size_t)h->reps[r].n * 3);
-    for (double& x : s) x = rd.f64();
-    int rc = llg_set_state(h, (int32_t)r, s.data());
+    if (!(T[r] >= 0.0) || !std::isfinite(T[r]))
+      return h->fail(LLG_ERR_IO, "checkpoint %s: replica %zu has temperature %g", path, r, T[r]);
+    for (int a = 0; a < 3; ++a)
+      if (!std::isfinite(B[3 * r + a])) return h->fail(LLG_ERR_IO, "checkpoint %s: replica %zu field", path, r);
+  }
+  if (iteration < 0) return h->fail(LLG_ERR_IO, "checkpoint %s: negative iteration", path);
+  std::vector<std::vector<double>> states(h->reps.size());
+  for (size_t r = 0; r < h->reps.size(); ++r) {
+    states[r].resize((size_t)h->reps[r].n * 3);
+    for (double& x : states[r]) x = rd.f64();
+    for (double x : states[r])
+      if (!std::isfinite(x)) return h->fail(LLG_ERR_IO, "checkpoint %s: replica %zu holds a non-finite spin", path, r);
+  }
+  for (size_t r = 0; r < h->reps.size(); ++r) {
+    int rc = llg_set_state(h, (int32_t)r, states[r].data());
     if (rc) return rc;
   }
   for (size_t r = 0; r < h->reps.size(); ++r) {

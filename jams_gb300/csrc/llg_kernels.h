@@ -57,6 +57,12 @@ bool pair_rows_supported(int family);
 cudaError_t launch_tiled(int family, int ty, int rpt, int occupancy, int stage, unsigned grid, cudaStream_t st,
                          const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
                          float* aux, uint32_t k, uint32_t advance, bool dipole);
+// fused Heun step (llg_fused.cuh, instantiated by llg_fused_a.cu and
+// llg_fused_b.cu): one launch per step, s0 -> s1; tile rows fused_rows()
+bool fused_supported(int family);
+int fused_rows(int family, bool wide);
+cudaError_t launch_fused(int family, bool wide, int occupancy, unsigned grid, cudaStream_t st, const Params& P,
+                         const TiledParams& TP, const float* s0, float* s1, uint32_t k, uint32_t adv);
 template <bool DIP, int RPT>
 cudaError_t launch_tiled_t(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
                            const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,

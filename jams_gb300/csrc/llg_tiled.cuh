@@ -391,6 +391,11 @@ __device__ __forceinline__ void carry_init(int b, const float4* ring, int xs, in
   }
 }
 
+template <class F, int B>
+__device__ __forceinline__ void shell_combine(const TiledParams& TP, const float2 (&axy)[F::NSHELL],
+                                              const float (&az)[F::NSHELL], const float (&r)[3], float hi[3],
+                                              float lo[3]);
+
 // exchange field of basis site B at the thread's cell from one ring: plain
 // FP32 sum of the neighbour spins of each shell (x and y packed), then
 // h += J_shell * sum with TwoProd/TwoSum compensation; 3x3 remainders (REST
@@ -437,8 +442,17 @@ __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const floa
   } else {
     gather_all<F, TZ, TY, B>(std::make_integer_sequence<int, F::Z>{}, bm, b0, bp, axy, az, r, TP);
   }
-  // first shell: (hi, lo) is the exact product J a (TwoProd) plus the J
-  // low word, no TwoSum needed; the other shells are added with TwoSum
+  shell_combine<F, B>(TP, axy, az, r, hi, lo);
+}
+
+// h = sum over shells of J_shell * (neighbour sum of the shell), compensated:
+// the first shell's (hi, lo) is the exact product J a (TwoProd) plus the J
+// low word, no TwoSum needed; the other shells are added with TwoSum; the
+// 3x3 remainders (REST families) last
+template <class F, int B>
+__device__ __forceinline__ void shell_combine(const TiledParams& TP, const float2 (&axy)[F::NSHELL],
+                                              const float (&az)[F::NSHELL], const float (&r)[3], float hi[3],
+                                              float lo[3]) {
   float2 hxy, lxy;
   {
     const float2 J = make_float2(TP.shell_hi[B][0], TP.shell_hi[B][0]);

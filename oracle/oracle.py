@@ -280,13 +280,16 @@ def reference_available() -> bool:
     return os.path.exists(REF_LIB_PATH)
 
 
-_ref = None
+REF_OMP_LIB_PATH = os.path.join(HERE, "_ref_omp", "libjams_ref.so")
+_refs = {}
 
 
-def ref_lib():
-    global _ref
-    if _ref is None:
-        R = ctypes.CDLL(REF_LIB_PATH)
+def ref_lib(path: Optional[str] = None):
+    """The reference build (oracle/_ref) or another build of the same
+    harness, e.g. the OpenMP one in oracle/_ref_omp."""
+    path = path or REF_LIB_PATH
+    if path not in _refs:
+        R = ctypes.CDLL(path)
         R.ref_create.argtypes = [ctypes.POINTER(OrcModel), ctypes.c_double]
         R.ref_create.restype = ctypes.c_int
         R.ref_last_error.restype = ctypes.c_char_p
@@ -298,8 +301,8 @@ def ref_lib():
         R.ref_seed.restype = None
         R.ref_rk4_run.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         R.ref_term_fields.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
-        _ref = R
-    return _ref
+        _refs[path] = R
+    return _refs[path]
 
 
 class ReferenceSim:
@@ -311,8 +314,8 @@ class ReferenceSim:
     reference's RK4 kernels built for the host, driven as
     CudaRK4BaseSolver::run drives them (T = 0)."""
 
-    def __init__(self, workload, replica: int = 0, seed: Optional[int] = None):
-        self.R = ref_lib()
+    def __init__(self, workload, replica: int = 0, seed: Optional[int] = None, lib_path: Optional[str] = None):
+        self.R = ref_lib(lib_path)
         if seed is not None:
             self.R.ref_seed(int(seed))
         self.packed = _Packed(workload, replica, True)

@@ -84,8 +84,15 @@ def long_cases():
 # bcc 10^3 x 2 (2000 spins) with the three-shell exchange and cubic
 # anisotropy of the bcc 64^3 benchmark (mean-field ordering temperature
 # about 85 K): 40 K in the ordered phase, 300 K in the paramagnetic phase.
-# Start +z; burn-in steps, then samples every `every` steps.
+# Start +z; burn-in steps, then samples every `every` steps.  The error of a
+# mean comes from independent runs: the spectral NSE of one run of this
+# length underestimates the run-to-run spread of <|M|> at 40 K several times
+# (slow magnetisation modes), so the reference runs THERMAL_REF_SEEDS
+# independent seeds and the GPU forms THERMAL_GPU_REPLICAS independent
+# replicas, and each side's error is the standard error over its runs.
 THERMAL_SEED = 20261204
+THERMAL_REF_SEEDS = 8
+THERMAL_GPU_REPLICAS = 16
 
 
 def thermal_cases():
@@ -113,4 +120,19 @@ def thermal_summary(abs_m, energies, n_spins):
         out[k + "_mean"] = float(x.mean())
         out[k + "_nse"] = stats.num_std_err(x)
         out[k + "_geweke"] = stats.geweke(x)[0]
+    return out
+
+
+def over_runs(per_run):
+    """Mean and standard error of the mean over independent runs of per-run
+    means {quantity: [value per run]}."""
+    import math
+
+    import numpy as np
+
+    out = {}
+    for k, v in per_run.items():
+        v = np.asarray(v, dtype=np.float64)
+        out[k + "_mean"] = float(v.mean())
+        out[k + "_err"] = float(v.std(ddof=1) / math.sqrt(v.size))
     return out

@@ -28,9 +28,10 @@ kernels built for the host (oracle/ref_rk4_kernels.cc).
 The thermal cases run the reference's Heun solver at T > 0 with its own
 noise (pcg32_k1024 + std::normal_distribution, cpu_llg_heun.cc:50-63),
 seeded through the reference's global generator so that the fixture can be
-made again.  They hold the means and numerical standard errors of |M| (the
-magnetisation monitor's normalisation by the summed moments) and of the
-energies per spin, sampled as tests/golden/cases.py states.
+made again, once per seed (THERMAL_REF_SEEDS independent runs, in parallel
+processes).  They hold each run's time averages of |M| (the magnetisation
+monitor's normalisation by the summed moments) and of the energies per spin,
+and their mean and standard error over the runs.
 """
 from __future__ import annotations
 
@@ -45,8 +46,8 @@ sys.path.insert(0, ROOT)
 
 from jams_gb300 import workloads as W  # noqa: E402
 from oracle import oracle as O  # noqa: E402
-from tests.golden.cases import (THERMAL_SEED, cases, dipole_cases, long_cases, pulse_cases,  # noqa: E402
-                                thermal_cases, thermal_summary)
+from tests.golden.cases import (THERMAL_REF_SEEDS, THERMAL_SEED, cases, dipole_cases, long_cases,  # noqa: E402
+                                over_runs, pulse_cases, thermal_cases, thermal_summary)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -86,24 +87,40 @@ def main():
             out["s%d" % k] = s
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, {k: getattr(v, "shape", v) for k, v in out.items()})
-    for name, (w, burn, every, nsamp) in thermal_cases().items():
-        if only and name not in only:
-            continue
-        ref = O.ReferenceSim(w, seed=THERMAL_SEED)
-        s = ref.run(W.initial_state(w, 0), burn)
-        mus = np.tile(w.model.mus, w.spins_per_replica[0] // w.model.nb)
-        abs_m, energies = [], []
-        for _ in range(nsamp):
-            s = ref.run(s, every)
-            m = (mus[:, None] * s).sum(axis=0) / mus.sum()
-            abs_m.append(float(np.linalg.norm(m)))
-            energies.append(ref.energies(s))
-        summ = thermal_summary(abs_m, energies, len(s))
-        out = {"temperature": w.replicas[0].temperature, "L": np.array(w.replicas[0].L), "burn_in": burn,
-               "every": every, "samples": nsamp, "seed": THERMAL_SEED, **summ}
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
-        print(name, {k: float(v) for k, v in summ.items()})
+    todo = [n for n in thermal_cases() if not only or n in only]
+    if todo:
+        import multiprocessing as mp
 
+        jobs = [(n, THERMAL_SEED + k) for n in todo for k in range(THERMAL_REF_SEEDS)]
+        with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+            runs = pool.starmap(thermal_run, jobs)
+        for name in todo:
+            w, burn, every, nsamp = thermal_cases()[name]
+            mine = [r for (n, _), r in zip(jobs, runs) if n == name]
+            per_run = {q: [r[q + "_mean"] for r in mine] for q in ("abs_m", "e_total", "e_term0", "e_term1")}
+            summ = over_runs(per_run)
+            out = {"temperature": w.replicas[0].temperature, "L": np.array(w.replicas[0].L), "burn_in": burn,
+                   "every": every, "samples": nsamp, "seeds": np.array([sd for (n, sd) in jobs if n == name]),
+                   **{q + "_runs": np.array(v) for q, v in per_run.items()},
+                   "run_nse_abs_m": np.array([r["abs_m_nse"] for r in mine]), **summ}
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+            print(name, {k: float(v) for k, v in summ.items()})
+
+
+def thermal_run(name, seed):
+    """One seeded thermal run of the reference (a process of its own: the
+    harness holds one solver per process)."""
+    w, burn, every, nsamp = thermal_cases()[name]
+    ref = O.ReferenceSim(w, seed=seed)
+    s = ref.run(W.initial_state(w, 0), burn)
+    mus = np.tile(w.model.mus, w.spins_per_replica[0] // w.model.nb)
+    abs_m, energies = [], []
+    for _ in range(nsamp):
+        s = ref.run(s, every)
+        m = (mus[:, None] * s).sum(axis=0) / mus.sum()
+        abs_m.append(float(np.linalg.norm(m)))
+        energies.append(ref.energies(s))
+    return thermal_summary(abs_m, energies, len(s))
 
 if __name__ == "__main__":
     main()

@@ -48,6 +48,12 @@ CASES = {
     "bcc3_fp64": (lambda: W.bcc_three_shell(L=5, T=300.0, start="random"), "FP64", None),
     "sc_film_dipole": (lambda: W.sc_ferromagnet(L=(6, 5, 3), periodic=(1, 1, 0), dipole_cutoff=2.2), "FP32C", None),
     "pulse_zeeman": (lambda: pulse_cases()["bcc4_sinc_zeeman_dc_ac"], "FP64", None),
+    # the fused Heun step: wide and narrow tiles, open and wrapping halos
+    "bcc3_fused": (lambda: W.bcc_three_shell(L=(5, 6, 35), T=300.0, start="random"), "FP32C",
+                   (2, False, 2, False, False, True)),
+    "sc_open_fused_narrow": (_open_sc, "FP32C", (4, False, 4, True, False, True)),
+    "fcc_fused": (lambda: W.fcc_ferromagnet(L=(3, 4, 5), T=300.0, start="random"), "FP32C",
+                  (2, False, 2, False, False, True)),
 }
 
 
@@ -57,7 +63,7 @@ def test_checked_build_runs_clean_and_equal(llg, checked, name):
     w = make()
     p = getattr(llg, prec)
     sims = []
-    for chk in (False, True):
+    for chk in (True, False):   # the checked build first: it skips and reports any access out of range
         s = llg.Solver(w, precision=p, steps_per_graph=4, checked=chk)
         if tuning:
             s.set_tuning(*tuning)
@@ -67,7 +73,7 @@ def test_checked_build_runs_clean_and_equal(llg, checked, name):
         s.step(5)
         s.synchronize()   # raises LLG_ERR_BOUNDS if any index was out of range
         sims.append(s)
-    a, b = sims
+    b, a = sims
     assert np.array_equal(a.get_state(-1), b.get_state(-1))
     assert np.array_equal(a.fields(0), b.fields(0))
     assert np.array_equal(a.observables(0)[1], b.observables(0)[1])

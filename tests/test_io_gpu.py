@@ -92,6 +92,32 @@ def test_checkpoint_rejects_other_models_and_corruption(llg, tmp_path):
     assert other.iteration == 0
 
 
+def test_checkpoint_rejects_other_hamiltonian_parameters(llg, tmp_path):
+    """The fingerprint covers the terms and their parameters: the same
+    lattice, seed and precision with another J, K or field is refused, and
+    the refused load leaves the solver untouched."""
+    w = W.bcc_three_shell(L=5, T=300.0, start="random")
+    a = fresh(llg, w, llg.FP32C)
+    a.step(2)
+    path = tmp_path / "run.ckpt"
+    a.save_checkpoint(str(path))
+    for change in ("J", "K", "terms"):
+        w2 = W.bcc_three_shell(L=5, T=300.0, start="random")
+        if change == "J":
+            w2.model.terms[0].J = w2.model.terms[0].J * 1.01
+        elif change == "K":
+            w2.model.terms[1].K = w2.model.terms[1].K * 2.0
+        else:
+            w2.model.terms = w2.model.terms[:1]
+        other = fresh(llg, w2, llg.FP32C)
+        before = other.get_state(-1)
+        with pytest.raises(llg.LLGError, match="different model"):
+            other.load_checkpoint(str(path))
+        assert np.array_equal(other.get_state(-1), before)
+        assert other.iteration == 0
+    fresh(llg, W.bcc_three_shell(L=5, T=300.0, start="random"), llg.FP32C).load_checkpoint(str(path))
+
+
 def test_pinned_host_buffers_go_through_the_mapped_path(llg):
     """Pinned host buffers are read in place by the unpack kernel (results
     come back through the copy engines); the result equals the pageable

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from jams_gb300 import workloads as W
-from tests.golden.cases import cases
+from tests.golden.cases import cases, pulse_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -308,18 +308,85 @@ def test_tiling_choices_give_identical_results(llg, name):
     choices = [(1, False, 2, False, False), (1, True, 4, False, False), (3, False, 4, False, False),
                (4, True, 3, False, False), (8, True, 2, False, False), (64, False, 2, False, False),
                (2, True, 4, True, False), (6, False, 3, True, False), (64, True, 2, True, False)]
+    choices = [c + (False,) for c in choices]
     if name != "tri":
-        choices += [(2, False, 2, False, True), (4, True, 2, False, True), (64, True, 2, False, True)]
-    for tx, store, occ, narrow, pair in choices:
+        choices += [(2, False, 2, False, True, False), (4, True, 2, False, True, False),
+                    (64, True, 2, False, True, False)]
+        # the fused step (wide and narrow tiles, both occupancy variants)
+        choices += [(2, False, 2, False, False, True), (4, False, 4, True, False, True),
+                    (6, False, 4, False, False, True), (64, False, 2, True, False, True)]
+    for tx, store, occ, narrow, pair, fused in choices:
         s = solver(llg, w, llg.FP32C, steps_per_graph=4)
-        s.set_tuning(tx, store, occ, narrow, pair)
+        s.set_tuning(tx, store, occ, narrow, pair, fused)
         assert s.kernel_info()["rows_per_thread"] == (2 if pair else 1)
+        assert s.kernel_info()["fused"] == fused
         for r in range(len(w.replicas)):
             s.set_state(W.initial_state(w, r), r)
         s.step(11)
         outs.append(s.get_state(-1))
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
+
+
+def _periodic(w, per):
+    w.model.periodic = per
+    return w
+
+
+FUSED_CASES = {
+    # ragged z (33 = 32 + 1) and y tiles
+    "sc_ragged": lambda: W.sc_ferromagnet(L=(5, 7, 33), T=100.0),
+    # open along x, and along y and z
+    "sc_open_x": lambda: W.sc_ferromagnet(L=(6, 9, 35), T=100.0, periodic=(0, 1, 1)),
+    "sc_open_yz": lambda: W.sc_ferromagnet(L=(7, 5, 9), T=50.0, periodic=(1, 0, 0)),
+    # periodic axes shorter than the tile and its halo (the halo wraps more than once)
+    "bcc_tiny": lambda: W.bcc_nearest_neighbour(L=(4, 3, 3), T=500.0, start="random"),
+    "bcc3_open_z": lambda: _periodic(W.bcc_three_shell(L=(6, 9, 35), T=300.0, start="random"), (1, 1, 0)),
+    "bcc3_odd_x": lambda: W.bcc_three_shell(L=(9, 8, 40), T=300.0, start="random"),
+    "fcc_ragged": lambda: W.fcc_ferromagnet(L=(3, 5, 66), T=300.0, start="random"),
+    "fcc2_open_y": lambda: _periodic(W.fcc_ferromagnet(L=(4, 6, 33), T=300.0, J2=0.2, start="random"), (1, 0, 1)),
+    # a time-dependent applied field and zeeman ac field (stage times)
+    "bcc_pulse": lambda: pulse_cases()["bcc4_sinc_zeeman_dc_ac"],
+}
+
+
+@pytest.mark.parametrize("name", sorted(FUSED_CASES))
+def test_fused_step_equals_the_two_pass_step(llg, name):
+    """The fused Heun step (predictor of tile + halo in shared memory, then
+    the corrector in the same sweep) gives the stage kernels' states bit for
+    bit: the same operations per spin, the same Philox noise for the halo
+    cells, at open and periodic boundaries, ragged tiles and lattices smaller
+    than a tile."""
+    w = FUSED_CASES[name]()
+    ref = solver(llg, w, llg.FP32C, steps_per_graph=4)
+    assert ref.kernel_info()["family"] != "generic"
+    ref.set_tuning(4, True, 2)
+    for r in range(len(w.replicas)):
+        ref.set_state(W.initial_state(w, r), r)
+    ref.step(9)
+    want = ref.get_state(-1)
+    for tx, occ, narrow in ((2, 2, False), (4, 4, True), (64, 2, False)):
+        s = solver(llg, w, llg.FP32C, steps_per_graph=4)
+        s.set_tuning(tx, False, occ, narrow, False, True)
+        assert s.kernel_info()["fused"]
+        for r in range(len(w.replicas)):
+            s.set_state(W.initial_state(w, r), r)
+        s.step(9)
+        got = s.get_state(-1)
+        assert np.array_equal(got, want), (tx, occ, narrow, np.abs(got - want).max())
+        s.step(1)
+        assert s.last_launch_count == 1   # one kernel per step, which also advances the step counter
+        s.close()
+
+
+def test_fused_step_is_refused_where_unsupported(llg):
+    tri = W.triangular_dmi_field_sweep(L=(20, 30, 1), n_fields=1, T=5.0)
+    s = solver(llg, tri, llg.FP32C)
+    with pytest.raises(llg.LLGError, match="fused step"):
+        s.set_tuning(4, False, 2, False, False, True)
+    sc = solver(llg, W.sc_ferromagnet(L=16), llg.FP32C)
+    with pytest.raises(llg.LLGError, match="fused step"):
+        sc.set_tuning(4, True, 2, False, False, True)
 
 
 def test_two_rows_per_thread_is_refused_where_unsupported(llg):
