@@ -135,8 +135,9 @@ def kernel_name(info: dict, integ: str, stage: int, precision: str, dipole: bool
         nt = info["tile_z"] * (info["tile_y"] // rpt) * {"fcc": 4, "fcc2": 4, "bcc": 2, "bcc3": 2}.get(
             info["family"], 1)
         minb = info["occupancy"] * max(1, 256 // nt)
-        return "tiled_stage<%s, %d, %d, %d, %d, %d, %d>" % (fam, info["tile_z"], info["tile_y"], rpt, st, minb,
-                                                          1 if dipole else 0)
+        tma = 1 if info.get("tma") and st != 1 else 0
+        return "tiled_stage<%s, %d, %d, %d, %d, %d, %d, %d>" % (fam, info["tile_z"], info["tile_y"], rpt, st, minb,
+                                                              1 if dipole else 0, tma)
     suffix = "_f32" if precision == "fp32c" else "_f64"
     if integ == "heun":
         return ("heun_predict" if stage == 0 else "heun_correct") + suffix
@@ -165,7 +166,7 @@ def parse(argv=None):
     p.add_argument("--profile-steps", type=int, default=50)
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--tuning", default="", help="planes_per_cta,flags,occupancy instead of autotuning (flags: 1 stored rhs, 2 narrow tile, "
-                        "4 two rows per thread, 8 the fused Heun step)")
+                        "4 two rows per thread, 8 the fused Heun step, 256 TMA plane loads)")
     return p.parse_args(argv)
 
 
@@ -398,12 +399,12 @@ def run_reference(args, rank, world):
 
 def tiled_stem(name: str):
     """(family, tile z, tile y, stage) of a tiled_stage kernel name: template
-    arguments <F, TZ, TY, RPT, STAGE, MINB, DIP>, or <F, TZ, TY, STAGE, MINB[,
-    DIP]> in captures of the kernels before rows per thread existed."""
+    arguments <F, TZ, TY, RPT, STAGE, MINB, DIP[, TMA]>, or <F, TZ, TY, STAGE,
+    MINB[, DIP]> in captures of the kernels before rows per thread existed."""
     if not name.startswith("tiled_stage<"):
         return None
     args = [a.strip() for a in name[name.index("<") + 1:name.rindex(">")].split(",")]
-    return tuple(args[:3] + [args[4] if len(args) == 7 else args[3]])
+    return tuple(args[:3] + [args[4] if len(args) >= 7 else args[3]])
 
 
 def accuracy_vs_fp64(w, steps=1000, cap=0):
@@ -531,7 +532,7 @@ def make_solver(llg, w, prec, local, stream, tuning_arg: str = "", tune: bool = 
         sol.set_state(W.initial_state(w, r), r)
     if tuning_arg:
         tx, fl, oc = (int(v) for v in tuning_arg.split(","))
-        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2), bool(fl & 4), bool(fl & 8))
+        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2), bool(fl & 4), bool(fl & 8), bool(fl & 256))
         tuning = sol.kernel_info()
     else:
         # the choice is cached per lattice shape ($JAMS_LLG_TUNE_CACHE), so a

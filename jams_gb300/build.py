@@ -22,7 +22,8 @@ LIB = os.path.join(OUT, "libjams_llg.so")
 # checked, misses reported as LLG_ERR_BOUNDS; a library of its own
 OUT_CHECKED = os.path.join(HERE, "_build_checked")
 LIB_CHECKED = os.path.join(OUT_CHECKED, "libjams_llg.so")
-SOURCES = ["llg_kernels.cu", "llg_tiled.cu", "llg_tiled_dipole.cu", "llg_tiled_pair.cu", "llg_fused_a.cu",
+SOURCES = ["llg_kernels.cu", "llg_tiled.cu", "llg_tiled_dipole.cu", "llg_tiled_pair.cu", "llg_tiled_tma.cu",
+           "llg_tiled_tma_pair.cu", "llg_fused_a.cu",
            "llg_fused_b.cu", "llg_observe.cu", "llg_host.cu", "llg_noalloc.cu", "llg_config.cu", "llg_io.cu",
            "llg_dipole.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -13,7 +13,9 @@
 // site, class) describes the whole matrix.  For the FP64 form the entries of
 // each class are stored in ascending j, the order in which the CSR row sum
 // visits them.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <array>
@@ -165,6 +167,8 @@ struct llg_handle {
   int tz = 0, ty = 0;
   int rpt = 1;               // rows per thread of the tiled kernels (1 or 2)
   uint64_t model_hash = 0;   // the descriptor's Hamiltonian and material parameters (checkpoint fingerprint)
+  bool tma = false;          // tiled kernels: planes arrive by TMA box loads (tmaps: one per state buffer)
+  CUtensorMap tmaps[3];
   bool fused = false;        // Heun: one fused step kernel (predictor over tile + halo in shared memory)
   bool fused_wide = true;    // its wide tile (fused_rows)
   TiledParams TP{};
@@ -404,6 +408,58 @@ int build_tiles4(llg_handle* h) {
 void drop_graphs(llg_handle* h) {
   for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
   h->graphs.clear();
+}
+
+// cuTensorMapEncodeTiled, from the driver through the runtime (the library
+// links the runtime only)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// whether the tiled kernels can take their planes by TMA: one replica, a
+// family with 32-cell-wide tiles, rows whose byte stride is a multiple of
+// 16, and the driver's encoder; the reason when not
+const char* tma_unsupported(const llg_handle* h) {
+  if (!h->tiled || h->fp64) return "the tiled FP32 kernels only";
+  if (h->dipole) return "not with a dipole term";
+  if (h->reps.size() != 1) return "one replica only";
+  int lo, width, rows;
+  if (!tma_box(h->family, h->ty, &lo, &width, &rows)) return "not for this lattice family";
+  const ReplicaDev& R = h->reps[0];
+  if (R.vs[2] != h->nb || R.vs[1] != (int64_t)R.vL[2] * h->nb || (R.vs[1] * 4) % 16 != 0)
+    return "rows must be contiguous with a byte stride that is a multiple of 16";
+  if (!tensor_map_encoder()) return "the driver has no cuTensorMapEncodeTiled";
+  return nullptr;
+}
+
+// the tensor map of state buffer k: (z x basis, y, x, component) of
+// replica 0, box (width, rows, 1 plane, 3 components)
+int build_tensor_maps(llg_handle* h) {
+  int lo, width, rows;
+  tma_box(h->family, h->ty, &lo, &width, &rows);
+  const ReplicaDev& R = h->reps[0];
+  const cuuint64_t dims[4] = {(cuuint64_t)R.vL[2] * h->nb, (cuuint64_t)R.vL[1], (cuuint64_t)R.vL[0], 3};
+  const cuuint64_t strides[3] = {(cuuint64_t)R.vs[1] * 4, (cuuint64_t)R.vs[0] * 4, (cuuint64_t)h->npad * 4};
+  const cuuint32_t box[4] = {(cuuint32_t)width, (cuuint32_t)rows, 1, 3};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  for (int k = 0; k < 3; ++k) {
+    float* base = reinterpret_cast<float*>(h->state[k].p) + R.offset;
+    const CUresult r = tensor_map_encoder()(&h->tmaps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box,
+                                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return h->fail(LLG_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  }
+  return 0;
 }
 
 // FNV-1a over the values that define a model's physics besides the lattice
@@ -1148,19 +1204,23 @@ bool launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
     if (h->integrator == LLG_HEUN) {
       float* s0 = buf<float>(h, cur);
       float* sp = buf<float>(h, 1);
+      // TMA: the tensor map of the buffer the stage gathers from
+      const CUtensorMap* m0 = h->tma ? &h->tmaps[cur] : nullptr;
+      const CUtensorMap* m1 = h->tma ? &h->tmaps[1] : nullptr;
       if (stage == 0)
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, advance, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, advance, h->dipole != nullptr, m0);
       else if (h->store_mode)
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks, advance, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks, advance, h->dipole != nullptr, m1);
       else
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, advance, h->dipole != nullptr);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, advance, h->dipole != nullptr, m1);
     } else {
       float* s0 = buf<float>(h, 0);
       float* a = buf<float>(h, 1);
       float* b = buf<float>(h, 2);
       float* in = stage == 0 ? s0 : (stage == 2 ? b : a);
       float* out = stage == 0 ? a : (stage == 1 ? b : (stage == 2 ? a : s0));
-      launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, advance, h->dipole != nullptr);
+      const CUtensorMap* m = h->tma ? &h->tmaps[stage == 0 ? 0 : (stage == 2 ? 2 : 1)] : nullptr;
+      launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, advance, h->dipole != nullptr, m);
     }
     return true;
   }
@@ -1381,7 +1441,7 @@ static int step_blocks(llg_handle* h, int32_t nsteps) {
   while (remaining > 0) {
     const int n = remaining >= K && K > 1 ? K : remaining;
     GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX + 8192 * h->ty +
-                     131072 * h->rpt + 524288 * (h->fused ? 1 : 0),
+                     131072 * h->rpt + 524288 * (h->fused ? 1 : 0) + 1048576 * (h->tma ? 1 : 0),
                  n};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end() && (n == K || h->graphs.size() < kMaxGraphs)) {
@@ -1690,6 +1750,7 @@ int llg_kernel_info(const llg_handle* h, int32_t* info) {
   info[6] = h->occupancy;
   info[7] = h->tiled ? h->rpt : 0;
   info[8] = h->fused ? 1 : 0;
+  info[9] = h->tma ? 1 : 0;
   return 0;
 }
 
@@ -1697,7 +1758,7 @@ static std::string tuning_key(const llg_handle* h) {
   cudaDeviceProp prop;
   cudaGetDeviceProperties(&prop, h->device);
   std::string k = std::string(prop.name) + "|fam" + std::to_string(h->family) + "|int" +
-                  std::to_string(h->integrator) + "|nb" + std::to_string(h->nb) + "|nt" + std::to_string(h->nterms) + "|k3";
+                  std::to_string(h->integrator) + "|nb" + std::to_string(h->nb) + "|nt" + std::to_string(h->nterms) + "|k4";
   for (auto& R : h->reps)
     k += "|" + std::to_string(R.L[0]) + "x" + std::to_string(R.L[1]) + "x" + std::to_string(R.L[2]) +
          (R.thermal ? "T" : "0");
@@ -1768,7 +1829,10 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
   h->fused = fused;
   h->fused_wide = (store_rhs & 2) == 0;
   h->store_mode = (store_rhs & 1) != 0 && h->integrator == LLG_HEUN;
-  const int occ = store_rhs >> 4;
+  // bit 8: TMA plane loads (the two-pass tiled kernels)
+  const bool tma = (store_rhs & 256) != 0;
+  if (tma && fused) return h->fail(LLG_ERR_BAD_DESC, "TMA plane loads: the two-pass tiled kernels only");
+  const int occ = (store_rhs >> 4) & 7;
   h->occupancy = occ >= 4 ? 4 : (occ == 3 ? 3 : 2);
   if (pair) h->occupancy = 2;   // two rows per thread need up to 128 registers
   h->rpt = pair ? 2 : 1;
@@ -1783,6 +1847,14 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
     h->TP.TX = planes_per_cta;
     int rc = build_tiles4(h);
     if (rc) return rc;
+  }
+  h->tma = false;
+  if (tma) {
+    const char* why = tma_unsupported(h);
+    if (why) return h->fail(LLG_ERR_BAD_DESC, "TMA plane loads: %s", why);
+    int rc = build_tensor_maps(h);
+    if (rc) return rc;
+    h->tma = true;
   }
   return 0;
 }
@@ -1878,6 +1950,19 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
             if (h->integrator == LLG_HEUN) cands.push_back({t, 5 | (occ << 4)});
           }
         }
+  // TMA plane loads: the same tilings again (where supported: the tile
+  // rows of a candidate decide the box)
+  {
+    const size_t n0 = cands.size();
+    const int ty0 = h->ty;
+    for (size_t c = 0; c < n0; ++c) {
+      int wide_tz = 0, wide_ty = 0;
+      tiled_geometry(h->family, &wide_tz, &wide_ty);
+      h->ty = (cands[c].second & 2) ? narrow_tile_rows(h->family) : wide_ty;
+      if (!tma_unsupported(h)) cands.push_back({cands[c].first, cands[c].second | 256});
+    }
+    h->ty = ty0;
+  }
   // the fused Heun step: wide or narrow tile, occupancy 2 or 4 (x 256 threads)
   if (h->integrator == LLG_HEUN && fused_supported(h->family) && !h->dipole)
     for (int t : {2, 4, 8, 16, 32, 64})
@@ -1895,7 +1980,8 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   tiled_geometry(h->family, &wide_tz0, &wide_ty0);
   std::pair<int, int> choice = {h->TP.TX, h->fused ? (8 | (h->fused_wide ? 0 : 2) | (h->occupancy << 4))
                                                    : ((h->store_mode ? 1 : 0) | (h->ty != wide_ty0 ? 2 : 0) |
-                                                      (h->rpt == 2 ? 4 : 0) | (h->occupancy << 4))};
+                                                      (h->rpt == 2 ? 4 : 0) | (h->occupancy << 4) |
+                                                      (h->tma ? 256 : 0))};
   // each trial runs as llg_step runs steps: one CUDA graph of trial_steps
   // steps (captured and run once untimed, then timed)
   const int spg0 = h->steps_per_graph;

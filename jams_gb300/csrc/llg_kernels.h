@@ -1,6 +1,7 @@
 // Declarations of the kernels in llg_kernels.cu, launched by llg_host.cu.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "llg_internal.h"
@@ -54,19 +55,22 @@ void tiled_geometry(int family, int* tz, int* ty);
 // a family that pair_rows_supported, without a dipole term)
 int narrow_tile_rows(int family);
 bool pair_rows_supported(int family);
+// map: the tensor map of the gathered buffer for TMA plane loads (null:
+// planes staged through registers); tma_box gives its box geometry
 cudaError_t launch_tiled(int family, int ty, int rpt, int occupancy, int stage, unsigned grid, cudaStream_t st,
                          const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
-                         float* aux, uint32_t k, uint32_t advance, bool dipole);
+                         float* aux, uint32_t k, uint32_t advance, bool dipole, const CUtensorMap* map);
+bool tma_box(int family, int ty, int* lo, int* width, int* rows);
 // fused Heun step (llg_fused.cuh, instantiated by llg_fused_a.cu and
 // llg_fused_b.cu): one launch per step, s0 -> s1; tile rows fused_rows()
 bool fused_supported(int family);
 int fused_rows(int family, bool wide);
 cudaError_t launch_fused(int family, bool wide, int occupancy, unsigned grid, cudaStream_t st, const Params& P,
                          const TiledParams& TP, const float* s0, float* s1, uint32_t k, uint32_t adv);
-template <bool DIP, int RPT>
+template <bool DIP, int RPT, bool TMA>
 cudaError_t launch_tiled_t(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
                            const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
-                           float* aux, uint32_t k, uint32_t adv);
+                           float* aux, uint32_t k, uint32_t adv, const CUtensorMap* map);
 
 // observables (llg_observe.cu): ordered per-tile partial sums copied to
 // h_partials [ntiles][nq] = (sum mu_s Sx, Sy, Sz, sum mu_s, E_term...)

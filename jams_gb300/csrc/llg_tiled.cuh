@@ -16,6 +16,8 @@
 // Warps are laid out along Z (32 consecutive cells) with the basis site
 // uniform per warp, so the per-basis stencil never diverges.
 #pragma once
+#include <cuda.h>
+
 #include <cstdint>
 #include <utility>
 
@@ -622,6 +624,157 @@ __device__ __forceinline__ void store_plane(const Params& P, float4* ring, int x
       slot[fp.dst[q]] = make_float4(pr.v[q][0], pr.v[q][1], pr.v[q][2], 0.f);
 }
 
+// ------------------------------------------------------ TMA plane fetch --
+// The plane x + 2 can instead arrive by TMA: one thread issues a
+// cp.async.bulk.tensor box load (the plane's rows y0 - RY .. y0 + TY + RY - 1,
+// the three components as a fourth dimension) into one of two staging
+// buffers, completion is counted on an mbarrier, and the threads transpose
+// the box (one float per component) into the float4 ring.  Coordinates
+// outside the lattice read zeros (open boundaries); positions that wrap
+// around a periodic y or z boundary are read from global memory instead.
+// The box starts on a 16-byte boundary: LO elements before z0 - RZ.
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// waits for phase `parity` of the mbarrier for at most about a second of
+// wall time (a poll may suspend the thread for a while); false when it gave up
+constexpr uint64_t kTmaWaitNs = 1000000000ull;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (global_ns() - t0 < kTmaWaitNs)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+template <class F, int TZ, int TY>
+struct TmaGeo {
+  static constexpr int NB = F::NB, RY = F::RY, RZ = F::RZ;
+  static constexpr int LO = (RZ * NB) % 4 == 0 ? 0 : 4 - (RZ * NB) % 4;
+  static constexpr int BW = ((TZ + 2 * RZ) * NB + LO + 3) / 4 * 4;   // box width, elements
+  static constexpr int ROWS = TY + 2 * RY;
+  static constexpr int STG = 3 * ROWS * BW;                         // floats of one box
+  static constexpr int STG_PAD = (STG * 4 + 127) / 128 * 128;       // bytes of one staging buffer
+  static constexpr bool FITS = BW <= 256 && ROWS <= 256;            // TMA box dimensions are at most 256
+};
+
+// per thread: the ring positions it transposes (ring order, idx = tid + q
+// NT) and where each comes from: >= 0 the box offset of component 0, < 0
+// -(spin index in the plane) - 1 of a periodic image read from global memory
+template <class F, int TZ, int TY, int RPT>
+struct TmaPlan {
+  int src[Geo<F, TZ, TY, RPT>::PER_THREAD];
+};
+
+template <class F, int TZ, int TY, int RPT>
+__device__ __forceinline__ void plan_tma(const View& V, int y0, int z0, int tid, TmaPlan<F, TZ, TY, RPT>& tp) {
+  using G = Geo<F, TZ, TY, RPT>;
+  using T = TmaGeo<F, TZ, TY>;
+#pragma unroll
+  for (int q = 0; q < G::PER_THREAD; ++q) {
+    const int idx = tid + q * G::NT;
+    const int zz = idx % G::PZ;
+    const int yy = (idx / G::PZ) % G::PY;
+    const int bb = idx / (G::PZ * G::PY);
+    const int cy = y0 - F::RY + yy, cz = z0 - F::RZ + zz;
+    const bool inside = cy >= 0 && cy < V.L[1] && cz >= 0 && cz < V.L[2];
+    int src = yy * T::BW + zz * G::NB + bb + T::LO;
+    if (!inside && idx < G::PLANE) {
+      // a periodic image comes from global memory; a position outside an
+      // open boundary keeps the box's zero
+      bool valid = true;
+      const int gy = wrap_sel(cy, V.L[1], V.per[1], valid);
+      const int gz = wrap_sel(cz, V.L[2], V.per[2], valid);
+      if (valid) src = -(gy * (int)V.st[1] + gz * (int)V.st[2] + bb) - 1;
+    }
+    tp.src[q] = src;
+  }
+}
+
+// the box of plane x (staging buffer `stg`) into ring slot x & 3
+template <class F, int TZ, int TY, int RPT>
+__device__ __forceinline__ void transpose_plane(const Params& P, const View& V, const float* __restrict__ s,
+                                                int x, const float* stg, float4* ring, const TmaPlan<F, TZ, TY, RPT>& tp) {
+  using G = Geo<F, TZ, TY, RPT>;
+  using T = TmaGeo<F, TZ, TY>;
+  bool xvalid = true;
+  const int gx = wrap_sel(x, V.L[0], V.per[0], xvalid);
+  const float* sx = s + V.offset + (int64_t)gx * V.st[0];
+  float4* slot = ring + (x & 3) * G::PLANE;
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+#pragma unroll
+  for (int q = 0; q < G::PER_THREAD; ++q) {
+    const int idx = tid + q * G::NT;
+    if (idx < G::PLANE) {
+      const int src = tp.src[q];
+      float4 v;
+      if (src >= 0) {
+        const bool ok = LLG_IN_RANGE(P, src + 2 * T::ROWS * T::BW, 0, T::STG);
+        v = ok ? make_float4(stg[src], stg[src + T::ROWS * T::BW], stg[src + 2 * T::ROWS * T::BW], 0.f)
+               : make_float4(0.f, 0.f, 0.f, 0.f);
+      } else {
+        const int i = -src - 1;
+        const bool ok = xvalid && LLG_IN_RANGE(P, (int64_t)gx * V.st[0] + i, 0, (int64_t)V.L[0] * V.st[0]);
+        v = ok ? make_float4(__ldg(sx + i), __ldg(sx + P.npad + i), __ldg(sx + 2 * P.npad + i), 0.f)
+               : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      slot[idx] = v;
+    }
+  }
+}
+
+// one thread: the box of plane x into staging buffer x & 1
+template <class F, int TZ, int TY>
+__device__ __forceinline__ void issue_plane(const CUtensorMap* map, const View& V, int x, int y0, int z0,
+                                            unsigned char* stg_base, uint64_t* bars) {
+  using T = TmaGeo<F, TZ, TY>;
+  bool xvalid = true;
+  const int gx = wrap_sel(x, V.L[0], V.per[0], xvalid);
+  const int k = x & 1;
+  // the threads' reads of this buffer (generic proxy) come before the TMA
+  // write (async proxy) that overwrites it
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  mbar_expect_tx(&bars[k], (uint32_t)(T::STG * 4));
+  // a plane outside an open x boundary: a plane coordinate out of range reads zeros
+  tma_load_4d(stg_base + k * T::STG_PAD, map, &bars[k], (z0 - F::RZ) * F::NB - T::LO, y0 - F::RY,
+              xvalid ? gx : -1, 0);
+}
+
 }  // namespace
 
 // STAGE: 0 Heun predictor (writes sp; with aux != null also rhs0 into aux)
@@ -633,17 +786,29 @@ __device__ __forceinline__ void store_plane(const Params& P, float4* ring, int x
 // (loop, addresses, fetch bookkeeping, barrier) is shared by two spins and
 // the two rows' neighbour loads overlap; each spin's arithmetic is the same
 // as with RPT = 1, so the results agree bit for bit.
-template <class F, int TZ, int TY, int RPT, int STAGE, int MINB, bool DIP>
+// TMA: the gathered state's planes arrive by TMA box loads (tmap: the
+// tensor map of the buffer the stage gathers from); one ring only, so STAGE 1
+// (two rings) always stages through registers.
+template <class F, int TZ, int TY, int RPT, int STAGE, int MINB, bool DIP, bool TMA>
 __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     tiled_stage(const __grid_constant__ Params P, const __grid_constant__ TiledParams TP, const float* s0,
-                const float* sin, float* out, float* aux, uint32_t kstep, uint32_t advance) {
+                const float* sin, float* out, float* aux, uint32_t kstep, uint32_t advance,
+                const __grid_constant__ CUtensorMap tmap) {
   using G = Geo<F, TZ, TY, RPT>;
   constexpr int NR = STAGE == 1 ? 2 : 1;
   constexpr int TYT = TY / RPT;   // thread rows per basis site
+  constexpr bool USE_TMA = TMA && NR == 1;
   static_assert(TY % RPT == 0, "rows per thread must divide the tile rows");
-  extern __shared__ float4 smem[];
-  float4* ring0 = smem;                    // ring of the gathered state
-  float4* ring1 = smem + 4 * G::PLANE;     // second ring (s0) for STAGE 1
+  static_assert(!USE_TMA || TmaGeo<F, TZ, TY>::FITS, "TMA box dimensions are at most 256");
+  extern __shared__ __align__(128) float4 smem[];
+  // TMA: two staging buffers on a 128-byte boundary, then the ring, then the
+  // two mbarriers
+  unsigned char* sbase = reinterpret_cast<unsigned char*>(smem);
+  if constexpr (USE_TMA) sbase += (128u - (smem_u32(smem) & 127u)) & 127u;
+  float4* ring0 = USE_TMA ? reinterpret_cast<float4*>(sbase + 2 * TmaGeo<F, TZ, TY>::STG_PAD) : smem;
+  float4* ring1 = ring0 + 4 * G::PLANE;    // second ring (s0) for STAGE 1
+  uint64_t* bars = reinterpret_cast<uint64_t*>(ring0 + NR * 4 * G::PLANE);
+  __shared__ int s_abort;   // a TMA wait gave up: every thread leaves the plane loop
   // programmatic dependent launch: the next stage's CTAs may be scheduled
   // once every CTA of this one has started; they set up, then wait for this
   // launch to complete before they read what it wrote
@@ -688,9 +853,21 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   const float* s0x = s0 + V.offset;
   const float* s0y = s0x + P.npad;
   const float* s0z = s0y + P.npad;
-  const int xe = min(x0 + TP.TX, V.L[0]);
+  int xe = min(x0 + TP.TX, V.L[0]);
   FetchPlan<F, TZ, TY, RPT> fp;
-  plan_fetch<F, TZ, TY, RPT>(V, y0, z0, tid, fp);
+  TmaPlan<F, TZ, TY, RPT> tp;
+  if constexpr (USE_TMA) {
+    plan_tma<F, TZ, TY, RPT>(V, y0, z0, tid, tp);
+    if (tid == 0) {
+      mbar_init(&bars[0], 1);
+      mbar_init(&bars[1], 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      s_abort = 0;
+    }
+    __syncthreads();
+  } else {
+    plan_fetch<F, TZ, TY, RPT>(V, y0, z0, tid, fp);
+  }
   // everything below reads the output of earlier launches (spins, stored
   // rhs, dipole field, step counter): wait for them to complete (returns at
   // once for a launch without a programmatic dependency)
@@ -703,7 +880,39 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   float hb0[3] = {0.f, 0.f, 0.f};
   if (STAGE == 1) field_terms_hb(P, R, b, pulse_at32(P, step, 0), hb0);
 
-  {
+  // TMA: planes x are waited for in order; bit k of `phase` is the parity
+  // of the next completion of staging buffer k; thread 0 counts the planes it
+  // issued and waited for
+  uint32_t phase = 0;
+  int issued = 0, waited = 0;
+  auto wait_transpose = [&](int x) {
+    if constexpr (USE_TMA) {
+      const int k = x & 1;
+      if (!mbar_wait(&bars[k], (phase >> k) & 1u)) s_abort = 1;
+      phase ^= 1u << k;
+      ++waited;
+      transpose_plane<F, TZ, TY, RPT>(P, V, gather_src, x,
+                                      reinterpret_cast<const float*>(sbase + k * TmaGeo<F, TZ, TY>::STG_PAD), ring0, tp);
+    }
+  };
+  auto issue = [&](int x) {
+    if constexpr (USE_TMA) {
+      if (tid == 0) {
+        issue_plane<F, TZ, TY>(&tmap, V, x, y0, z0, sbase, bars);
+        ++issued;
+      }
+    }
+  };
+  if constexpr (USE_TMA) {
+    issue(x0 - 1);
+    issue(x0);
+    wait_transpose(x0 - 1);
+    wait_transpose(x0);
+    __syncthreads();   // both staging buffers read
+    issue(x0 + 1);
+    if (x0 + 2 <= xe) issue(x0 + 2);
+    wait_transpose(x0 + 1);
+  } else {
     PlaneRegs<F, TZ, TY, RPT> pr;
 #pragma unroll
     for (int d = -1; d <= 1; ++d) {
@@ -716,6 +925,9 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     }
   }
   __syncthreads();
+  if constexpr (USE_TMA) {
+    if (s_abort) xe = x0;   // every thread skips the plane loop
+  }
   // carried partial sums of the separable stencils (ring1: s0 of STAGE 1)
   Carry cy0[RPT], cy1[RPT];
 #pragma unroll
@@ -732,7 +944,11 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   for (int x = x0; x < xe; ++x) {
     const bool more = x + 1 < xe;
     PlaneRegs<F, TZ, TY, RPT> pf0, pf1;
-    if (more) {
+    if constexpr (USE_TMA) {
+      // plane x + 3 into the staging buffer plane x + 1 left (read before
+      // the last barrier); plane x + 2 is already on its way
+      if (x + 3 <= xe) issue(x + 3);
+    } else if (more) {
       fetch_plane<F, TZ, TY, RPT>(P, V, gather_src, P.npad, x + 2, fp, pf0);
       if (NR == 2) fetch_plane<F, TZ, TY, RPT>(P, V, s0, P.npad, x + 2, fp, pf1);
     }
@@ -855,11 +1071,25 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
         }
       }
     }
-    if (more) {
+    if constexpr (USE_TMA) {
+      if (more) wait_transpose(x + 2);
+    } else if (more) {
       store_plane<F, TZ, TY, RPT>(P, ring0, x + 2, fp, pf0);
       if (NR == 2) store_plane<F, TZ, TY, RPT>(P, ring1, x + 2, fp, pf1);
     }
     __syncthreads();
+    if constexpr (USE_TMA) {
+      if (s_abort) break;   // read after the barrier: the same in every thread
+    }
+  }
+  if constexpr (USE_TMA) {
+    if (s_abort && tid == 0) {
+      // report, and let the copies still in flight land (bounded) before the
+      // CTA's shared memory is released
+      atomicOr(P.status, 4u);
+      for (int x = x0 - 1 + waited; waited < issued; ++x, ++waited)
+        mbar_wait(&bars[x & 1], (phase >> (x & 1)) & 1u), phase ^= 1u << (x & 1);
+    }
   }
   // the launch that ends a block of steps advances the noise step counter by
   // `advance`: the last CTA to finish does it, when every CTA has read the
@@ -879,55 +1109,66 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
 namespace {
 
 template <class F, int TZ, int TY>
-size_t smem_bytes(int stage) {
-  return (size_t)(stage == 1 ? 2 : 1) * 4 * Geo<F, TZ, TY>::PLANE * sizeof(float4);
+size_t smem_bytes(int stage, bool tma) {
+  const size_t rings = (size_t)(stage == 1 ? 2 : 1) * 4 * Geo<F, TZ, TY>::PLANE * sizeof(float4);
+  // TMA (one ring): alignment slack, two staging buffers, two mbarriers
+  return tma && stage != 1 ? rings + 128 + 2 * (size_t)TmaGeo<F, TZ, TY>::STG_PAD + 16 : rings;
 }
 
-template <class F, int TZ, int TY, int RPT, int STAGE, int MINB, bool DIP>
+template <class F, int TZ, int TY, int RPT, int STAGE, int MINB, bool DIP, bool TMA>
 cudaError_t launch_one(unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP, const float* s0,
-                       const float* sin, float* out, float* aux, uint32_t k, uint32_t adv) {
-  const size_t sm = smem_bytes<F, TZ, TY>(STAGE);
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tiled_stage<F, TZ, TY, RPT, STAGE, MINB, DIP>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    attr = true;
+                       const float* sin, float* out, float* aux, uint32_t k, uint32_t adv, const CUtensorMap* map) {
+  if constexpr (TMA && STAGE == 1) {
+    // two rings: the register-staged kernel
+    return launch_one<F, TZ, TY, RPT, STAGE, MINB, DIP, false>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+  } else {
+    const size_t sm = smem_bytes<F, TZ, TY>(STAGE, TMA);
+    static bool attr = false;
+    if (!attr) {
+      cudaError_t e = cudaFuncSetAttribute(tiled_stage<F, TZ, TY, RPT, STAGE, MINB, DIP, TMA>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+    if (TMA && !map) return cudaErrorInvalidValue;
+    CUtensorMap none{};
+    // launched with programmatic stream serialisation: its setup overlaps the
+    // end of the previous kernel in the stream (CUDA graphs keep the
+    // programmatic edge)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(TZ, (TY / RPT) * F::NB);
+    cfg.dynamicSmemBytes = sm;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, tiled_stage<F, TZ, TY, RPT, STAGE, MINB, DIP, TMA>, P, TP, s0, sin, out, aux, k,
+                              adv, TMA ? *map : none);
   }
-  // launched with programmatic stream serialisation: its setup overlaps the
-  // end of the previous kernel in the stream (CUDA graphs keep the
-  // programmatic edge)
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(TZ, (TY / RPT) * F::NB);
-  cfg.dynamicSmemBytes = sm;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, tiled_stage<F, TZ, TY, RPT, STAGE, MINB, DIP>, P, TP, s0, sin, out, aux, k, adv);
 }
 
-template <class F, int TZ, int TY, int RPT, int MINB, bool DIP>
+template <class F, int TZ, int TY, int RPT, int MINB, bool DIP, bool TMA>
 cudaError_t launch_family(int stage, unsigned grid, cudaStream_t st, const Params& P, const TiledParams& TP,
-                          const float* s0, const float* sin, float* out, float* aux, uint32_t k, uint32_t adv) {
+                          const float* s0, const float* sin, float* out, float* aux, uint32_t k, uint32_t adv,
+                          const CUtensorMap* map) {
   switch (stage) {
-    case 0: return launch_one<F, TZ, TY, RPT, 0, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
-    case 1: return launch_one<F, TZ, TY, RPT, 1, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
-    case 2: return launch_one<F, TZ, TY, RPT, 2, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
-    case 3: return launch_one<F, TZ, TY, RPT, 3, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
-    case 4: return launch_one<F, TZ, TY, RPT, 4, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
-    case 5: return launch_one<F, TZ, TY, RPT, 5, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
-    default: return launch_one<F, TZ, TY, RPT, 6, MINB, DIP>(grid, st, P, TP, s0, sin, out, aux, k, adv);
+    case 0: return launch_one<F, TZ, TY, RPT, 0, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+    case 1: return launch_one<F, TZ, TY, RPT, 1, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+    case 2: return launch_one<F, TZ, TY, RPT, 2, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+    case 3: return launch_one<F, TZ, TY, RPT, 3, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+    case 4: return launch_one<F, TZ, TY, RPT, 4, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+    case 5: return launch_one<F, TZ, TY, RPT, 5, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+    default: return launch_one<F, TZ, TY, RPT, 6, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
   }
 }
 
-template <class F, int TZ, int TY, int RPT, bool DIP>
+template <class F, int TZ, int TY, int RPT, bool DIP, bool TMA>
 cudaError_t launch_occ(int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
                        const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux, uint32_t k,
-                       uint32_t adv) {
+                       uint32_t adv, const CUtensorMap* map) {
   // occupancy variant, as the resident threads of 2, 3 or 4 CTAs of 256
   // threads (up to 128, 80 or 64 registers per thread); CTAs of 128 threads
   // (narrow tiles, two rows per thread) run twice as many per SM with the
@@ -935,60 +1176,68 @@ cudaError_t launch_occ(int occupancy, int stage, unsigned grid, cudaStream_t st,
   // they run at occupancy 2 only.
   constexpr int S = 256 / Geo<F, TZ, TY, RPT>::NT > 1 ? 256 / Geo<F, TZ, TY, RPT>::NT : 1;
   if constexpr (RPT == 1) {
-    if (occupancy >= 4) return launch_family<F, TZ, TY, 1, 4 * S, DIP>
-        (stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
-    if (occupancy == 3) return launch_family<F, TZ, TY, 1, 3 * S, DIP>
-        (stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+    if (occupancy >= 4) return launch_family<F, TZ, TY, 1, 4 * S, DIP, TMA>
+        (stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+    if (occupancy == 3) return launch_family<F, TZ, TY, 1, 3 * S, DIP, TMA>
+        (stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
   }
-  return launch_family<F, TZ, TY, RPT, 2 * S, DIP>(stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+  return launch_family<F, TZ, TY, RPT, 2 * S, DIP, TMA>(stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
 }
 
 }  // namespace
 
 // the tiled stage kernels with (DIP) or without the dipole field planes, one
-// (RPT = 1) or two rows per thread; llg_tiled.cu instantiates <false, 1>,
-// llg_tiled_dipole.cu <true, 1> and llg_tiled_pair.cu <false, 2>.
+// (RPT = 1) or two rows per thread, planes staged through registers or by
+// TMA (TMA); llg_tiled.cu instantiates <false, 1, false>, llg_tiled_dipole.cu
+// <true, 1, false>, llg_tiled_pair.cu <false, 2, false>, llg_tiled_tma.cu
+// <false, 1, true> and llg_tiled_tma_pair.cu <false, 2, true>.
 // ty: rows of the CTA tile, the family's wide tile or, for simple cubic,
 // the narrow one (half the rows: twice the CTAs, for small lattices; the
 // bcc narrow tile measured slower at 64^3 and 256^3, its halo rows cost more
 // than the extra CTAs gain).  Two rows per thread: the wide tiles of the
-// families with at least two rows (not triangular).
-template <bool DIP, int RPT>
+// families with at least two rows (not triangular).  TMA: the 32-cell-wide
+// tiles (not triangular); map is the tensor map of the gathered buffer.
+template <bool DIP, int RPT, bool TMA>
 cudaError_t launch_tiled_t(int family, int ty, int occupancy, int stage, unsigned grid, cudaStream_t st,
                            const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
-                           float* aux, uint32_t k, uint32_t adv) {
+                           float* aux, uint32_t k, uint32_t adv, const CUtensorMap* map) {
   if constexpr (RPT == 1) {
     switch (family) {
       case kFamSC:
-        return ty == 4 ? launch_occ<FamSC, 32, 4, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k,
-                                                          adv)
-                       : launch_occ<FamSC, 32, 8, 1, DIP>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k,
-                                                          adv);
-      case kFamBCC: return launch_occ<FamBCC, 32, 4, 1, DIP>
-          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
-      case kFamBCC3: return launch_occ<FamBCC3, 32, 4, 1, DIP>
-          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
-      case kFamTRI: return launch_occ<FamTRI, 256, 1, 1, DIP>
-          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
-      case kFamFCC: return launch_occ<FamFCC, 32, 2, 1, DIP>
-          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
-      case kFamFCC2: return launch_occ<FamFCC2, 32, 2, 1, DIP>
-          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+        return ty == 4 ? launch_occ<FamSC, 32, 4, 1, DIP, TMA>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux,
+                                                               k, adv, map)
+                       : launch_occ<FamSC, 32, 8, 1, DIP, TMA>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux,
+                                                               k, adv, map);
+      case kFamBCC: return launch_occ<FamBCC, 32, 4, 1, DIP, TMA>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+      case kFamBCC3: return launch_occ<FamBCC3, 32, 4, 1, DIP, TMA>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+      case kFamTRI:
+        if constexpr (TMA) {
+          return cudaErrorInvalidValue;
+        } else {
+          return launch_occ<FamTRI, 256, 1, 1, DIP, false>(occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k,
+                                                           adv, map);
+        }
+      case kFamFCC: return launch_occ<FamFCC, 32, 2, 1, DIP, TMA>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+      case kFamFCC2: return launch_occ<FamFCC2, 32, 2, 1, DIP, TMA>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
       default: return cudaErrorInvalidValue;
     }
   } else {
     if (ty != 8 && family == kFamSC) return cudaErrorInvalidValue;
     switch (family) {
-      case kFamSC: return launch_occ<FamSC, 32, 8, RPT, DIP>
-          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
-      case kFamBCC: return launch_occ<FamBCC, 32, 4, RPT, DIP>
-          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
-      case kFamBCC3: return launch_occ<FamBCC3, 32, 4, RPT, DIP>
-          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
-      case kFamFCC: return launch_occ<FamFCC, 32, 2, RPT, DIP>
-          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
-      case kFamFCC2: return launch_occ<FamFCC2, 32, 2, RPT, DIP>
-          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv);
+      case kFamSC: return launch_occ<FamSC, 32, 8, RPT, DIP, TMA>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+      case kFamBCC: return launch_occ<FamBCC, 32, 4, RPT, DIP, TMA>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+      case kFamBCC3: return launch_occ<FamBCC3, 32, 4, RPT, DIP, TMA>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+      case kFamFCC: return launch_occ<FamFCC, 32, 2, RPT, DIP, TMA>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+      case kFamFCC2: return launch_occ<FamFCC2, 32, 2, RPT, DIP, TMA>
+          (occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, adv, map);
       default: return cudaErrorInvalidValue;
     }
   }

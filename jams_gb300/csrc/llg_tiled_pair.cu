@@ -5,8 +5,8 @@
 
 namespace jams_llg {
 
-template cudaError_t launch_tiled_t<false, 2>(int, int, int, int, unsigned, cudaStream_t, const Params&,
-                                              const TiledParams&, const float*, const float*, float*, float*,
-                                              uint32_t, uint32_t);
+template cudaError_t launch_tiled_t<false, 2, false>(int, int, int, int, unsigned, cudaStream_t, const Params&,
+                                                     const TiledParams&, const float*, const float*, float*, float*,
+                                                     uint32_t, uint32_t, const CUtensorMap*);
 
 }  // namespace jams_llg

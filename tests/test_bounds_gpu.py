@@ -54,6 +54,13 @@ CASES = {
     "sc_open_fused_narrow": (_open_sc, "FP32C", (4, False, 4, True, False, True)),
     "fcc_fused": (lambda: W.fcc_ferromagnet(L=(3, 4, 5), T=300.0, start="random"), "FP32C",
                   (2, False, 2, False, False, True)),
+    # planes loaded by TMA: stored rhs, two rows per thread, open axes
+    "bcc3_tma": (lambda: W.bcc_three_shell(L=(5, 6, 36), T=300.0, start="random"), "FP32C",
+                 (2, True, 4, False, False, False, True)),
+    "bcc3_tma_pair": (lambda: W.bcc_three_shell(L=(5, 6, 36), T=300.0, start="random"), "FP32C",
+                      (4, True, 2, False, True, False, True)),
+    "sc_open_tma": (lambda: W.sc_ferromagnet(L=(7, 5, 12), T=50.0, periodic=(0, 1, 0)), "FP32C",
+                    (2, True, 4, True, False, False, True)),
 }
 
 

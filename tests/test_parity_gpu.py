@@ -315,11 +315,18 @@ def test_tiling_choices_give_identical_results(llg, name):
         # the fused step (wide and narrow tiles, both occupancy variants)
         choices += [(2, False, 2, False, False, True), (4, False, 4, True, False, True),
                     (6, False, 4, False, False, True), (64, False, 2, True, False, True)]
-    for tx, store, occ, narrow, pair, fused in choices:
+    choices = [c + (False,) for c in choices]
+    if name != "tri" and len(w.replicas) == 1:
+        # planes loaded by TMA: stored and recomputed rhs, one and two rows
+        choices += [(2, True, 4, False, False, False, True), (4, False, 2, False, False, False, True),
+                    (6, True, 3, True, False, False, True), (4, True, 2, False, True, False, True),
+                    (64, True, 2, False, False, False, True)]
+    for tx, store, occ, narrow, pair, fused, tma in choices:
         s = solver(llg, w, llg.FP32C, steps_per_graph=4)
-        s.set_tuning(tx, store, occ, narrow, pair, fused)
+        s.set_tuning(tx, store, occ, narrow, pair, fused, tma)
         assert s.kernel_info()["rows_per_thread"] == (2 if pair else 1)
         assert s.kernel_info()["fused"] == fused
+        assert s.kernel_info()["tma"] == tma
         for r in range(len(w.replicas)):
             s.set_state(W.initial_state(w, r), r)
         s.step(11)
@@ -377,6 +384,55 @@ def test_fused_step_equals_the_two_pass_step(llg, name):
         s.step(1)
         assert s.last_launch_count == 1   # one kernel per step, which also advances the step counter
         s.close()
+
+
+# TMA rows: the contiguous row (z cells x basis sites) a multiple of 16 bytes
+TMA_CASES = {
+    "sc_ragged": lambda: W.sc_ferromagnet(L=(5, 7, 36), T=100.0),
+    "sc_open_x": lambda: W.sc_ferromagnet(L=(6, 9, 40), T=100.0, periodic=(0, 1, 1)),
+    "sc_open_yz": lambda: W.sc_ferromagnet(L=(7, 5, 12), T=50.0, periodic=(1, 0, 0)),
+    "bcc_tiny": lambda: W.bcc_nearest_neighbour(L=(4, 3, 4), T=500.0, start="random"),
+    "bcc3_open_z": lambda: _periodic(W.bcc_three_shell(L=(6, 9, 34), T=300.0, start="random"), (1, 1, 0)),
+    "bcc3_odd_x": lambda: W.bcc_three_shell(L=(9, 8, 40), T=300.0, start="random"),
+    "fcc_ragged": lambda: W.fcc_ferromagnet(L=(3, 5, 66), T=300.0, start="random"),
+    "fcc2_open_y": lambda: _periodic(W.fcc_ferromagnet(L=(4, 6, 33), T=300.0, J2=0.2, start="random"), (1, 0, 1)),
+    "bcc_pulse": lambda: pulse_cases()["bcc4_sinc_zeeman_dc_ac"],
+}
+
+
+@pytest.mark.parametrize("name", sorted(TMA_CASES))
+def test_tma_plane_loads_equal_register_staging(llg, name):
+    """The stage kernels with planes loaded by TMA box loads (zeros outside
+    open boundaries, periodic images read from global memory) give the
+    register-staged kernels' states bit for bit, Heun and RK4."""
+    w = TMA_CASES[name]()
+    for integ in (W.HEUN, W.RK4):
+        w.model.integrator = integ
+        outs = []
+        for tma in (False, True):
+            for tx, store, occ in ((2, True, 4), (4, False, 2), (64, True, 2)):
+                s = solver(llg, w, llg.FP32C, steps_per_graph=4)
+                s.set_tuning(tx, store, occ, False, False, False, tma)
+                s.set_state(W.initial_state(w, 0), 0)
+                s.step(9)
+                outs.append(s.get_state(0))
+                s.close()
+        for o in outs[1:]:
+            assert np.array_equal(o, outs[0]), np.abs(o - outs[0]).max()
+
+
+def test_tma_is_refused_where_unsupported(llg):
+    sweep = W.sc_temperature_sweep(n_replicas=2, L_min=8, L_max=8)
+    s = solver(llg, sweep, llg.FP32C)
+    with pytest.raises(llg.LLGError, match="one replica"):
+        s.set_tuning(4, True, 2, False, False, False, True)
+    tri = W.triangular_dmi_field_sweep(L=(20, 30, 1), n_fields=1, T=5.0)
+    t = solver(llg, tri, llg.FP32C)
+    with pytest.raises(llg.LLGError, match="TMA"):
+        t.set_tuning(4, True, 2, False, False, False, True)
+    odd = solver(llg, W.sc_ferromagnet(L=(6, 5, 9)), llg.FP32C)   # rows of 9 floats: 36 bytes
+    with pytest.raises(llg.LLGError, match="multiple of 16"):
+        odd.set_tuning(4, True, 2, False, False, False, True)
 
 
 def test_fused_step_is_refused_where_unsupported(llg):
