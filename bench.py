@@ -666,8 +666,9 @@ def main():
                                       ms_per_step, n_spins)
     ns = len(STAGE_BYTES[(integ, args.precision)])
 
-    # ---- dipole term: FFT convolution before every stage (cuFFT transforms
-    # and this library's scatter / k-space product / gather kernels)
+    # ---- dipole term: FFT convolution before every stage (this library's
+    # transform passes with the scatter and gather fused in, and its k-space
+    # product)
     dipole = None
     if any(t.kind == W.TERM_DIPOLE for t in w.model.terms):
         dipole = {"ms_per_evaluation": float(dip_ms.mean()), "evaluations_per_step": ns,

@@ -68,7 +68,7 @@ def build(force: bool = False, verbose: bool = False, extra=(), checked: bool = 
         return lib
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(lambda s: _compile(s, list(extra), out), srcs))
-    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", lib, *objs, "-lcufft"]
+    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", lib, *objs]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), res.stdout + res.stderr))

@@ -12,17 +12,18 @@
 //   scatter the spins onto the grid -> R2C -> h_i(q) = sum_j mu_j W_ij(q) S_j(q)
 //   -> C2R -> h_i = mu_i h_i(r) / prod(M) back into SoA planes,
 // the reference's sequence (cuda_dipole_fft.cu:184-209) with the tensor
-// normalised by the grid size as there.  cuFFT does the transforms; the
-// scatter, the k-space product and the gather are this file's kernels.
-// FP32C evaluates in single precision (R2C / C2R, float tensors computed in
-// double); FP64 in double.
-#include <cufft.h>
-
+// normalised by the grid size as there.  The transforms are this library's
+// own (llg_fft.cuh): one pass per axis, the scatter fused into the first
+// (real) pass and the gather into the last.  FP32C evaluates in single
+// precision (float tensors computed in double); FP64 in double.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <vector>
 
 #include "llg_dipole.h"
+#include "llg_fft.cuh"
 
 namespace jams_llg {
 
@@ -51,40 +52,60 @@ struct Dev {
   }
 };
 
-const char* cufft_name(cufftResult r) {
-  switch (r) {
-    case CUFFT_SUCCESS: return "success";
-    case CUFFT_INVALID_PLAN: return "invalid plan";
-    case CUFFT_ALLOC_FAILED: return "allocation failed";
-    case CUFFT_INVALID_VALUE: return "invalid value";
-    case CUFFT_INTERNAL_ERROR: return "internal error";
-    case CUFFT_EXEC_FAILED: return "execution failed";
-    case CUFFT_SETUP_FAILED: return "setup failed";
-    case CUFFT_INVALID_SIZE: return "invalid size";
-    default: return "cuFFT error";
+// ------------------------------------------------------------------ kernels
+
+// position (x, y, z) of point p of line o along the real axis h (the axes
+// after h have one cell)
+__device__ __forceinline__ void line_cell(int64_t o, int p, int h, const int M[3], int c[3]) {
+  c[0] = c[1] = c[2] = 0;
+  c[h] = p;
+  for (int a = h - 1; a >= 0; --a) {
+    c[a] = (int)(o % M[a]);
+    o /= M[a];
   }
 }
 
-// ------------------------------------------------------------------ kernels
-
-// spins of one replica onto its FFT grid: component c of basis site b at
-// grid row (c nb + b); cells outside the lattice (padding) are zero
+// the spins of one replica on its FFT grid, read by the forward real pass
+// (the scatter fused into it): field f = component * nb + basis site; cells
+// outside the lattice (padding) are zero
 template <class Real>
-__global__ void __launch_bounds__(kDipBlock) dip_scatter(const Real* __restrict__ s, int64_t npad, int64_t offset,
-                                                         int L0, int L1, int L2, int nb, int M1, int M2,
-                                                         int64_t Mtot, Real* __restrict__ grid) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= Mtot) return;
-  const int z = (int)(n % M2);
-  const int64_t t = n / M2;
-  const int y = (int)(t % M1);
-  const int x = (int)(t / M1);
-  const bool in = x < L0 && y < L1 && z < L2;
-  const int64_t i0 = in ? (((int64_t)x * L1 + y) * L2 + z) * nb : 0;
-  for (int b = 0; b < nb; ++b)
-    for (int c = 0; c < 3; ++c)
-      grid[(int64_t)(c * nb + b) * Mtot + n] = in ? s[c * npad + offset + i0 + b] : Real(0);
-}
+struct SpinSource {
+  const Real* s;
+  int64_t npad, offset;
+  int L[3], M[3], h, nb;
+  __device__ Real operator()(int64_t f, int64_t o, int p) const {
+    int c[3];
+    line_cell(o, p, h, M, c);
+    if (c[0] >= L[0] || c[1] >= L[1] || c[2] >= L[2]) return Real(0);
+    const int m = (int)(f / nb), b = (int)(f % nb);
+    return s[m * npad + offset + (((int64_t)c[0] * L[1] + c[1]) * L[2] + c[2]) * nb + b];
+  }
+};
+
+// a real grid of fields (the tensors at set-up)
+struct GridSource {
+  const double* g;
+  int64_t Mtot;
+  int Mh;
+  __device__ double operator()(int64_t f, int64_t o, int p) const { return g[f * Mtot + o * Mh + p]; }
+};
+
+// the field planes of one replica, written by the inverse real pass (the
+// gather fused into it): mu_s times the transform, lattice cells only
+template <class Real>
+struct FieldSink {
+  Real* hp;
+  int64_t npad, offset;
+  int L[3], M[3], h, nb;
+  MusArr mus;
+  __device__ void operator()(int64_t f, int64_t o, int p, Real v) const {
+    int c[3];
+    line_cell(o, p, h, M, c);
+    if (c[0] >= L[0] || c[1] >= L[1] || c[2] >= L[2]) return;
+    const int m = (int)(f / nb), b = (int)(f % nb);
+    hp[m * npad + offset + (((int64_t)c[0] * L[1] + c[1]) * L[2] + c[2]) * nb + b] = (Real)mus.v[b] * v;
+  }
+};
 
 // h_i(q) = sum_j mu_j W_ij(q) S_j(q) for every k-space point q.  W_ij is the
 // transform of a real tensor, so W_ji = conj(W_ij); W_ii is the transform of
@@ -161,26 +182,6 @@ void launch_convolve(int nb, const C* ks, const Real* wd, const C* wo, C* kh, in
   }
 }
 
-// grid -> SoA field planes of the replica, times mu_i; one thread per
-// lattice cell (coalesced reads of every grid row; the basis sites of a cell
-// are adjacent in the planes)
-template <class Real>
-__global__ void __launch_bounds__(kDipBlock) dip_gather(const Real* __restrict__ grid, int64_t Mtot, int L1, int L2,
-                                                        int nb, int M1, int M2, int64_t ncells, int64_t offset,
-                                                        int64_t npad, MusArr mus, Real* __restrict__ h) {
-  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (cell >= ncells) return;
-  const int z = (int)(cell % L2);
-  const int y = (int)((cell / L2) % L1);
-  const int x = (int)(cell / ((int64_t)L1 * L2));
-  const int64_t n = ((int64_t)x * M1 + y) * M2 + z;
-  for (int b = 0; b < nb; ++b) {
-    const Real mu = (Real)mus.v[b];
-    for (int c = 0; c < 3; ++c)
-      h[c * npad + offset + cell * nb + b] = mu * grid[(int64_t)(c * nb + b) * Mtot + n];
-  }
-}
-
 __global__ void dip_tensor_scatter(const int64_t* __restrict__ idx, const double* __restrict__ vals, int64_t n,
                                    int64_t Mtot, double* __restrict__ grid) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -206,18 +207,6 @@ __global__ void dip_store_tensor(const double2* __restrict__ a, Real* __restrict
 }
 
 unsigned blocks(int64_t n) { return (unsigned)((n + kDipBlock - 1) / kDipBlock); }
-
-// A batched 3-D real transform over M with the size-1 axes left out
-cufftResult make_plan(cufftHandle* plan, const int M[3], cufftType type, int batch, int64_t* Mq) {
-  int dims[3], r = 0;
-  for (int k = 0; k < 3; ++k)
-    if (M[k] > 1) dims[r++] = M[k];
-  if (r == 0) dims[r++] = 1;
-  int64_t q = 1;
-  for (int k = 0; k < r - 1; ++k) q *= dims[k];
-  *Mq = q * (dims[r - 1] / 2 + 1);
-  return cufftPlanMany(plan, r, dims, nullptr, 1, 0, nullptr, 1, 0, type, batch);
-}
 
 }  // namespace
 
@@ -255,14 +244,11 @@ struct DipoleReplica {
   int M[3] = {1, 1, 1};
   int64_t offset = 0;
   int64_t Mtot = 0, Mq = 0;
-  cufftHandle fwd = 0, inv = 0;
-  bool have_fwd = false, have_inv = false;
-  Dev<unsigned char> grid, ks, kh, wd, wo;   // wd: diagonal tensors (real), wo: i < j (complex)
-  size_t work = 0;
-  ~DipoleReplica() {
-    if (have_fwd) cufftDestroy(fwd);
-    if (have_inv) cufftDestroy(inv);
-  }
+  int h = 2;                        // the halved (real) axis: the last one longer than one cell
+  FftPlan1D plan[3] = {};
+  Dev<double2> twd[3];              // W_M^t = exp(-2 pi i t / M) per axis
+  Dev<float2> twf[3];
+  Dev<unsigned char> ks, kh, wd, wo;   // wd: diagonal tensors (real), wo: i < j (complex)
 };
 
 struct DipoleField {
@@ -276,6 +262,97 @@ struct DipoleField {
 };
 
 namespace {
+
+// --------------------------------------------------------- FFT driving --
+
+// complex values per shared-memory buffer of a transform pass
+template <class C>
+constexpr int fft_elems() {
+  return sizeof(C) == sizeof(float2) ? 4096 : 2048;
+}
+
+// dynamic shared memory above the default for a transform kernel (once per
+// kernel and size)
+cudaError_t allow_smem(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::vector<std::pair<const void*, size_t>> have;
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  std::lock_guard<std::mutex> lock(mu);
+  for (auto& e : have)
+    if (e.first == kernel && e.second >= bytes) return cudaSuccess;
+  const cudaError_t ce = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (ce == cudaSuccess) have.push_back({kernel, bytes});
+  return ce;
+}
+
+template <class C>
+const C* twiddles(const DipoleReplica& R, int a);
+template <>
+const float2* twiddles<float2>(const DipoleReplica& R, int a) {
+  return R.twf[a].p;
+}
+template <>
+const double2* twiddles<double2>(const DipoleReplica& R, int a) {
+  return R.twd[a].p;
+}
+
+// length of axis b in the half-spectrum grid
+int64_t kdim(const DipoleReplica& R, int b) {
+  return b == R.h ? R.M[b] / 2 + 1 : (b < R.h ? R.M[b] : 1);
+}
+
+// the complex passes along the axes before h, in place on k (nfields fields)
+template <class C>
+cudaError_t complex_passes(const DipoleReplica& R, C* k, int nfields, bool inverse, cudaStream_t st) {
+  for (int s = 0; s < R.h; ++s) {
+    const int a = inverse ? R.h - 1 - s : s;
+    const int n = R.M[a];
+    if (n == 1) continue;
+    int64_t stride = 1, outer = nfields;
+    for (int b = a + 1; b < 3; ++b) stride *= kdim(R, b);
+    for (int b = 0; b < a; ++b) outer *= kdim(R, b);
+    const int G = (int)std::min<int64_t>(stride, fft_batch(n, fft_elems<C>()));
+    const size_t sm = (size_t)2 * G * n * sizeof(C);
+    cudaError_t ce = allow_smem((const void*)fft_pass<C>, sm);
+    if (ce != cudaSuccess) return ce;
+    const int64_t grid = outer * ((stride + G - 1) / G);
+    fft_pass<C><<<(unsigned)grid, kFftThreads, sm, st>>>(k, outer, (int)stride, G, R.plan[a], twiddles<C>(R, a),
+                                                         inverse);
+  }
+  return cudaGetLastError();
+}
+
+// forward transform of nfields real fields read through src into the half
+// spectrum k
+template <class C, class Src>
+cudaError_t forward_transform(const DipoleReplica& R, Src src, int nfields, C* k, cudaStream_t st) {
+  const int n = R.M[R.h];
+  const int64_t O = R.Mtot / n, nlines = (int64_t)nfields * O;
+  const int G = fft_batch(n, fft_elems<C>());
+  const size_t sm = (size_t)2 * G * n * sizeof(C);
+  cudaError_t ce = allow_smem((const void*)fft_real_forward<C, Src>, sm);
+  if (ce != cudaSuccess) return ce;
+  fft_real_forward<C, Src><<<(unsigned)((nlines + G - 1) / G), kFftThreads, sm, st>>>(src, nlines, O, G, R.plan[R.h],
+                                                                                      twiddles<C>(R, R.h), k);
+  ce = cudaGetLastError();
+  return ce == cudaSuccess ? complex_passes<C>(R, k, nfields, false, st) : ce;
+}
+
+// inverse transform of the half spectrum k (overwritten) into sink
+template <class C, class Sink>
+cudaError_t inverse_transform(const DipoleReplica& R, C* k, int nfields, Sink sink, cudaStream_t st) {
+  cudaError_t ce = complex_passes<C>(R, k, nfields, true, st);
+  if (ce != cudaSuccess) return ce;
+  const int n = R.M[R.h];
+  const int64_t O = R.Mtot / n, nlines = (int64_t)nfields * O;
+  const int G = fft_batch(n, fft_elems<C>());
+  const size_t sm = (size_t)2 * G * n * sizeof(C);
+  ce = allow_smem((const void*)fft_real_inverse<C, Sink>, sm);
+  if (ce != cudaSuccess) return ce;
+  fft_real_inverse<C, Sink><<<(unsigned)((nlines + G - 1) / G), kFftThreads, sm, st>>>(k, nlines, O, G, R.plan[R.h],
+                                                                                       twiddles<C>(R, R.h), sink);
+  return cudaGetLastError();
+}
 
 // the non-zero tensor entries of basis pair (bi, bj) on replica grid R:
 // grid index and (xx, xy, xz, yy, yz, zz) x mu0 / (4 pi a^3) / prod(M)
@@ -390,24 +467,31 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
       return nullptr;
     }
     R->Mtot = (int64_t)R->M[0] * R->M[1] * R->M[2];
-    cufftResult fr = make_plan(&R->fwd, R->M, fp64 ? CUFFT_D2Z : CUFFT_R2C, 3 * nb, &R->Mq);
-    R->have_fwd = fr == CUFFT_SUCCESS;
-    if (fr == CUFFT_SUCCESS) {
-      int64_t mq = 0;
-      fr = make_plan(&R->inv, R->M, fp64 ? CUFFT_Z2D : CUFFT_C2R, 3 * nb, &mq);
-      R->have_inv = fr == CUFFT_SUCCESS;
+    R->h = 0;
+    for (int k = 0; k < 3; ++k)
+      if (R->M[k] > 1) R->h = k;
+    R->Mq = R->Mtot / R->M[R->h] * (R->M[R->h] / 2 + 1);
+    cudaError_t ce = cudaSuccess;
+    for (int k = 0; k < 3 && ce == cudaSuccess; ++k) {
+      const int n = R->M[k];
+      if (n > 7168) {
+        err = "dipole: a grid axis of " + std::to_string(n) + " cells is longer than the transform supports (7168)";
+        delete D;
+        return nullptr;
+      }
+      R->plan[k] = fft_plan(n);
+      std::vector<double2> td(n);
+      std::vector<float2> tf(n);
+      for (int t = 0; t < n; ++t) {
+        const double ang = 2.0 * kPiD * (double)t / (double)n;
+        td[t] = make_double2(std::cos(ang), -std::sin(ang));
+        tf[t] = make_float2((float)td[t].x, (float)td[t].y);
+      }
+      ce = R->twd[k].alloc(n);
+      if (ce == cudaSuccess) ce = R->twf[k].alloc(n);
+      if (ce == cudaSuccess) ce = cudaMemcpy(R->twd[k].p, td.data(), n * sizeof(double2), cudaMemcpyHostToDevice);
+      if (ce == cudaSuccess) ce = cudaMemcpy(R->twf[k].p, tf.data(), n * sizeof(float2), cudaMemcpyHostToDevice);
     }
-    if (fr != CUFFT_SUCCESS) {
-      err = std::string("dipole: cufftPlanMany: ") + cufft_name(fr);
-      delete D;
-      return nullptr;
-    }
-    size_t ws = 0;
-    cufftGetSize(R->fwd, &ws);
-    R->work = ws;
-    cufftGetSize(R->inv, &ws);
-    R->work += ws;
-    cudaError_t ce = R->grid.alloc((size_t)3 * nb * R->Mtot * real);
     if (ce == cudaSuccess) ce = R->ks.alloc((size_t)3 * nb * R->Mq * cplx);
     if (ce == cudaSuccess) ce = R->kh.alloc((size_t)3 * nb * R->Mq * cplx);
     if (ce == cudaSuccess) ce = R->wd.alloc((size_t)nb * 6 * R->Mq * real);
@@ -417,15 +501,8 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
       delete D;
       return nullptr;
     }
-    // tensors: scatter the in-cutoff entries onto a zero grid, D2Z, keep
-    cufftHandle tplan;
-    int64_t mq6 = 0;
-    fr = make_plan(&tplan, R->M, CUFFT_D2Z, 6, &mq6);
-    if (fr != CUFFT_SUCCESS) {
-      err = std::string("dipole: tensor plan: ") + cufft_name(fr);
-      delete D;
-      return nullptr;
-    }
+    // tensors: scatter the in-cutoff entries onto a zero grid, transform
+    // (double), keep in the replica's precision
     Dev<double> tgrid;
     Dev<double2> tk;
     Dev<int64_t> didx;
@@ -451,11 +528,8 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
           }
         }
         if (ce != cudaSuccess) break;
-        fr = cufftExecD2Z(tplan, tgrid.p, reinterpret_cast<cufftDoubleComplex*>(tk.p));
-        if (fr != CUFFT_SUCCESS) {
-          err = std::string("dipole: tensor transform: ") + cufft_name(fr);
-          break;
-        }
+        ce = forward_transform<double2>(*R, GridSource{tgrid.p, R->Mtot, R->M[R->h]}, 6, tk.p, 0);
+        if (ce != cudaSuccess) break;
         const int64_t n = 6 * R->Mq;
         unsigned char* rdst = bi == bj ? R->wd.p + (size_t)bi * 6 * R->Mq * real : nullptr;
         unsigned char* cdst = bi == bj ? nullptr : R->wo.p + (size_t)(pair++) * 6 * R->Mq * cplx;
@@ -467,7 +541,6 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
               tk.p, reinterpret_cast<float*>(rdst), reinterpret_cast<float2*>(cdst), n);
         ce = cudaGetLastError();
       }
-    cufftDestroy(tplan);
     if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
     if (ce != cudaSuccess && err.empty()) err = cuda_msg(ce, "dipole: building tensors");
     if (!err.empty()) {
@@ -482,52 +555,38 @@ void dipole_destroy(DipoleField* d) { delete d; }
 
 size_t dipole_device_bytes(const DipoleField* d) {
   size_t b = 0;
-  for (const auto* R : d->reps) b += R->grid.n + R->ks.n + R->kh.n + R->wd.n + R->wo.n + R->work;
+  for (const auto* R : d->reps) b += R->ks.n + R->kh.n + R->wd.n + R->wo.n;
   return b;
 }
 
-std::string dipole_compute(DipoleField* D, const void* s, void* h, int64_t npad, cudaStream_t st) {
+namespace {
+
+template <class Real, class C>
+std::string compute_replica(const DipoleField* D, DipoleReplica* R, const void* s, void* h, int64_t npad,
+                            cudaStream_t st) {
   const int nb = D->nb;
+  C* ks = reinterpret_cast<C*>(R->ks.p);
+  C* kh = reinterpret_cast<C*>(R->kh.p);
+  SpinSource<Real> src{static_cast<const Real*>(s), npad, R->offset, {R->L[0], R->L[1], R->L[2]},
+                       {R->M[0], R->M[1], R->M[2]}, R->h, nb};
+  cudaError_t ce = forward_transform<C>(*R, src, 3 * nb, ks, st);
+  if (ce != cudaSuccess) return cuda_msg(ce, "dipole: forward transform");
+  launch_convolve<C, Real>(nb, ks, reinterpret_cast<const Real*>(R->wd.p), reinterpret_cast<const C*>(R->wo.p), kh,
+                           R->Mq, D->mus, st);
+  FieldSink<Real> sink{static_cast<Real*>(h), npad, R->offset, {R->L[0], R->L[1], R->L[2]},
+                       {R->M[0], R->M[1], R->M[2]}, R->h, nb, D->mus};
+  ce = inverse_transform<C>(*R, kh, 3 * nb, sink, st);
+  if (ce != cudaSuccess) return cuda_msg(ce, "dipole: inverse transform");
+  return std::string();
+}
+
+}  // namespace
+
+std::string dipole_compute(DipoleField* D, const void* s, void* h, int64_t npad, cudaStream_t st) {
   for (DipoleReplica* R : D->reps) {
-    const int64_t ncells = (int64_t)R->L[0] * R->L[1] * R->L[2];
-    cufftResult fr = cufftSetStream(R->fwd, st);
-    if (fr == CUFFT_SUCCESS) fr = cufftSetStream(R->inv, st);
-    if (fr != CUFFT_SUCCESS) return std::string("dipole: cufftSetStream: ") + cufft_name(fr);
-    if (D->fp64) {
-      double* grid = reinterpret_cast<double*>(R->grid.p);
-      auto* ks = reinterpret_cast<cufftDoubleComplex*>(R->ks.p);
-      auto* kh = reinterpret_cast<cufftDoubleComplex*>(R->kh.p);
-      dip_scatter<double><<<blocks(R->Mtot), kDipBlock, 0, st>>>(static_cast<const double*>(s), npad, R->offset,
-                                                                R->L[0], R->L[1], R->L[2], nb, R->M[1], R->M[2],
-                                                                R->Mtot, grid);
-      fr = cufftExecD2Z(R->fwd, grid, ks);
-      if (fr != CUFFT_SUCCESS) return std::string("dipole: D2Z: ") + cufft_name(fr);
-      launch_convolve<double2, double>(nb, ks, reinterpret_cast<const double*>(R->wd.p),
-                                       reinterpret_cast<const double2*>(R->wo.p), kh, R->Mq, D->mus, st);
-      fr = cufftExecZ2D(R->inv, kh, grid);
-      if (fr != CUFFT_SUCCESS) return std::string("dipole: Z2D: ") + cufft_name(fr);
-      dip_gather<double><<<blocks(ncells), kDipBlock, 0, st>>>(grid, R->Mtot, R->L[1], R->L[2], nb, R->M[1],
-                                                               R->M[2], ncells, R->offset, npad, D->mus,
-                                                               static_cast<double*>(h));
-    } else {
-      float* grid = reinterpret_cast<float*>(R->grid.p);
-      auto* ks = reinterpret_cast<cufftComplex*>(R->ks.p);
-      auto* kh = reinterpret_cast<cufftComplex*>(R->kh.p);
-      dip_scatter<float><<<blocks(R->Mtot), kDipBlock, 0, st>>>(static_cast<const float*>(s), npad, R->offset,
-                                                               R->L[0], R->L[1], R->L[2], nb, R->M[1], R->M[2],
-                                                               R->Mtot, grid);
-      fr = cufftExecR2C(R->fwd, grid, ks);
-      if (fr != CUFFT_SUCCESS) return std::string("dipole: R2C: ") + cufft_name(fr);
-      launch_convolve<float2, float>(nb, ks, reinterpret_cast<const float*>(R->wd.p),
-                                     reinterpret_cast<const float2*>(R->wo.p), kh, R->Mq, D->mus, st);
-      fr = cufftExecC2R(R->inv, kh, grid);
-      if (fr != CUFFT_SUCCESS) return std::string("dipole: C2R: ") + cufft_name(fr);
-      dip_gather<float><<<blocks(ncells), kDipBlock, 0, st>>>(grid, R->Mtot, R->L[1], R->L[2], nb, R->M[1],
-                                                              R->M[2], ncells, R->offset, npad, D->mus,
-                                                              static_cast<float*>(h));
-    }
-    const cudaError_t ce = cudaGetLastError();
-    if (ce != cudaSuccess) return cuda_msg(ce, "dipole kernels");
+    const std::string e = D->fp64 ? compute_replica<double, double2>(D, R, s, h, npad, st)
+                                  : compute_replica<float, float2>(D, R, s, h, npad, st);
+    if (!e.empty()) return e;
   }
   return std::string();
 }

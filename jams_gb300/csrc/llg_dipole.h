@@ -26,9 +26,10 @@ struct DipoleReplicaSpec {
 
 struct DipoleField;
 
-// Builds the k-space tensors and FFT plans of every replica.  Returns null
-// and sets err when the geometry is invalid (cutoff beyond the inradius of
-// the periodic supercell, coincident sites) or a CUDA / cuFFT call fails.
+// Builds the k-space tensors, transform plans and twiddle tables of every
+// replica.  Returns null and sets err when the geometry is invalid (cutoff
+// beyond the inradius of the periodic supercell, coincident sites, a grid
+// axis longer than 7168 cells) or a CUDA call fails.
 DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3], const double* mus,
                            const std::vector<DipoleReplicaSpec>& reps, bool fp64, std::string& err);
 void dipole_destroy(DipoleField* d);

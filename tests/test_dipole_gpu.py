@@ -1,5 +1,5 @@
-"""The dipole-dipole term on the GPU (FFT convolution, cuFFT transforms,
-this library's k-space product) against the oracle's direct sum: fields,
+"""The dipole-dipole term on the GPU (FFT convolution with this library's
+own transforms and k-space product) against the oracle's direct sum: fields,
 energies and trajectories, periodic and open boundaries, Heun and RK4, both
 precisions, the tiled and the gather FP32 kernels."""
 import numpy as np
