@@ -97,6 +97,10 @@ WORKLOADS = {
     # (FFT convolution, r_c = 8 lattice parameters)
     "bcc64_3shell_dipole": lambda: W.bcc_three_shell(L=64, T=300.0, start="+z", dipole_cutoff=8.0),
     "bcc256_3shell_dipole": lambda: W.bcc_three_shell(L=256, T=500.0, steps=2000, dipole_cutoff=8.0),
+    # profiling case of the 256-point transform passes: FFT grid larger than
+    # L2 (204 MB per half spectrum), about 1.5 GB on the device
+    "bcc256x256x128_3shell_dipole": lambda: W.bcc_three_shell(L=(256, 256, 128), T=500.0, steps=2000,
+                                                               dipole_cutoff=8.0),
     # profiling cases: state larger than L2 (129 MB) but a few GB on the device
     "bcc192_nn": lambda: W.bcc_nearest_neighbour(L=192, T=500.0),
     "bcc192_3shell": lambda: W.bcc_three_shell(L=192, T=500.0),

@@ -20,10 +20,13 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "llg_dipole.h"
 #include "llg_fft.cuh"
+#include "llg_fft_reg.cuh"
 
 namespace jams_llg {
 
@@ -54,32 +57,51 @@ struct Dev {
 
 // ------------------------------------------------------------------ kernels
 
-// position (x, y, z) of point p of line o along the real axis h (the axes
-// after h have one cell)
-__device__ __forceinline__ void line_cell(int64_t o, int p, int h, const int M[3], int c[3]) {
-  c[0] = c[1] = c[2] = 0;
-  c[h] = p;
-  for (int a = h - 1; a >= 0; --a) {
-    c[a] = (int)(o % M[a]);
-    o /= M[a];
+// The cells of one replica's FFT grid: grid index g = o * M_h + p for point
+// p of line o along the real axis h (the axes after h have one cell), split
+// into (x, y, z) by two divisions; field f = component * nb + basis site.
+// Along h consecutive cells are nb spins apart, so a line is also a base
+// index and its L_h lattice points (the rest of the line is padding).
+struct GridCells {
+  int L[3], M[3];
+  FastDiv dM1, dM2, dnb;
+  int nb, h;
+  int64_t npad, offset;
+  // spin-plane index of field f at grid cell g, or -1 for a padding cell
+  __device__ __forceinline__ int64_t plane_index(int f, int g) const {
+    const int t = (int)fdiv((uint32_t)g, dM2);
+    const int z = g - t * M[2];
+    const int x = (int)fdiv((uint32_t)t, dM1);
+    const int y = t - x * M[1];
+    if (x >= L[0] || y >= L[1] || z >= L[2]) return -1;
+    const int m = (int)fdiv((uint32_t)f, dnb), b = f - m * nb;
+    return m * npad + offset + (((int64_t)x * L[1] + y) * L[2] + z) * nb + b;
   }
-}
+  // spin-plane index of point 0 of line o of field f, or -1 when the line
+  // lies in the padding
+  __device__ __forceinline__ int64_t line_base(int f, int o) const {
+    return plane_index(f, o * M[h]);
+  }
+};
 
 // the spins of one replica on its FFT grid, read by the forward real pass
-// (the scatter fused into it): field f = component * nb + basis site; cells
-// outside the lattice (padding) are zero
+// (the scatter fused into it); cells outside the lattice (padding) are zero
 template <class Real>
 struct SpinSource {
   const Real* s;
-  int64_t npad, offset;
-  int L[3], M[3], h, nb;
-  __device__ Real operator()(int64_t f, int64_t o, int p) const {
-    int c[3];
-    line_cell(o, p, h, M, c);
-    if (c[0] >= L[0] || c[1] >= L[1] || c[2] >= L[2]) return Real(0);
-    const int m = (int)(f / nb), b = (int)(f % nb);
-    return s[m * npad + offset + (((int64_t)c[0] * L[1] + c[1]) * L[2] + c[2]) * nb + b];
+  GridCells gc;
+  int Mh;
+  __device__ Real operator()(int f, int o, int p) const {
+    const int64_t i = gc.plane_index(f, o * Mh + p);
+    return i < 0 ? Real(0) : __ldg(s + i);
   }
+  // one line: point p is line(...)[p * nb] for p < L_h, zero beyond
+  __device__ const Real* line(int f, int o) const {
+    const int64_t i = gc.line_base(f, o);
+    return i < 0 ? nullptr : s + i;
+  }
+  __device__ int length() const { return gc.L[gc.h]; }
+  __device__ int step() const { return gc.nb; }
 };
 
 // a real grid of fields (the tensors at set-up)
@@ -87,7 +109,7 @@ struct GridSource {
   const double* g;
   int64_t Mtot;
   int Mh;
-  __device__ double operator()(int64_t f, int64_t o, int p) const { return g[f * Mtot + o * Mh + p]; }
+  __device__ double operator()(int f, int o, int p) const { return g[f * Mtot + (int64_t)o * Mh + p]; }
 };
 
 // the field planes of one replica, written by the inverse real pass (the
@@ -95,16 +117,21 @@ struct GridSource {
 template <class Real>
 struct FieldSink {
   Real* hp;
-  int64_t npad, offset;
-  int L[3], M[3], h, nb;
+  GridCells gc;
+  int Mh;
   MusArr mus;
-  __device__ void operator()(int64_t f, int64_t o, int p, Real v) const {
-    int c[3];
-    line_cell(o, p, h, M, c);
-    if (c[0] >= L[0] || c[1] >= L[1] || c[2] >= L[2]) return;
-    const int m = (int)(f / nb), b = (int)(f % nb);
-    hp[m * npad + offset + (((int64_t)c[0] * L[1] + c[1]) * L[2] + c[2]) * nb + b] = (Real)mus.v[b] * v;
+  __device__ void operator()(int f, int o, int p, Real v) const {
+    const int64_t i = gc.plane_index(f, o * Mh + p);
+    if (i >= 0) hp[i] = (Real)mus.v[f - (int)fdiv((uint32_t)f, gc.dnb) * gc.nb] * v;
   }
+  // one line (as SpinSource::line) and the moment of field f's site
+  __device__ Real* line(int f, int o) const {
+    const int64_t i = gc.line_base(f, o);
+    return i < 0 ? nullptr : hp + i;
+  }
+  __device__ Real moment(int f) const { return (Real)mus.v[f - (int)fdiv((uint32_t)f, gc.dnb) * gc.nb]; }
+  __device__ int length() const { return gc.L[gc.h]; }
+  __device__ int step() const { return gc.nb; }
 };
 
 // h_i(q) = sum_j mu_j W_ij(q) S_j(q) for every k-space point q.  W_ij is the
@@ -131,6 +158,10 @@ template <class C, class Real, int NB>
 __global__ void __launch_bounds__(kDipBlock) dip_convolve(const C* __restrict__ ks, const Real* __restrict__ wd,
                                                           const C* __restrict__ wo, C* __restrict__ kh, int64_t Mq,
                                                           MusArr mus) {
+  // programmatic dependent launch: the next pass may be scheduled now; wait
+  // for the forward transform before reading its spectrum
+  asm volatile("griddepcontrol.launch_dependents;");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= Mq) return;
   C s[NB][3], h[NB][3];
@@ -171,14 +202,22 @@ __global__ void __launch_bounds__(kDipBlock) dip_convolve(const C* __restrict__ 
 }
 
 template <class C, class Real>
-void launch_convolve(int nb, const C* ks, const Real* wd, const C* wo, C* kh, int64_t Mq, const MusArr& mus,
-                     cudaStream_t st) {
-  const unsigned g = (unsigned)((Mq + kDipBlock - 1) / kDipBlock);
+cudaError_t launch_convolve(int nb, const C* ks, const Real* wd, const C* wo, C* kh, int64_t Mq, const MusArr& mus,
+                            cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)((Mq + kDipBlock - 1) / kDipBlock));
+  cfg.blockDim = dim3(kDipBlock);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
   switch (nb) {
-    case 1: dip_convolve<C, Real, 1><<<g, kDipBlock, 0, st>>>(ks, wd, wo, kh, Mq, mus); break;
-    case 2: dip_convolve<C, Real, 2><<<g, kDipBlock, 0, st>>>(ks, wd, wo, kh, Mq, mus); break;
-    case 3: dip_convolve<C, Real, 3><<<g, kDipBlock, 0, st>>>(ks, wd, wo, kh, Mq, mus); break;
-    default: dip_convolve<C, Real, 4><<<g, kDipBlock, 0, st>>>(ks, wd, wo, kh, Mq, mus); break;
+    case 1: return cudaLaunchKernelEx(&cfg, dip_convolve<C, Real, 1>, ks, wd, wo, kh, Mq, mus);
+    case 2: return cudaLaunchKernelEx(&cfg, dip_convolve<C, Real, 2>, ks, wd, wo, kh, Mq, mus);
+    case 3: return cudaLaunchKernelEx(&cfg, dip_convolve<C, Real, 3>, ks, wd, wo, kh, Mq, mus);
+    default: return cudaLaunchKernelEx(&cfg, dip_convolve<C, Real, 4>, ks, wd, wo, kh, Mq, mus);
   }
 }
 
@@ -265,11 +304,18 @@ namespace {
 
 // --------------------------------------------------------- FFT driving --
 
-// complex values per shared-memory buffer of a transform pass
+// complex values per shared-memory buffer of a transform pass (more when
+// one line is longer), and lines per CTA of a strided pass (16 x 8 B or
+// 8 x 16 B: one 128-byte run of global memory per line element)
 template <class C>
 constexpr int fft_elems() {
-  return sizeof(C) == sizeof(float2) ? 4096 : 2048;
+  return sizeof(C) == sizeof(float2) ? 2048 : 1024;
 }
+template <class C>
+constexpr int fft_pass_lines() {
+  return sizeof(C) == sizeof(float2) ? 16 : 8;
+}
+inline int lines_per_cta(int n, int elems, int cap) { return std::max(1, std::min(cap, elems / n)); }
 
 // dynamic shared memory above the default for a transform kernel (once per
 // kernel and size)
@@ -301,9 +347,94 @@ int64_t kdim(const DipoleReplica& R, int b) {
   return b == R.h ? R.M[b] / 2 + 1 : (b < R.h ? R.M[b] : 1);
 }
 
-// the complex passes along the axes before h, in place on k (nfields fields)
+// a transform kernel on stream st; with programmatic stream serialisation
+// (pdl) its twiddle load overlaps the previous kernel's tail
+template <class... P, class... A>
+cudaError_t launch_fft(void (*kernel)(P...), unsigned grid, size_t smem, cudaStream_t st, bool pdl, A&&... args) {
+  cudaError_t ce = allow_smem((const void*)kernel, smem);
+  if (ce != cudaSuccess) return ce;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kFftThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
+
+// the register passes take single-precision lines of a power-of-two length
+// in [16, 1024]
+inline bool reg_length(int n) { return n >= kFftRegMin && n <= kFftRegMax && (n & (n - 1)) == 0; }
+
+template <int N>
+cudaError_t reg_pass(float2* k, int stride, int64_t outer, const float2* tw, bool inverse, cudaStream_t st,
+                     bool pdl) {
+  constexpr int G = 256 / RegShape<N>::T;
+  const int64_t chunks = (stride + G - 1) / G;
+  const unsigned grid = (unsigned)(outer * chunks);
+  return inverse ? launch_fft(fft_pass_reg<N, true>, grid, reg_pass_smem<N>(), st, pdl, k, stride,
+                              fast_div((uint32_t)chunks), tw)
+                 : launch_fft(fft_pass_reg<N, false>, grid, reg_pass_smem<N>(), st, pdl, k, stride,
+                              fast_div((uint32_t)chunks), tw);
+}
+
+// sites: the line pairs are basis-site pairs (an even number of fields,
+// 8-byte aligned pairs in the planes)
+template <int N, class Src>
+cudaError_t reg_forward(const Src& src, int nlines, int O, bool sites, const float2* tw, float2* k, cudaStream_t st,
+                        bool pdl) {
+  constexpr int G = 256 / RegShape<N>::T;
+  const int npairs = sites ? nlines / 2 : (nlines + 1) / 2;
+  const unsigned grid = (unsigned)((npairs + G - 1) / G);
+  return sites ? launch_fft(fft_real_forward_reg<N, true, Src>, grid, reg_real_smem<N>(), st, pdl, src, nlines,
+                            npairs, fast_div((uint32_t)O), tw, k)
+               : launch_fft(fft_real_forward_reg<N, false, Src>, grid, reg_real_smem<N>(), st, pdl, src, nlines,
+                            npairs, fast_div((uint32_t)O), tw, k);
+}
+
+template <int N, class Sink>
+cudaError_t reg_inverse(const float2* k, int nlines, int O, bool sites, const float2* tw, const Sink& sink,
+                        cudaStream_t st, bool pdl) {
+  constexpr int G = 256 / RegShape<N>::T;
+  const int npairs = sites ? nlines / 2 : (nlines + 1) / 2;
+  const unsigned grid = (unsigned)((npairs + G - 1) / G);
+  return sites ? launch_fft(fft_real_inverse_reg<N, true, Sink>, grid, reg_real_smem<N>(), st, pdl, k, nlines,
+                            npairs, fast_div((uint32_t)O), tw, sink)
+               : launch_fft(fft_real_inverse_reg<N, false, Sink>, grid, reg_real_smem<N>(), st, pdl, k, nlines,
+                            npairs, fast_div((uint32_t)O), tw, sink);
+}
+
+// F<N>::run(args...) for the register length n
+#define JAMS_FFT_REG_SWITCH(n, CALL) \
+  switch (n) {                       \
+    case 16: return CALL(16);        \
+    case 32: return CALL(32);        \
+    case 64: return CALL(64);        \
+    case 128: return CALL(128);      \
+    case 256: return CALL(256);      \
+    case 512: return CALL(512);      \
+    default: return CALL(1024);      \
+  }
+
 template <class C>
-cudaError_t complex_passes(const DipoleReplica& R, C* k, int nfields, bool inverse, cudaStream_t st) {
+cudaError_t reg_pass_any(int n, C* k, int stride, int64_t outer, const C* tw, bool inverse, cudaStream_t st, bool pdl) {
+  if constexpr (std::is_same<C, float2>::value) {
+#define JAMS_CALL(N) reg_pass<N>(k, stride, outer, tw, inverse, st, pdl)
+    JAMS_FFT_REG_SWITCH(n, JAMS_CALL)
+#undef JAMS_CALL
+  }
+  return cudaErrorInvalidValue;
+}
+
+// the complex passes along the axes before h, in place on k (nfields fields);
+// each axis's stride counts the later axes of the half-spectrum grid, at
+// least the M_h / 2 + 1 >= 2 values of axis h
+template <class C>
+cudaError_t complex_passes(const DipoleReplica& R, C* k, int nfields, bool inverse, cudaStream_t st, bool pdl) {
   for (int s = 0; s < R.h; ++s) {
     const int a = inverse ? R.h - 1 - s : s;
     const int n = R.M[a];
@@ -311,47 +442,66 @@ cudaError_t complex_passes(const DipoleReplica& R, C* k, int nfields, bool inver
     int64_t stride = 1, outer = nfields;
     for (int b = a + 1; b < 3; ++b) stride *= kdim(R, b);
     for (int b = 0; b < a; ++b) outer *= kdim(R, b);
-    const int G = (int)std::min<int64_t>(stride, fft_batch(n, fft_elems<C>()));
-    const size_t sm = (size_t)2 * G * n * sizeof(C);
-    cudaError_t ce = allow_smem((const void*)fft_pass<C>, sm);
+    if (std::is_same<C, float2>::value && reg_length(n)) {
+      const cudaError_t ce = reg_pass_any<C>(n, k, (int)stride, outer, twiddles<C>(R, a), inverse, st, pdl);
+      if (ce != cudaSuccess) return ce;
+      continue;
+    }
+    const int G = (int)std::min<int64_t>(stride, lines_per_cta(n, 2 * fft_elems<C>(), fft_pass_lines<C>()));
+    const int64_t chunks = (stride + G - 1) / G;
+    const size_t sm = (size_t)(2 * G + 1) * n * sizeof(C);
+    const cudaError_t ce =
+        launch_fft(fft_pass<C>, (unsigned)(outer * chunks), sm, st, pdl, k, (int)stride, G, fast_div((uint32_t)G),
+                   fast_div((uint32_t)chunks), R.plan[a], twiddles<C>(R, a), inverse);
     if (ce != cudaSuccess) return ce;
-    const int64_t grid = outer * ((stride + G - 1) / G);
-    fft_pass<C><<<(unsigned)grid, kFftThreads, sm, st>>>(k, outer, (int)stride, G, R.plan[a], twiddles<C>(R, a),
-                                                         inverse);
   }
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 // forward transform of nfields real fields read through src into the half
-// spectrum k
+// spectrum k (the real pass takes line pairs)
 template <class C, class Src>
-cudaError_t forward_transform(const DipoleReplica& R, Src src, int nfields, C* k, cudaStream_t st) {
+cudaError_t forward_transform(const DipoleReplica& R, const Src& src, int nfields, C* k, cudaStream_t st, bool pdl,
+                              bool sites = false) {
   const int n = R.M[R.h];
-  const int64_t O = R.Mtot / n, nlines = (int64_t)nfields * O;
-  const int G = fft_batch(n, fft_elems<C>());
-  const size_t sm = (size_t)2 * G * n * sizeof(C);
-  cudaError_t ce = allow_smem((const void*)fft_real_forward<C, Src>, sm);
-  if (ce != cudaSuccess) return ce;
-  fft_real_forward<C, Src><<<(unsigned)((nlines + G - 1) / G), kFftThreads, sm, st>>>(src, nlines, O, G, R.plan[R.h],
-                                                                                      twiddles<C>(R, R.h), k);
-  ce = cudaGetLastError();
-  return ce == cudaSuccess ? complex_passes<C>(R, k, nfields, false, st) : ce;
+  const int O = (int)(R.Mtot / n), nlines = nfields * O, npairs = (nlines + 1) / 2;
+  if constexpr (std::is_same<C, float2>::value) {
+    if (reg_length(n)) {
+      const float2* tw = twiddles<C>(R, R.h);
+      cudaError_t ce = cudaSuccess;
+#define JAMS_CALL(N) reg_forward<N, Src>(src, nlines, O, sites, tw, k, st, pdl)
+      ce = [&]() -> cudaError_t { JAMS_FFT_REG_SWITCH(n, JAMS_CALL) }();
+#undef JAMS_CALL
+      return ce == cudaSuccess ? complex_passes<C>(R, k, nfields, false, st, pdl) : ce;
+    }
+  }
+  const int G = lines_per_cta(n, fft_elems<C>(), 256);
+  const size_t sm = (size_t)(2 * G + 1) * n * sizeof(C);
+  const cudaError_t ce = launch_fft(fft_real_forward<C, Src>, (unsigned)((npairs + G - 1) / G), sm, st, pdl, src,
+                                    nlines, fast_div((uint32_t)O), G, R.plan[R.h], twiddles<C>(R, R.h), k);
+  return ce == cudaSuccess ? complex_passes<C>(R, k, nfields, false, st, pdl) : ce;
 }
 
 // inverse transform of the half spectrum k (overwritten) into sink
 template <class C, class Sink>
-cudaError_t inverse_transform(const DipoleReplica& R, C* k, int nfields, Sink sink, cudaStream_t st) {
-  cudaError_t ce = complex_passes<C>(R, k, nfields, true, st);
+cudaError_t inverse_transform(const DipoleReplica& R, C* k, int nfields, const Sink& sink, cudaStream_t st, bool pdl,
+                              bool sites = false) {
+  const cudaError_t ce = complex_passes<C>(R, k, nfields, true, st, pdl);
   if (ce != cudaSuccess) return ce;
   const int n = R.M[R.h];
-  const int64_t O = R.Mtot / n, nlines = (int64_t)nfields * O;
-  const int G = fft_batch(n, fft_elems<C>());
-  const size_t sm = (size_t)2 * G * n * sizeof(C);
-  ce = allow_smem((const void*)fft_real_inverse<C, Sink>, sm);
-  if (ce != cudaSuccess) return ce;
-  fft_real_inverse<C, Sink><<<(unsigned)((nlines + G - 1) / G), kFftThreads, sm, st>>>(k, nlines, O, G, R.plan[R.h],
-                                                                                       twiddles<C>(R, R.h), sink);
-  return cudaGetLastError();
+  const int O = (int)(R.Mtot / n), nlines = nfields * O, npairs = (nlines + 1) / 2;
+  if constexpr (std::is_same<C, float2>::value) {
+    if (reg_length(n)) {
+      const float2* tw = twiddles<C>(R, R.h);
+#define JAMS_CALL(N) reg_inverse<N, Sink>(k, nlines, O, sites, tw, sink, st, pdl)
+      JAMS_FFT_REG_SWITCH(n, JAMS_CALL)
+#undef JAMS_CALL
+    }
+  }
+  const int G = lines_per_cta(n, fft_elems<C>(), 256);
+  const size_t sm = (size_t)(2 * G + 1) * n * sizeof(C);
+  return launch_fft(fft_real_inverse<C, Sink>, (unsigned)((npairs + G - 1) / G), sm, st, pdl, (const C*)k, nlines,
+                    fast_div((uint32_t)O), G, R.plan[R.h], twiddles<C>(R, R.h), sink);
 }
 
 // the non-zero tensor entries of basis pair (bi, bj) on replica grid R:
@@ -471,6 +621,11 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
     for (int k = 0; k < 3; ++k)
       if (R->M[k] > 1) R->h = k;
     R->Mq = R->Mtot / R->M[R->h] * (R->M[R->h] / 2 + 1);
+    if ((int64_t)std::max(3 * nb, 6) * R->Mtot >= ((int64_t)1 << 31)) {
+      err = "dipole: the FFT grid of " + std::to_string(R->Mtot) + " cells is too large (fields x cells >= 2^31)";
+      delete D;
+      return nullptr;
+    }
     cudaError_t ce = cudaSuccess;
     for (int k = 0; k < 3 && ce == cudaSuccess; ++k) {
       const int n = R->M[k];
@@ -528,7 +683,7 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
           }
         }
         if (ce != cudaSuccess) break;
-        ce = forward_transform<double2>(*R, GridSource{tgrid.p, R->Mtot, R->M[R->h]}, 6, tk.p, 0);
+        ce = forward_transform<double2>(*R, GridSource{tgrid.p, R->Mtot, R->M[R->h]}, 6, tk.p, 0, false);
         if (ce != cudaSuccess) break;
         const int64_t n = 6 * R->Mq;
         unsigned char* rdst = bi == bj ? R->wd.p + (size_t)bi * 6 * R->Mq * real : nullptr;
@@ -561,21 +716,40 @@ size_t dipole_device_bytes(const DipoleField* d) {
 
 namespace {
 
+GridCells grid_cells(const DipoleReplica& R, int nb, int64_t npad) {
+  GridCells gc;
+  for (int k = 0; k < 3; ++k) {
+    gc.L[k] = R.L[k];
+    gc.M[k] = R.M[k];
+  }
+  gc.dM1 = fast_div((uint32_t)R.M[1]);
+  gc.dM2 = fast_div((uint32_t)R.M[2]);
+  gc.dnb = fast_div((uint32_t)nb);
+  gc.nb = nb;
+  gc.h = R.h;
+  gc.npad = npad;
+  gc.offset = R.offset;
+  return gc;
+}
+
 template <class Real, class C>
 std::string compute_replica(const DipoleField* D, DipoleReplica* R, const void* s, void* h, int64_t npad,
                             cudaStream_t st) {
   const int nb = D->nb;
   C* ks = reinterpret_cast<C*>(R->ks.p);
   C* kh = reinterpret_cast<C*>(R->kh.p);
-  SpinSource<Real> src{static_cast<const Real*>(s), npad, R->offset, {R->L[0], R->L[1], R->L[2]},
-                       {R->M[0], R->M[1], R->M[2]}, R->h, nb};
-  cudaError_t ce = forward_transform<C>(*R, src, 3 * nb, ks, st);
+  const GridCells gc = grid_cells(*R, nb, npad);
+  const SpinSource<Real> src{static_cast<const Real*>(s), gc, R->M[R->h]};
+  // basis-site pairs for the real passes: an even basis and even plane
+  // offsets (8-byte aligned pairs)
+  const bool sites = nb % 2 == 0 && npad % 2 == 0 && R->offset % 2 == 0;
+  cudaError_t ce = forward_transform<C>(*R, src, 3 * nb, ks, st, true, sites);
   if (ce != cudaSuccess) return cuda_msg(ce, "dipole: forward transform");
-  launch_convolve<C, Real>(nb, ks, reinterpret_cast<const Real*>(R->wd.p), reinterpret_cast<const C*>(R->wo.p), kh,
-                           R->Mq, D->mus, st);
-  FieldSink<Real> sink{static_cast<Real*>(h), npad, R->offset, {R->L[0], R->L[1], R->L[2]},
-                       {R->M[0], R->M[1], R->M[2]}, R->h, nb, D->mus};
-  ce = inverse_transform<C>(*R, kh, 3 * nb, sink, st);
+  ce = launch_convolve<C, Real>(nb, ks, reinterpret_cast<const Real*>(R->wd.p), reinterpret_cast<const C*>(R->wo.p),
+                                kh, R->Mq, D->mus, st);
+  if (ce != cudaSuccess) return cuda_msg(ce, "dipole: k-space product");
+  const FieldSink<Real> sink{static_cast<Real*>(h), gc, R->M[R->h], D->mus};
+  ce = inverse_transform<C>(*R, kh, 3 * nb, sink, st, true, sites);
   if (ce != cudaSuccess) return cuda_msg(ce, "dipole: inverse transform");
   return std::string();
 }

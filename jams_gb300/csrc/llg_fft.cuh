@@ -19,12 +19,28 @@
 // transform is normalised.
 //
 // The real axis h is contiguous in both the real grid and the half spectrum
-// (every later axis has one cell).  The forward real pass reads its line
-// through a source functor (the spin planes, fusing the scatter onto the
-// grid, or a real grid), transforms it as a complex line with zero imaginary
-// part and keeps outputs 0 .. N/2.  The inverse real pass rebuilds the full
-// spectrum by Hermitian symmetry, transforms it and hands the real parts to
-// a sink functor (the field planes, fusing the gather).
+// (every later axis has one cell).  The real passes take two real lines a, b
+// as one complex line z = a + i b ("two for one"): the forward pass reads
+// them through a source functor (the spin planes, fusing the scatter onto
+// the grid, or a real grid), transforms z and separates
+//   A[q] = (Z[q] + conj Z[N-q]) / 2,  B[q] = (Z[q] - conj Z[N-q]) / 2i,
+// keeping q = 0 .. N/2.  The inverse pass completes each half spectrum by
+// Hermitian symmetry (X[N-q] = conj X[q], the imaginary parts of X[0] and
+// X[N/2] dropped as a complex-to-real transform does), transforms A + i B
+// and hands the real part (line a) and the imaginary part (line b) to a sink
+// functor (the field planes, fusing the gather).
+//
+// Every pass keeps its twiddle table in shared memory, and is launched with
+// programmatic stream serialisation where the caller asks: it loads the
+// table, then waits for the previous kernel in the stream to complete before
+// it touches the grid.
+//
+// Index arithmetic is 32-bit (the host keeps every grid below 2^31 values)
+// and divides by run-time constants through multiply-high reciprocals
+// (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994): for 1 <= d < 2^31, l = ceil(log2 d),
+// mul = floor(2^32 (2^l - d) / d) + 1, and x / d = (umulhi(x, mul) + x) >> l
+// for every x < 2^31.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -33,35 +49,75 @@
 
 namespace jams_llg {
 
-constexpr int kFftMaxStages = 30;
+constexpr int kFftMaxStages = 16;
 constexpr int kFftThreads = 256;
 
+struct FastDiv {
+  uint32_t d = 1, mul = 1;
+  int shift = 0;
+};
+
+inline FastDiv fast_div(uint32_t d) {
+  FastDiv f;
+  f.d = d;
+  int l = 0;
+  while ((1ull << l) < d) ++l;
+  f.shift = l;
+  f.mul = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+  return f;
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t x, const FastDiv& f) { return (__umulhi(x, f.mul) + x) >> f.shift; }
+
+// one Stockham stage: radix R, m = n / R butterflies, Ns = product of the
+// earlier radices, st = n / (Ns R) the twiddle step
+struct FftStage {
+  int R, m, Ns, st;
+  FastDiv dm, dNs;
+};
+
 struct FftPlan1D {
-  int n;
-  int nstages;
-  int radix[kFftMaxStages];
+  int n = 1;
+  int nstages = 0;
+  FastDiv dn, dnh;   // n and n / 2 + 1
+  FftStage stage[kFftMaxStages];
 };
 
 // radices of n: 4 while more than 4 remains, then 4, 2, 3, 5, 7 and the
-// remaining primes
+// remaining primes (n <= 7168 needs at most 13 stages)
 inline FftPlan1D fft_plan(int n) {
-  FftPlan1D p{};
+  FftPlan1D p;
   p.n = n;
+  p.dn = fast_div((uint32_t)n);
+  p.dnh = fast_div((uint32_t)(n / 2 + 1));
+  int rad[kFftMaxStages], ns = 0;
   int m = n;
-  while (m % 4 == 0 && m > 4) {
-    p.radix[p.nstages++] = 4;
+  while (m % 4 == 0 && m > 4 && ns < kFftMaxStages) {
+    rad[ns++] = 4;
     m /= 4;
   }
   for (int r : {4, 2, 3, 5, 7})
-    while (m % r == 0) {
-      p.radix[p.nstages++] = r;
+    while (m % r == 0 && ns < kFftMaxStages) {
+      rad[ns++] = r;
       m /= r;
     }
-  for (int r = 11; m > 1; r += 2)
-    while (m % r == 0) {
-      p.radix[p.nstages++] = r;
+  for (int r = 11; m > 1 && ns < kFftMaxStages; r += 2)
+    while (m % r == 0 && ns < kFftMaxStages) {
+      rad[ns++] = r;
       m /= r;
     }
+  int Ns = 1;
+  for (int s = 0; s < ns; ++s) {
+    FftStage& S = p.stage[s];
+    S.R = rad[s];
+    S.m = n / S.R;
+    S.Ns = Ns;
+    S.st = n / (Ns * S.R);
+    S.dm = fast_div((uint32_t)S.m);
+    S.dNs = fast_div((uint32_t)Ns);
+    Ns *= S.R;
+  }
+  p.nstages = ns;
   return p;
 }
 
@@ -85,42 +141,51 @@ __device__ __forceinline__ C cmul(C a, C b) {
 
 // W_N^t (inverse: its conjugate) from the table of exp(-2 pi i t / N)
 template <class C>
-__device__ __forceinline__ C twiddle(const C* __restrict__ tw, int t, bool inverse) {
+__device__ __forceinline__ C twiddle(const C* tw, int t, bool inverse) {
   const C w = tw[t];
   return inverse ? CT<C>::make(w.x, -w.y) : w;
 }
 
-// transforms `nlines` lines of length P.n held in shared memory at a, b the
-// same size; every thread of the CTA takes part.  Element e of line l sits at
+// the twiddle table into shared memory; then, under programmatic dependent
+// launch, let the next kernel be scheduled and wait for the previous one to
+// complete (without the launch attribute both return at once)
+template <class C>
+__device__ __forceinline__ void fft_prologue(C* tws, const C* __restrict__ tw, int n) {
+  for (int t = threadIdx.x; t < n; t += blockDim.x) tws[t] = __ldg(tw + t);
+  asm volatile("griddepcontrol.launch_dependents;");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// transforms `nl` lines of length P.n held in shared memory at a, b the same
+// size; every thread of the CTA takes part.  Element e of line l sits at
 // l * P.n + e (INTER false: consecutive threads take consecutive butterflies
-// of one line) or at e * nlines + l (INTER true: the lines interleaved,
+// of one line) or at e * nl + l (INTER true: the lines interleaved,
 // consecutive threads take the same butterfly of consecutive lines, so that
-// neither the strided loads nor the butterflies conflict on shared-memory
-// banks).  Returns the buffer that holds the result.
+// neither the strided global loads nor the butterflies conflict on
+// shared-memory banks; dnl divides by nl).  Returns the buffer that holds the
+// result.
 template <class C, bool INTER>
-__device__ C* fft_lines(C* a, C* b, int nlines, const FftPlan1D& P, const C* __restrict__ tw, bool inverse) {
+__device__ C* fft_lines(C* a, C* b, int nl, const FastDiv& dnl, const FftPlan1D& P, const C* tw, bool inverse) {
   const int n = P.n;
-  const int tid = threadIdx.x;
-  const int es = INTER ? nlines : 1;     // element stride within a line
-  int Ns = 1;
+  const int es = INTER ? nl : 1;   // element stride within a line
   for (int s = 0; s < P.nstages; ++s) {
-    const int R = P.radix[s];
-    const int m = n / R;
-    const int st = n / (Ns * R);
-    const int items = nlines * m;
-    for (int it = tid; it < items; it += blockDim.x) {
+    const FftStage& S = P.stage[s];
+    const int R = S.R, m = S.m, Ns = S.Ns, st = S.st;
+    const int items = nl * m;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
       int line, j;
       if (INTER) {
-        j = it / nlines;
-        line = it - j * nlines;
+        j = (int)fdiv((uint32_t)it, dnl);
+        line = it - j * nl;
       } else {
-        line = it / m;
+        line = (int)fdiv((uint32_t)it, S.dm);
         j = it - line * m;
       }
       const C* in = a + (INTER ? line : line * n);
       C* out = b + (INTER ? line : line * n);
-      const int k = j % Ns;
-      const int dst = (j / Ns) * Ns * R + k;
+      const int jq = (int)fdiv((uint32_t)j, S.dNs);
+      const int k = j - jq * Ns;
+      const int dst = jq * Ns * R + k;
       if (R == 2) {
         const C v0 = in[j * es];
         const C v1 = k ? cmul(in[(j + m) * es], twiddle(tw, k * st, inverse)) : in[(j + m) * es];
@@ -143,16 +208,19 @@ __device__ C* fft_lines(C* a, C* b, int nlines, const FftPlan1D& P, const C* __r
         out[(dst + 2 * Ns) * es] = CT<C>::make(s02.x - s13.x, s02.y - s13.y);
         out[(dst + 3 * Ns) * es] = CT<C>::make(d02.x - id13.x, d02.y - id13.y);
       } else {
-        // any other radix: each output from all R inputs, the twiddle and
-        // the R-point DFT factor as one power of W_N
+        // any other radix: output q from all R inputs, the twiddle and the
+        // R-point DFT factor together as W_N^{r (k st + q m)} (R m = n)
         for (int q = 0; q < R; ++q) {
           typename CT<C>::Real ax = 0, ay = 0;
+          const int step = k * st + q * m;   // < 2 n
+          int t = 0;
           for (int r = 0; r < R; ++r) {
-            const int t = (k * r * st + ((r * q) % R) * m) % n;
             const C w = twiddle(tw, t, inverse);
             const C v = in[(j + r * m) * es];
             ax += v.x * w.x - v.y * w.y;
             ay += v.x * w.y + v.y * w.x;
+            t += step;
+            while (t >= n) t -= n;
           }
           out[(dst + q * Ns) * es] = CT<C>::make(ax, ay);
         }
@@ -162,117 +230,134 @@ __device__ C* fft_lines(C* a, C* b, int nlines, const FftPlan1D& P, const C* __r
     C* t = a;
     a = b;
     b = t;
-    Ns *= R;
   }
   return a;
 }
 
-// lines per CTA for length n: at most `elems` complex values per buffer
-__host__ __device__ inline int fft_batch(int n, int elems) {
-  const int g = elems / n;
-  return g < 1 ? 1 : (g > 256 ? 256 : g);
-}
-
-// complex pass along an axis whose elements are `stride` apart (stride > 1:
-// the lines of one outer block are its `stride` consecutive inner offsets;
-// a CTA takes `G` consecutive ones) or contiguous (stride == 1: a CTA takes
-// G consecutive lines).  In place.
+// complex pass along an axis whose elements are `stride` (> 1) apart: the
+// lines of one outer block are its `stride` consecutive inner offsets, a CTA
+// takes G consecutive ones (dchunks.d = ceil(stride / G) CTAs per outer
+// block), and element el of its lines is one contiguous run of global
+// memory.  In place.
 template <class C>
-__global__ void __launch_bounds__(kFftThreads) fft_pass(C* __restrict__ g, int64_t outer, int stride, int G,
-                                                        const __grid_constant__ FftPlan1D P, const C* __restrict__ tw,
-                                                        bool inverse) {
+__global__ void __launch_bounds__(kFftThreads) fft_pass(C* __restrict__ g, int stride, int G, const FastDiv dG,
+                                                        const FastDiv dchunks, const __grid_constant__ FftPlan1D P,
+                                                        const C* __restrict__ tw, bool inverse) {
   extern __shared__ unsigned char fft_smem[];
-  C* a = reinterpret_cast<C*>(fft_smem);
-  C* b = a + (size_t)G * P.n;
+  C* tws = reinterpret_cast<C*>(fft_smem);
+  C* a = tws + P.n;
+  C* b = a + G * P.n;
   const int n = P.n;
-  int64_t base;
-  int lines;
-  if (stride == 1) {
-    const int64_t l0 = (int64_t)blockIdx.x * G;
-    lines = (int)min((int64_t)G, outer - l0);
-    base = l0 * n;
-    for (int e = threadIdx.x; e < lines * n; e += blockDim.x) a[e] = g[base + e];
-  } else {
-    const int64_t chunks = (stride + G - 1) / G;
-    const int64_t o = blockIdx.x / chunks;
-    const int i0 = (int)(blockIdx.x % chunks) * G;
-    lines = min(G, stride - i0);
-    base = o * (int64_t)n * stride + i0;
-    // element el of the `lines` inner offsets: one contiguous run of global
-    // memory, stored interleaved (a[el * lines + l])
-    for (int e = threadIdx.x; e < lines * n; e += blockDim.x) {
-      const int el = e / lines, l = e - el * lines;
-      a[e] = g[base + (int64_t)el * stride + l];
-    }
+  fft_prologue(tws, tw, n);
+  const int o = (int)fdiv(blockIdx.x, dchunks);
+  const int i0 = (int)(blockIdx.x - (uint32_t)o * dchunks.d) * G;
+  const int lines = min(G, stride - i0);
+  const int64_t base = (int64_t)o * n * stride + i0;
+  for (int e = threadIdx.x; e < G * n; e += blockDim.x) {
+    const int el = (int)fdiv((uint32_t)e, dG), l = e - el * G;
+    a[e] = l < lines ? g[base + (int64_t)el * stride + l] : CT<C>::make(0, 0);
   }
   __syncthreads();
-  if (stride == 1) {
-    const C* r = fft_lines<C, false>(a, b, lines, P, tw, inverse);
-    for (int e = threadIdx.x; e < lines * n; e += blockDim.x) g[base + e] = r[e];
-  } else {
-    const C* r = fft_lines<C, true>(a, b, lines, P, tw, inverse);
-    for (int e = threadIdx.x; e < lines * n; e += blockDim.x) {
-      const int el = e / lines, l = e - el * lines;
-      g[base + (int64_t)el * stride + l] = r[e];
-    }
+  const C* r = fft_lines<C, true>(a, b, G, dG, P, tws, inverse);
+  for (int e = threadIdx.x; e < G * n; e += blockDim.x) {
+    const int el = (int)fdiv((uint32_t)e, dG), l = e - el * G;
+    if (l < lines) g[base + (int64_t)el * stride + l] = r[e];
   }
 }
 
-// forward pass along the real axis: line l = (field f, position o before the
-// axis); src(f, o, p) gives the real value at position p of the line.  Writes
-// outputs 0 .. N/2 of every line to k[(f * O + o) * (N/2 + 1) + q].
+// (field, position before the axis) of real line l = f * O + o, and of l + 1
+struct LinePair {
+  int fa, oa, fb, ob;
+};
+__device__ __forceinline__ LinePair line_pair(int la, const FastDiv& dO) {
+  LinePair q;
+  q.fa = (int)fdiv((uint32_t)la, dO);
+  q.oa = la - q.fa * (int)dO.d;
+  const bool wrap = q.oa + 1 == (int)dO.d;
+  q.fb = wrap ? q.fa + 1 : q.fa;
+  q.ob = wrap ? 0 : q.oa + 1;
+  return q;
+}
+
+// forward pass along the real axis over nlines real lines, l = f * O + o
+// (field f, position o before the axis, dO.d = O); src(f, o, p) gives the
+// real value at position p of a line.  A CTA takes G line pairs (2 c, 2 c + 1)
+// and writes outputs 0 .. N/2 of every line to k[l * (N/2 + 1) + q].
 template <class C, class Src>
-__global__ void __launch_bounds__(kFftThreads) fft_real_forward(const __grid_constant__ Src src, int64_t nlines,
-                                                                int64_t O, int G, const __grid_constant__ FftPlan1D P,
+__global__ void __launch_bounds__(kFftThreads) fft_real_forward(const __grid_constant__ Src src, int nlines,
+                                                                const FastDiv dO, int G,
+                                                                const __grid_constant__ FftPlan1D P,
                                                                 const C* __restrict__ tw, C* __restrict__ k) {
   extern __shared__ unsigned char fft_smem[];
-  C* a = reinterpret_cast<C*>(fft_smem);
-  C* b = a + (size_t)G * P.n;
+  C* tws = reinterpret_cast<C*>(fft_smem);
+  C* a = tws + P.n;
+  C* b = a + G * P.n;
   const int n = P.n, nh = n / 2 + 1;
-  const int64_t l0 = (int64_t)blockIdx.x * G;
-  const int lines = (int)min((int64_t)G, nlines - l0);
+  fft_prologue(tws, tw, n);
+  const int c0 = blockIdx.x * G;
+  const int npairs = (nlines + 1) / 2;
+  const int lines = min(G, npairs - c0);
   for (int e = threadIdx.x; e < lines * n; e += blockDim.x) {
-    const int l = e / n, p = e - l * n;
-    const int64_t line = l0 + l;
-    a[e] = CT<C>::make(src(line / O, line % O, p), 0);
+    const int c = (int)fdiv((uint32_t)e, P.dn), p = e - c * n;
+    const int la = 2 * (c0 + c);
+    const LinePair q = line_pair(la, dO);
+    const auto va = src(q.fa, q.oa, p);
+    const auto vb = la + 1 < nlines ? src(q.fb, q.ob, p) : decltype(va)(0);
+    a[e] = CT<C>::make(va, vb);
   }
   __syncthreads();
-  const C* r = fft_lines<C, false>(a, b, lines, P, tw, false);
+  const C* r = fft_lines<C, false>(a, b, lines, P.dn, P, tws, false);
   for (int e = threadIdx.x; e < lines * nh; e += blockDim.x) {
-    const int l = e / nh, q = e - l * nh;
-    k[(l0 + l) * nh + q] = r[l * n + q];
+    const int c = (int)fdiv((uint32_t)e, P.dnh), q = e - c * nh;
+    const C z = r[c * n + q], w = r[c * n + (q == 0 ? 0 : n - q)];
+    const typename CT<C>::Real half = 0.5;
+    const int64_t la = 2 * (int64_t)(c0 + c);
+    k[la * nh + q] = CT<C>::make(half * (z.x + w.x), half * (z.y - w.y));
+    if (la + 1 < nlines) k[(la + 1) * nh + q] = CT<C>::make(half * (z.y + w.y), half * (w.x - z.x));
   }
 }
 
-// inverse pass along the real axis: the half spectrum of line l at
-// k[l * (N/2 + 1) ..], completed by X[N - q] = conj(X[q]); sink(f, o, p, x)
-// receives the real part of output p
+// inverse pass along the real axis: the half spectrum of real line l at
+// k[l * (N/2 + 1) ..]; sink(f, o, p, x) receives output p of line l = f * O +
+// o.  A CTA takes G line pairs.
 template <class C, class Sink>
-__global__ void __launch_bounds__(kFftThreads) fft_real_inverse(const C* __restrict__ k, int64_t nlines, int64_t O,
-                                                                int G, const __grid_constant__ FftPlan1D P,
-                                                                const C* __restrict__ tw, const __grid_constant__ Sink sink) {
+__global__ void __launch_bounds__(kFftThreads) fft_real_inverse(const C* __restrict__ k, int nlines,
+                                                                const FastDiv dO, int G,
+                                                                const __grid_constant__ FftPlan1D P,
+                                                                const C* __restrict__ tw,
+                                                                const __grid_constant__ Sink sink) {
   extern __shared__ unsigned char fft_smem[];
-  C* a = reinterpret_cast<C*>(fft_smem);
-  C* b = a + (size_t)G * P.n;
+  C* tws = reinterpret_cast<C*>(fft_smem);
+  C* a = tws + P.n;
+  C* b = a + G * P.n;
   const int n = P.n, nh = n / 2 + 1;
-  const int64_t l0 = (int64_t)blockIdx.x * G;
-  const int lines = (int)min((int64_t)G, nlines - l0);
+  fft_prologue(tws, tw, n);
+  const int c0 = blockIdx.x * G;
+  const int npairs = (nlines + 1) / 2;
+  const int lines = min(G, npairs - c0);
   for (int e = threadIdx.x; e < lines * n; e += blockDim.x) {
-    const int l = e / n, p = e - l * n;
-    const int64_t row = (l0 + l) * nh;
-    if (p < nh) {
-      a[e] = k[row + p];
-    } else {
-      const C v = k[row + (n - p)];
-      a[e] = CT<C>::make(v.x, -v.y);
+    const int c = (int)fdiv((uint32_t)e, P.dn), p = e - c * n;
+    const int64_t la = 2 * (int64_t)(c0 + c);
+    const bool mirror = p >= nh;
+    const int64_t off = mirror ? n - p : p;
+    const bool edge = p == 0 || 2 * p == n;   // X[0], X[N/2]: real
+    C xa = k[la * nh + off];
+    C xb = la + 1 < nlines ? k[(la + 1) * nh + off] : CT<C>::make(0, 0);
+    if (mirror) {
+      xa.y = -xa.y;
+      xb.y = -xb.y;
     }
+    if (edge) xa.y = xb.y = 0;
+    a[e] = CT<C>::make(xa.x - xb.y, xa.y + xb.x);   // A + i B
   }
   __syncthreads();
-  const C* r = fft_lines<C, false>(a, b, lines, P, tw, true);
+  const C* r = fft_lines<C, false>(a, b, lines, P.dn, P, tws, true);
   for (int e = threadIdx.x; e < lines * n; e += blockDim.x) {
-    const int l = e / n, p = e - l * n;
-    const int64_t line = l0 + l;
-    sink(line / O, line % O, p, r[e].x);
+    const int c = (int)fdiv((uint32_t)e, P.dn), p = e - c * n;
+    const int la = 2 * (c0 + c);
+    const LinePair q = line_pair(la, dO);
+    sink(q.fa, q.oa, p, r[e].x);
+    if (la + 1 < nlines) sink(q.fb, q.ob, p, r[e].y);
   }
 }
 

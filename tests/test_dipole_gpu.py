@@ -2,10 +2,11 @@
 own transforms and k-space product) against the oracle's direct sum: fields,
 energies and trajectories, periodic and open boundaries, Heun and RK4, both
 precisions, the tiled and the gather FP32 kernels."""
+import copy
+import os
+
 import numpy as np
 import pytest
-
-import os
 
 from jams_gb300 import configs as C
 from jams_gb300 import workloads as W
@@ -19,6 +20,11 @@ FP64_FIELD_TOL = 1e-12       # relative to the largest field component
 FP32C_FIELD_TOL = 2e-6
 FP64_RUN_TOL = 1e-10         # max |dS| after 100 T = 0 steps (FFT rounding, not bit-exact)
 FP32C_RUN_TOL = 1e-5         # max |dS| after 1000 T = 0 steps
+# the dipole term's field alone, relative to its largest component: the FP32
+# transforms round at ~1e-7 per pass, the tensors are stored in single
+# precision
+FP64_DIPOLE_TOL = 1e-11
+FP32C_DIPOLE_TOL = 2e-5
 
 
 def cases():
@@ -29,8 +35,48 @@ def cases():
     }
 
 
+def transform_cases():
+    """Grids whose axes take every transform kernel: the single-precision
+    register passes (power-of-two lengths 16..1024: the last grid axis as a
+    real pass, the others as strided complex passes) beside the Stockham
+    passes (other lengths, and every FP64 axis).  A periodic axis of L cells
+    is an FFT axis of L points, an open one of 2L."""
+    return {
+        "bcc16_periodic": W.bcc_three_shell(L=16, T=0.0, start="random", dipole_cutoff=2.4),
+        "sc_4x4x256": W.sc_ferromagnet(L=(4, 4, 256), dipole_cutoff=1.5),
+        "sc_256x4x3": W.sc_ferromagnet(L=(256, 4, 3), dipole_cutoff=1.0),
+        "sc_film_32x16x16_open_z": W.sc_ferromagnet(L=(32, 16, 16), periodic=(1, 1, 0), dipole_cutoff=2.2),
+        "sc_128x64x8": W.sc_ferromagnet(L=(128, 64, 8), dipole_cutoff=1.5),
+        "sc_4x4x256_open_z": W.sc_ferromagnet(L=(4, 4, 256), periodic=(1, 1, 0), dipole_cutoff=1.5),
+        "sc_3x3x1024": W.sc_ferromagnet(L=(3, 3, 1024), dipole_cutoff=1.0),
+        "sc_1024x3x3": W.sc_ferromagnet(L=(1024, 3, 3), dipole_cutoff=1.0),
+    }
+
+
 def start(w, r=0):
     return W.initial_state(w, r)
+
+
+def oracle_dipole_field(oracle, w, s0):
+    """The oracle's dipole field: its total field less the field of the same
+    model without the dipole term (both in FP64)."""
+    w2 = copy.deepcopy(w)
+    w2.model.terms = [t for t in w2.model.terms if t.kind != W.TERM_DIPOLE]
+    return oracle.OracleSim(w, 0).fields(s0) - oracle.OracleSim(w2, 0).fields(s0)
+
+
+@pytest.mark.parametrize("name", sorted(transform_cases()))
+@pytest.mark.parametrize("prec", ["FP64", "FP32C"])
+def test_dipole_term_field_on_every_transform_length(llg, oracle, name, prec):
+    w = transform_cases()[name]
+    s = llg.Solver(w, precision=getattr(llg, prec))
+    s0 = start(w)
+    s.set_state(s0, 0)
+    want = oracle_dipole_field(oracle, w, s0)
+    got = s.term_fields([t.kind for t in w.model.terms].index(W.TERM_DIPOLE), 0)
+    tol = FP64_DIPOLE_TOL if prec == "FP64" else FP32C_DIPOLE_TOL
+    assert np.abs(want).max() > 0
+    assert np.abs(got - want).max() <= tol * np.abs(want).max()
 
 
 @pytest.mark.parametrize("name", sorted(cases()))
