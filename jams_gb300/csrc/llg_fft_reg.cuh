@@ -8,8 +8,8 @@
 //   X[k1 + E k2] = sum_t W_T^{t k2} W_N^{t k1} sum_e x[t + T e] W_E^{e k1}
 // (the two-factor Cooley-Tukey split): thread t loads x[t + T e] for every e
 // straight from global memory into registers, transforms them over e (an
-// E-point radix-2 DIT FFT in registers, every index and twiddle position a
-// compile-time constant), multiplies by W_N^{t k1}, and writes the E results
+// E-point radix-2 Stockham FFT in registers, every index and twiddle
+// position a compile-time constant), multiplies by W_N^{t k1}, and writes the E results
 // to shared memory; after one barrier each thread takes E / T of the k1 and
 // transforms over t (a T-point FFT in registers), holding X[k1 + E k2] for
 // every k2.  One shared-memory round trip per point instead of two per
@@ -59,12 +59,6 @@ struct RegShape<1024> {
   static constexpr int E = 32, T = 32;
 };
 
-constexpr int reg_log2(int n) { return n <= 1 ? 0 : 1 + reg_log2(n / 2); }
-__host__ __device__ constexpr int reg_bitrev(int i, int bits) {
-  int r = 0;
-  for (int b = 0; b < bits; ++b) r |= ((i >> b) & 1) << (bits - 1 - b);
-  return r;
-}
 
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -77,37 +71,43 @@ __device__ __forceinline__ float2 reg_twiddle(const float2* tws, int t) {
   return INV ? make_float2(w.x, -w.y) : w;
 }
 
-// D-point DFT of v in registers, natural order in and out: radix-2
-// decimation in time on the bit-reversed order; W_{2h}^j = W_N^{j N / 2h}
-// from the table (W^{D/4} = -i forward, +i inverse, needs no table)
-template <int D, int N, bool INV>
-__device__ __forceinline__ void reg_dft(float2 (&v)[D], const float2* tws) {
-  constexpr int B = reg_log2(D);
-  float2 w[D];
+// D-point DFT of v in registers, natural order in and out: self-sorting
+// (Stockham) radix-2 stages, one template instance per stage so that every
+// register index and twiddle position is a compile-time constant.  Stage
+// Ns (1, 2, 4, .. D/2) maps butterfly j < D/2, k = j mod Ns, as
+//   b[(j / Ns) 2 Ns + k]      = a[j] + W_{2Ns}^k a[j + D/2]
+//   b[(j / Ns) 2 Ns + k + Ns] = a[j] - W_{2Ns}^k a[j + D/2]
+// with W_{2Ns}^k = W_N^{k N / 2Ns} from the table (-i forward, +i inverse
+// at k = Ns / 2, needing no table).
+template <int D, int N, bool INV, int NS>
+struct RegStage {
+  __device__ __forceinline__ static void run(float2 (&a)[D], const float2* tws) {
+    if constexpr (NS < D) {
+      float2 b[D];
 #pragma unroll
-  for (int i = 0; i < D; ++i) w[reg_bitrev(i, B)] = v[i];
-#pragma unroll
-  for (int lg = 0; lg < B; ++lg) {
-    const int half = 1 << lg;
-#pragma unroll
-    for (int base = 0; base < D; base += 2 * half) {
-#pragma unroll
-      for (int j = 0; j < half; ++j) {
-        const float2 a = w[base + j];
-        float2 b = w[base + j + half];
-        if (j != 0) {
-          if (2 * j == half)
-            b = INV ? make_float2(-b.y, b.x) : make_float2(b.y, -b.x);
+      for (int j = 0; j < D / 2; ++j) {
+        const int k = j % NS, o = (j / NS) * 2 * NS + k;
+        const float2 v0 = a[j];
+        float2 v1 = a[j + D / 2];
+        if (k != 0) {
+          if (2 * k == NS)
+            v1 = INV ? make_float2(-v1.y, v1.x) : make_float2(v1.y, -v1.x);
           else
-            b = cmul(b, reg_twiddle<INV>(tws, j * (N / (2 * half))));
+            v1 = cmul(v1, reg_twiddle<INV>(tws, k * (N / (2 * NS))));
         }
-        w[base + j] = c_add(a, b);
-        w[base + j + half] = c_sub(a, b);
+        b[o] = c_add(v0, v1);
+        b[o + NS] = c_sub(v0, v1);
       }
+      RegStage<D, N, INV, 2 * NS>::run(b, tws);
+#pragma unroll
+      for (int i = 0; i < D; ++i) a[i] = b[i];
     }
   }
-#pragma unroll
-  for (int i = 0; i < D; ++i) v[i] = w[i];
+};
+
+template <int D, int N, bool INV>
+__device__ __forceinline__ void reg_dft(float2 (&v)[D], const float2* tws) {
+  RegStage<D, N, INV, 1>::run(v, tws);
 }
 
 // the first factor: v[e] = x[t + T e] -> W_N^{t k1} sum_e x[t + T e] W_E^{e k1}
