@@ -133,9 +133,13 @@ constexpr size_t reg_real_smem() {
 
 // complex pass along an axis whose elements are `stride` apart: CTA b takes
 // lines i0 .. i0 + G - 1 of outer block o (b = o * chunks + i0 / G,
-// dchunks.d = chunks); in place
+// dchunks.d = chunks); in place.  At 128 and 256 points three CTAs per SM
+// (80 registers, a 20-32 B spill) beat two without the spill: 1.11 against
+// 1.21 ms per bcc 256^3 dipole evaluation.  Other lengths take no minimum
+// (0): at 64 points a minimum raised the registers from 48 to 61 and made
+// the pass slower.
 template <int N, bool INV>
-__global__ void __launch_bounds__(256) fft_pass_reg(float2* __restrict__ g, int stride, const FastDiv dchunks,
+__global__ void __launch_bounds__(256, (N == 128 || N == 256) ? 3 : 0) fft_pass_reg(float2* __restrict__ g, int stride, const FastDiv dchunks,
                                                    const float2* __restrict__ tw) {
   constexpr int E = RegShape<N>::E, T = RegShape<N>::T, G = 256 / T;
   extern __shared__ unsigned char fft_smem[];
