@@ -68,7 +68,8 @@ STAGE_BYTES = {
 # fraction, on one GPU
 METRIC = "LLG spin-steps/s on 1 GB300: FP32 vs FP64 form at \u22641e-5 max|\u0394S|; % of HBM peak"
 # the default line also carries these workloads, each as an object of its own
-SECONDARY = {"bcc256_nn": {"three_shell": "bcc256_3shell", "config2": "bcc64_3shell"}}
+SECONDARY = {"bcc256_nn": {"three_shell": "bcc256_3shell", "config2": "bcc64_3shell",
+                           "with_dipole": "bcc256_3shell_dipole"}}
 DEFAULT_WORKLOAD = "bcc256_nn"
 
 # the fused Heun step (one kernel per step, FP32C): read s0, write s1
@@ -613,6 +614,47 @@ def stage_roofline(sol, w, name: str, precision: str, tuning: dict, flush, profi
     return roofline, dip_ms
 
 
+def dipole_fft_bytes(w) -> int:
+    """Algorithmic bytes of one FP32C dipole field evaluation, summed over
+    replicas: the forward real pass reads the 3 nb spin fields (4 B per
+    cell) and writes their half spectra (8 B per point); each complex pass
+    reads and writes the half spectra; the k-space product reads them and
+    the stored tensors (nb x 6 real + nb (nb - 1) / 2 x 6 complex per point)
+    and writes the field spectra; the inverse passes mirror the forward
+    ones, the inverse real pass writing the 3 nb field planes."""
+    nb, per = w.model.nb, w.model.periodic
+    total = 0
+    for r in w.replicas:
+        L = list(r.L)
+        M = [L[k] if per[k] or L[k] == 1 else 2 * L[k] for k in range(3)]
+        h = max([k for k in range(3) if M[k] > 1], default=0)
+        cells = int(np.prod(L))
+        mq = int(np.prod(M)) // M[h] * (M[h] // 2 + 1)
+        f = 3 * nb
+        passes = sum(1 for k in range(h) if M[k] > 1)
+        spec = f * mq * 8
+        real = f * cells * 4 + spec
+        tensor = nb * 6 * mq * 4 + nb * (nb - 1) // 2 * 6 * mq * 8
+        total += 2 * real + 2 * passes * 2 * spec + (2 * spec + tensor)
+    return total
+
+
+def dipole_object(w, dip_ms, stage_ms):
+    """The dipole term's share of a step: per-evaluation time, and the
+    transforms' algorithmic bytes over it against the measured copy peak."""
+    if not any(t.kind == W.TERM_DIPOLE for t in w.model.terms):
+        return None
+    peak, _ = load_peak()
+    ms = float(np.mean(dip_ms))
+    nbytes = dipole_fft_bytes(w)
+    return {"ms_per_evaluation": ms, "evaluations_per_step": int(len(dip_ms)),
+            "share_of_stage_time": float(np.sum(dip_ms) / (np.sum(dip_ms) + np.sum(stage_ms))),
+            "r_cutoff": next(t.r_cutoff for t in w.model.terms if t.kind == W.TERM_DIPOLE),
+            "transform": "this library's register / Stockham FFT passes, scatter and gather fused",
+            "bytes_per_evaluation": nbytes, "achieved_gbs": nbytes / (ms * 1e-3) / 1e9,
+            "frac": nbytes / (ms * 1e-3) / 1e9 / peak if peak else None}
+
+
 def secondary_form(torch, llg, args, name: str, precision: str, local: int, stream, flush, steps: int,
                    warmup: int):
     """One more workload or precision in the same line: value, ms per step,
@@ -625,11 +667,16 @@ def secondary_form(torch, llg, args, name: str, precision: str, local: int, stre
     total_ms, launches, _ = timed_steps(torch, sol, steps, warmup, flush, stream, 1, local, clocks)
     clk = clocks.stop()
     ms = total_ms / steps
-    roof, _ = stage_roofline(sol, w, name, precision, tuning, flush, max(5, args.profile_steps // 5), ms, n_spins)
+    roof, dip_ms = stage_roofline(sol, w, name, precision, tuning, flush, max(5, args.profile_steps // 5), ms,
+                                  n_spins)
     sol.close()
-    return {"workload": name, "description": w.description, "spins": int(n_spins), "precision": precision,
-            "value": n_spins * steps / (total_ms * 1e-3), "unit": "spin-steps/s", "steps": steps, "warmup": warmup,
-            "ms_per_step": ms, "gpu_launches": launches, "roofline": roof, "clocks": clk, "kernels": tuning}
+    out = {"workload": name, "description": w.description, "spins": int(n_spins), "precision": precision,
+           "value": n_spins * steps / (total_ms * 1e-3), "unit": "spin-steps/s", "steps": steps, "warmup": warmup,
+           "ms_per_step": ms, "gpu_launches": launches, "roofline": roof, "clocks": clk, "kernels": tuning}
+    dip = dipole_object(w, dip_ms, roof["stage_ms"]) if precision == "fp32c" else None
+    if dip:
+        out["dipole"] = dip
+    return out
 
 
 def main():
@@ -673,11 +720,7 @@ def main():
     # ---- dipole term: FFT convolution before every stage (this library's
     # transform passes with the scatter and gather fused in, and its k-space
     # product)
-    dipole = None
-    if any(t.kind == W.TERM_DIPOLE for t in w.model.terms):
-        dipole = {"ms_per_evaluation": float(dip_ms.mean()), "evaluations_per_step": ns,
-                  "share_of_stage_time": float(dip_ms.sum() / (dip_ms.sum() + np.sum(roofline["stage_ms"]))),
-                  "r_cutoff": next(t.r_cutoff for t in w.model.terms if t.kind == W.TERM_DIPOLE)}
+    dipole = dipole_object(w, dip_ms, roofline["stage_ms"]) if args.precision == "fp32c" else None
 
     # ---- steady state without flush: blocks of 100 steps as CUDA graphs
     blk = 100

@@ -708,6 +708,16 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
 
 void dipole_destroy(DipoleField* d) { delete d; }
 
+int64_t dipole_launches(const DipoleField* d) {
+  int64_t n = 0;
+  for (const auto* R : d->reps) {
+    int passes = 0;
+    for (int a = 0; a < R->h; ++a) passes += R->M[a] > 1;
+    n += 3 + 2 * passes;
+  }
+  return n;
+}
+
 size_t dipole_device_bytes(const DipoleField* d) {
   size_t b = 0;
   for (const auto* R : d->reps) b += R->ks.n + R->kh.n + R->wd.n + R->wo.n;

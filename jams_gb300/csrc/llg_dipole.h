@@ -33,6 +33,11 @@ struct DipoleField;
 DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3], const double* mus,
                            const std::vector<DipoleReplicaSpec>& reps, bool fp64, std::string& err);
 void dipole_destroy(DipoleField* d);
+// kernel launches of one field evaluation, over all replicas: per replica
+// the forward real pass, one complex pass per further grid axis longer than
+// one cell, the k-space product, the complex passes back and the inverse
+// real pass
+int64_t dipole_launches(const DipoleField* d);
 
 // Dipole field (meV) of the state planes `s` (three planes of npad reals,
 // float or double as at creation) into `h` (same layout), on stream st.

@@ -1090,6 +1090,9 @@ Real* buf(llg_handle* h, int k) {
 }
 
 int num_stages(const llg_handle* h) { return h->integrator == LLG_HEUN ? 2 : 4; }
+// launches per stage: the stage kernel and, where the model has a dipole
+// term, the transform kernels of the field evaluation before it
+int64_t stage_launches(const llg_handle* h) { return 1 + (h->dipole ? dipole_launches(h->dipole) : 0); }
 
 // time factors at solver time t (ps), the reference's double expressions:
 // f[0] = sinc(pi f_bw (t - t_c)), f[1] = cos(2 pi f_c (t - t_c)) of the
@@ -1288,9 +1291,9 @@ int64_t enqueue_steps(llg_handle* h, int nsteps, int cur) {
     }
     cur = next_buffer(h, cur);
   }
-  if (advanced) return (int64_t)nsteps * ns;
+  if (advanced) return (int64_t)nsteps * ns * stage_launches(h);
   advance_step_base<<<1, 1, 0, h->stream>>>(h->d_step_base.p, (uint32_t)nsteps);
-  return (int64_t)nsteps * ns + 1;
+  return (int64_t)nsteps * ns * stage_launches(h) + 1;
 }
 
 int state_buffer(const llg_handle* h) { return (h->fp64 || h->integrator == LLG_RK4) ? 0 : h->cur; }
@@ -1460,9 +1463,10 @@ static int step_blocks(llg_handle* h, int32_t nsteps) {
     if (it != h->graphs.end()) {
       cudaError_t ce = cudaGraphLaunch(it->second, h->stream);
       if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaGraphLaunch");
-      // per step: one fused kernel, or one kernel per stage; the other
-      // kernels' blocks end with the step-counter kernel
-      h->last_launches += (int64_t)n * (h->fused ? 1 : num_stages(h)) + (h->tiled ? 0 : 1);
+      // per step: one fused kernel, or one kernel per stage (each stage
+      // after the dipole term's transform kernels, where the model has one);
+      // the other kernels' blocks end with the step-counter kernel
+      h->last_launches += (int64_t)n * (h->fused ? 1 : num_stages(h) * stage_launches(h)) + (h->tiled ? 0 : 1);
     } else {
       h->last_launches += enqueue_steps(h, n, h->cur);
     }
@@ -1890,7 +1894,7 @@ int llg_profile_stages(llg_handle* h, int32_t nsteps, double* ms) {
   advance_step_base<<<1, 1, 0, h->stream>>>(h->d_step_base.p, (uint32_t)nsteps);
   h->cur = cur;
   h->iteration += nsteps;
-  h->last_launches = (int64_t)nsteps * ns + 1;
+  h->last_launches = (int64_t)nsteps * ns * stage_launches(h) + 1;
   cudaError_t ce = cudaStreamSynchronize(h->stream);
   if (ce != cudaSuccess) return h->cuda_fail(ce, "profiling stages");
   for (int stg = 0; stg < 2 * ns; ++stg) ms[stg] = 0.0;

@@ -119,6 +119,24 @@ def test_fp32c_dipole_run_within_bound(llg, oracle, name):
     assert np.abs(s.get_state(0) - ref).max() <= FP32C_RUN_TOL
 
 
+@pytest.mark.parametrize("name, per_evaluation", [("bcc3_periodic", 7), ("sc_film_open_z", 7), ("triangular_rk4", 5)])
+def test_dipole_launches_are_counted(llg, name, per_evaluation):
+    """Each stage evaluates the dipole field first: the forward real pass,
+    one complex pass per further grid axis, the k-space product, the passes
+    back and the inverse real pass (7 kernels on a 3-D grid, 5 on a
+    monolayer), per replica."""
+    w = cases()[name]
+    s = llg.Solver(w, precision=llg.FP32C, steps_per_graph=4)
+    for r in range(len(w.replicas)):
+        s.set_state(start(w, r), r)
+    s.step(8)
+    stages = 2 if w.model.integrator == W.HEUN else 4
+    tiled = s.kernel_info()["family"] != "generic"
+    blocks = 2   # two 4-step graph blocks; the gather form ends each with a step-counter kernel
+    want = 8 * stages * (1 + per_evaluation * len(w.replicas)) + (0 if tiled else blocks)
+    assert s.last_launch_count == want
+
+
 def test_dipole_tilings_agree(llg):
     """The tiled kernels add the FFT field like the other local terms: every
     tiling gives the same state."""
