@@ -119,13 +119,34 @@ def test_fp32c_dipole_run_within_bound(llg, oracle, name):
     assert np.abs(s.get_state(0) - ref).max() <= FP32C_RUN_TOL
 
 
-@pytest.mark.parametrize("name, per_evaluation", [("bcc3_periodic", 7), ("sc_film_open_z", 7), ("triangular_rk4", 5)])
+@pytest.mark.parametrize("prec", ["FP64", "FP32C"])
+def test_replicas_of_different_sizes_each_get_their_own_grid(llg, oracle, prec):
+    """Replicas of one handle with different lattices: each has its own FFT
+    grid, tensors and plans (register lengths 16 and 32 beside Stockham
+    lengths 6, 10 and 12), evaluated back to back into one set of planes."""
+    w = W.sc_ferromagnet(L=16, dipole_cutoff=1.5)
+    w.replicas = [W.Replica(L=(16, 16, 32)), W.Replica(L=(12, 10, 6)), W.Replica(L=(16, 16, 16))]
+    s = llg.Solver(w, precision=getattr(llg, prec))
+    k = [t.kind for t in w.model.terms].index(W.TERM_DIPOLE)
+    tol = FP64_DIPOLE_TOL if prec == "FP64" else FP32C_DIPOLE_TOL
+    for r in range(len(w.replicas)):
+        s.set_state(start(w, r), r)
+    for r in range(len(w.replicas)):
+        wr = copy.deepcopy(w)
+        wr.replicas = [w.replicas[r]]
+        want = oracle_dipole_field(oracle, wr, start(w, r))
+        got = s.term_fields(k, r)
+        assert np.abs(got - want).max() <= tol * np.abs(want).max(), r
+
+
+@pytest.mark.parametrize("name, per_evaluation", [("bcc3_periodic", 7), ("sc_film_open_z", 7), ("triangular_rk4", 5),
+                                                   ("bcc16_periodic", 7)])
 def test_dipole_launches_are_counted(llg, name, per_evaluation):
     """Each stage evaluates the dipole field first: the forward real pass,
     one complex pass per further grid axis, the k-space product, the passes
     back and the inverse real pass (7 kernels on a 3-D grid, 5 on a
-    monolayer), per replica."""
-    w = cases()[name]
+    monolayer), per replica, whichever transform kernels take the axes."""
+    w = {**cases(), **transform_cases()}[name]
     s = llg.Solver(w, precision=llg.FP32C, steps_per_graph=4)
     for r in range(len(w.replicas)):
         s.set_state(start(w, r), r)
