@@ -411,9 +411,11 @@ __global__ void __launch_bounds__(FusedGeo<F, TY>::NT, MINB)
       llg_rhs_t(L, s, h, w0, k);
       const float4 a4 = ring0[(x & 3) * G0::PLANE + core.own0 + b * G0::PY * G0::PZ];
       const float a[3] = {a4.x, a4.y, a4.z};
+      // s1 = unit(a + dt/2 rhs(s_pred)), a = s0 + dt/2 rhs(s0): the
+      // stored-rhs stage kernels' operations
       const float hdt = fm(0.5f, dt);
-      float v[3] = {ff(hdt, fa(rhs0[0], k[0]), a[0]), ff(hdt, fa(rhs0[1], k[1]), a[1]),
-                    ff(hdt, fa(rhs0[2], k[2]), a[2])};
+      const float ap[3] = {ff(hdt, rhs0[0], a[0]), ff(hdt, rhs0[1], a[1]), ff(hdt, rhs0[2], a[2])};
+      float v[3] = {ff(hdt, k[0], ap[0]), ff(hdt, k[1], ap[1]), ff(hdt, k[2], ap[2])};
       normalise_t(v);
       if (LLG_IN_RANGE(P, i, 0, (int64_t)V.L[0] * st0)) {
         if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);

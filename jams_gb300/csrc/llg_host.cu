@@ -162,7 +162,7 @@ struct llg_handle {
   // tiled FP32 path (lattice matched a stencil family)
   int family = kFamNone;
   bool tiled = false;
-  bool store_mode = false;   // Heun: predictor stores rhs(s0) instead of the corrector recomputing it
+  bool store_mode = false;   // Heun: predictor stores s0 + dt/2 rhs(s0) instead of the corrector recomputing rhs(s0)
   int occupancy = 2;         // tiled kernels compiled for >= 2, 3 or 4 CTAs per SM
   int tz = 0, ty = 0;
   int rpt = 1;               // rows per thread of the tiled kernels (1 or 2)
@@ -1242,7 +1242,7 @@ bool launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
       float* s0 = buf<float>(h, cur);
       float* sp = buf<float>(h, 1);
       float* s1 = buf<float>(h, 2 - cur);
-      // rhs(s0) stored by the predictor for the corrector
+      // s0 + dt/2 rhs(s0) stored by the predictor for the corrector
       float* rhs0 = reinterpret_cast<float*>(h->aux.p);
       if (stage == 0)
         heun_predict_f32<<<grid, kBlock, 0, st>>>(P, s0, sp, rhs0, ks);

@@ -446,7 +446,7 @@ __device__ __forceinline__ Me whoami(const Params& P, const ReplicaDev*& Rp) {
 // ================================================================== Heun ==
 
 // predictor: s_pred = unit(s0 + dt rhs(s0)); FP64 also stores ds = rhs/2
-// rhs0 (non-null): rhs(s0) stored for the corrector
+// rhs0 (non-null): the corrector's partial sum s0 + dt/2 rhs(s0) stored
 __global__ void __launch_bounds__(kBlock) heun_predict_f32(const __grid_constant__ Params P, const float* __restrict__ s0,
                                                           float* __restrict__ sp, float* __restrict__ rhs0,
                                                           uint32_t kstep) {
@@ -471,15 +471,17 @@ __global__ void __launch_bounds__(kBlock) heun_predict_f32(const __grid_constant
   O.y[me.gi] = v[1];
   O.z[me.gi] = v[2];
   if (rhs0) {
+    const float hdt = 0.5f * P.dt32;
     const Planes<float> A = planes(rhs0, P.npad);
-    A.x[me.gi] = rhs[0];
-    A.y[me.gi] = rhs[1];
-    A.z[me.gi] = rhs[2];
+    A.x[me.gi] = __fmaf_rn(hdt, rhs[0], s[0]);
+    A.y[me.gi] = __fmaf_rn(hdt, rhs[1], s[1]);
+    A.z[me.gi] = __fmaf_rn(hdt, rhs[2], s[2]);
   }
 }
 
-// corrector: s1 = unit(s0 + dt (rhs(s0) + rhs(s_pred)) / 2); rhs(s0) read
-// from the predictor's store (rhs0 non-null, the same value) or recomputed
+// corrector: s1 = unit(a + dt/2 rhs(s_pred)) with a = s0 + dt/2 rhs(s0),
+// read from the predictor's store (rhs0 non-null, the same value) or
+// recomputed
 __global__ void __launch_bounds__(kBlock) heun_correct_f32(const __grid_constant__ Params P, const float* __restrict__ s0,
                                                           const float* __restrict__ sp, float* __restrict__ s1,
                                                           const float* __restrict__ rhs0, uint32_t kstep) {
@@ -489,29 +491,32 @@ __global__ void __launch_bounds__(kBlock) heun_correct_f32(const __grid_constant
   const ReplicaDev& R = *Rp;
   const uint64_t step = *P.step_base + kstep;
   const Site st = locate(R, P.nb, me.i);
-  const Planes<const float> S0 = planes(s0, P.npad);
   const Planes<const float> SP = planes(sp, P.npad);
-  const float a[3] = {S0.x[me.gi], S0.y[me.gi], S0.z[me.gi]};
   const float p[3] = {SP.x[me.gi], SP.y[me.gi], SP.z[me.gi]};
+  const float hdt = 0.5f * P.dt32;
   float w[3];
   noise_f32(P, R, me.r, st.b, me.i, step, w);
-  float h[3], r0[3], r1[3];
+  float h[3], a[3], r1[3];
   if (rhs0) {
     const Planes<const float> A = planes(rhs0, P.npad);
-    r0[0] = A.x[me.gi];
-    r0[1] = A.y[me.gi];
-    r0[2] = A.z[me.gi];
+    a[0] = A.x[me.gi];
+    a[1] = A.y[me.gi];
+    a[2] = A.z[me.gi];
   }
   field_f32(P, R, st, me.gi, SP, p, h, P.hdip32, pulse_at32(P, step, 1));
   rhs_f32(P, st.b, p, h, w, r1);
   if (!rhs0) {
-    field_f32(P, R, st, me.gi, S0, a, h, P.hdip32_s0, pulse_at32(P, step, 0));
-    rhs_f32(P, st.b, a, h, w, r0);
+    const Planes<const float> S0 = planes(s0, P.npad);
+    const float q[3] = {S0.x[me.gi], S0.y[me.gi], S0.z[me.gi]};
+    float r0[3];
+    field_f32(P, R, st, me.gi, S0, q, h, P.hdip32_s0, pulse_at32(P, step, 0));
+    rhs_f32(P, st.b, q, h, w, r0);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) a[m] = __fmaf_rn(hdt, r0[m], q[m]);
   }
-  const float hdt = 0.5f * P.dt32;
   float v[3];
 #pragma unroll
-  for (int m = 0; m < 3; ++m) v[m] = __fmaf_rn(hdt, r0[m] + r1[m], a[m]);
+  for (int m = 0; m < 3; ++m) v[m] = __fmaf_rn(hdt, r1[m], a[m]);
   normalise_f32(v);
   flag_nonfinite(P, v);
   const Planes<float> O = planes(s1, P.npad);

@@ -777,9 +777,10 @@ __device__ __forceinline__ void issue_plane(const CUtensorMap* map, const View& 
 
 }  // namespace
 
-// STAGE: 0 Heun predictor (writes sp; with aux != null also rhs0 into aux)
+// STAGE: 0 Heun predictor (writes sp; with aux != null also the corrector's
+//          partial sum s0 + dt/2 rhs(s0) into aux)
 //        1 Heun corrector recomputing rhs(s0) (rings of s0 and sp)
-//        2 Heun corrector from stored rhs0 (ring of sp; own s0 and aux)
+//        2 Heun corrector from the stored partial sum (ring of sp; own aux)
 //        3..6 RK4 stages 1..4 (ring of sin; own s0, aux = k accumulator)
 // RPT: rows per thread.  With RPT = 2 a thread computes two neighbouring
 // rows of its column in every plane, so the per-plane work of a thread
@@ -972,7 +973,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
           w[r][m] = wn[r][m];
           own_s0[r][m] = own_r[r][m] = dip[r][m] = dip0[r][m] = 0.f;
         }
-        if (STAGE >= 2 && ld) {
+        if (STAGE >= 3 && ld) {
           own_s0[r][0] = __ldg(s0x + i);
           own_s0[r][1] = __ldg(s0y + i);
           own_s0[r][2] = __ldg(s0z + i);
@@ -1011,31 +1012,33 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
             oy[i] = v[1];
             oz[i] = v[2];
             if (ax) {
-              ax[i] = k[0];
-              ay[i] = k[1];
-              az[i] = k[2];
+              // the stored-rhs corrector's partial sum s0 + dt/2 rhs(s0)
+              const float hdt = fm(0.5f, dt);
+              ax[i] = ff(hdt, k[0], s[0]);
+              ay[i] = ff(hdt, k[1], s[1]);
+              az[i] = ff(hdt, k[2], s[2]);
             }
           }
         } else if (STAGE == 1 || STAGE == 2) {
-          float a[3], r0[3];
+          // s1 = unit(a + dt/2 rhs(s_pred)), a = s0 + dt/2 rhs(s0): computed
+          // here from the second ring (recompute) or the predictor's store
+          const float hdt = fm(0.5f, dt);
+          float a[3];
           if (STAGE == 1) {
-            float h0[3];
+            float h0[3], s0v[3], r0[3];
             LocalField L0 = L;
             L0.hb[0] = hb0[0];
             L0.hb[1] = hb0[1];
             L0.hb[2] = hb0[2];
-            field_tiled<F, TZ, TY>(L0, TP, b, ring1, x, own[r], cy1[r], h0, a, has_dip, dip0[r]);
-            llg_rhs_t(L, a, h0, w[r], r0);
+            field_tiled<F, TZ, TY>(L0, TP, b, ring1, x, own[r], cy1[r], h0, s0v, has_dip, dip0[r]);
+            llg_rhs_t(L, s0v, h0, w[r], r0);
+#pragma unroll
+            for (int m = 0; m < 3; ++m) a[m] = ff(hdt, r0[m], s0v[m]);
           } else {
 #pragma unroll
-            for (int m = 0; m < 3; ++m) {
-              a[m] = own_s0[r][m];
-              r0[m] = own_r[r][m];
-            }
+            for (int m = 0; m < 3; ++m) a[m] = own_r[r][m];
           }
-          const float hdt = fm(0.5f, dt);
-          float v[3] = {ff(hdt, fa(r0[0], k[0]), a[0]), ff(hdt, fa(r0[1], k[1]), a[1]),
-                        ff(hdt, fa(r0[2], k[2]), a[2])};
+          float v[3] = {ff(hdt, k[0], a[0]), ff(hdt, k[1], a[1]), ff(hdt, k[2], a[2])};
           normalise_t(v);
           if (st) {
             if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) atomicOr(P.status, 1u);
