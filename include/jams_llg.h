@@ -289,10 +289,11 @@ int llg_kernel_info(const llg_handle *h, int32_t *info);
 /* Tiling choice of the tiled FP32 kernels (no effect on other kernels):
    planes streamed per CTA (rounded up to even: the thermal noise of planes
    x and x + 1, x even, comes from one draw); flags bit 0: the Heun
-   predictor stores rhs(s0); bit 1: the narrow tile (half the rows, twice
-   the CTAs, for lattices too small to fill the GPU); bit 2: two rows per
-   thread (wide tile of sc, bcc and fcc lattices, no dipole term; occupancy
-   2 only); bit 3: the fused Heun step, one kernel per step that computes
+   predictor stores the corrector's partial sum s0 + dt/2 rhs(s0); bit 1:
+   the narrow tile (half the rows, twice the CTAs, for lattices too small
+   to fill the GPU); bit 2: two rows per thread (wide tile of sc, bcc and
+   fcc lattices, no dipole term; occupancy 2 only); bit 3:
+   the fused Heun step, one kernel per step that computes
    the predictor of its tile and a one-reach halo in shared memory and the
    corrector in the same sweep (sc, bcc and fcc lattices, no dipole term;
    bits 0 and 2 clear; bit 1 picks its narrow tile); flags >> 4: occupancy

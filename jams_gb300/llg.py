@@ -433,10 +433,12 @@ class Solver:
 
     def set_tuning(self, planes_per_cta: int, store_rhs: bool, occupancy: int = 2, narrow: bool = False,
                    pair: bool = False, fused: bool = False, tma: bool = False) -> None:
-        """Tiling of the tiled FP32 kernels: planes per CTA, stored rhs(s0)
-        (Heun), occupancy variant 2/3/4, narrow tile (half the rows), two
-        rows per thread, the fused Heun step (one kernel per step), planes
-        loaded by TMA."""
+        """Tiling of the tiled FP32 kernels: planes per CTA, stored-rhs mode
+        (Heun: the predictor stores the corrector's partial sum s0 + dt/2
+        rhs(s0) instead of the corrector recomputing rhs(s0)), occupancy
+        variant 2/3/4 (two rows per thread: 2), narrow tile (half the
+        rows), two rows per thread, the fused Heun step (one kernel per
+        step), planes loaded by TMA."""
         flags = int(bool(store_rhs)) | (int(bool(narrow)) << 1) | (int(bool(pair)) << 2) | \
             (int(bool(fused)) << 3) | (int(occupancy) << 4) | (int(bool(tma)) << 8)
         self._check(self.L.llg_set_tuning(self.h, int(planes_per_cta), flags))
