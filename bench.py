@@ -64,7 +64,7 @@ STAGE_BYTES = {
     ("rk4", "fp32c"): [36, 60, 60, 48],
     ("rk4", "fp64"): [72, 120, 120, 96],
 }
-# BASELINE metric: spin-steps/s of the FP32C and FP64 forms and the HBM
+# the metric: spin-steps/s of the FP32C and FP64 forms and the HBM
 # fraction, on one GPU
 METRIC = "LLG spin-steps/s on 1 GB300: FP32 vs FP64 form at \u22641e-5 max|\u0394S|; % of HBM peak"
 # the default line also carries these workloads, each as an object of its own
