@@ -629,8 +629,12 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
     cudaError_t ce = cudaSuccess;
     for (int k = 0; k < 3 && ce == cudaSuccess; ++k) {
       const int n = R->M[k];
-      if (n > 7168) {
-        err = "dipole: a grid axis of " + std::to_string(n) + " cells is longer than the transform supports (7168)";
+      // one line of a shared-memory pass: two buffers and the twiddle table
+      // within a CTA's 227 KB (4842 points in FP64, 9685 in FP32)
+      const int max_axis = (int)(227 * 1024 / (3 * (fp64 ? sizeof(double2) : sizeof(float2))));
+      if (n > max_axis) {
+        err = "dipole: a grid axis of " + std::to_string(n) + " cells is longer than the transform supports (" +
+              std::to_string(max_axis) + ")";
         delete D;
         return nullptr;
       }
