@@ -328,6 +328,7 @@ cudaError_t allow_smem(const void* kernel, size_t bytes) {
     if (e.first == kernel && e.second >= bytes) return cudaSuccess;
   const cudaError_t ce = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (ce == cudaSuccess) have.push_back({kernel, bytes});
+  else cudaGetLastError();   // returned here: not left for a later check to find
   return ce;
 }
 
@@ -595,6 +596,7 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
     err = "dipole: lattice_parameter and r_cutoff must be positive";
     return nullptr;
   }
+  cudaGetLastError();   // errors below are this call's own
   DipoleField* D = new DipoleField();
   D->fp64 = fp64;
   D->nb = nb;
@@ -629,9 +631,10 @@ DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3
     cudaError_t ce = cudaSuccess;
     for (int k = 0; k < 3 && ce == cudaSuccess; ++k) {
       const int n = R->M[k];
-      // one line of a shared-memory pass: two buffers and the twiddle table
-      // within a CTA's 227 KB (4842 points in FP64, 9685 in FP32)
-      const int max_axis = (int)(227 * 1024 / (3 * (fp64 ? sizeof(double2) : sizeof(float2))));
+      // one line of a shared-memory pass, two buffers and the twiddle table,
+      // within a CTA's 227 KB: 4842 points in FP64, the precision of the
+      // tensors' transforms in either form
+      const int max_axis = (int)(227 * 1024 / (3 * sizeof(double2)));
       if (n > max_axis) {
         err = "dipole: a grid axis of " + std::to_string(n) + " cells is longer than the transform supports (" +
               std::to_string(max_axis) + ")";

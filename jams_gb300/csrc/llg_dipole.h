@@ -29,8 +29,8 @@ struct DipoleField;
 // Builds the k-space tensors, transform plans and twiddle tables of every
 // replica.  Returns null and sets err when the geometry is invalid (cutoff
 // beyond the inradius of the periodic supercell, coincident sites, a grid
-// axis longer than one shared-memory transform line: 4842 points in FP64,
-// 9685 in FP32) or a CUDA call fails.
+// axis longer than one shared-memory transform line of the FP64 tensor
+// transforms, 4842 points) or a CUDA call fails.
 DipoleField* dipole_create(const DipoleGeometry& g, int nb, const int periodic[3], const double* mus,
                            const std::vector<DipoleReplicaSpec>& reps, bool fp64, std::string& err);
 void dipole_destroy(DipoleField* d);

@@ -84,7 +84,7 @@ struct FftPlan1D {
 };
 
 // radices of n: 4 while more than 4 remains, then 4, 2, 3, 5, 7 and the
-// remaining primes (n <= 9685 needs at most 13 stages)
+// remaining primes (n <= 4842 needs at most 12 stages)
 inline FftPlan1D fft_plan(int n) {
   FftPlan1D p;
   p.n = n;

@@ -1309,6 +1309,7 @@ int llg_create(const llg_desc* desc, llg_handle** out) {
   *out = nullptr;
   llg_handle* h = new (std::nothrow) llg_handle();
   if (!h) return tls_fail(LLG_ERR_OOM, "host allocation failed");
+  cudaGetLastError();   // a launch error found below is this handle's own
   int rc = build(h, desc);
   if (rc == 0) h->model_hash = model_hash(desc);
   if (rc == 0) rc = sync_replicas(h);

@@ -184,14 +184,17 @@ def test_dipole_from_config_equals_oracle(llg, oracle):
     assert np.abs(s.get_state(0) - ref).max() <= FP64_RUN_TOL
 
 
-def test_axis_longer_than_a_shared_memory_line_is_an_error(llg):
+@pytest.mark.parametrize("prec", ["FP64", "FP32C"])
+def test_axis_longer_than_a_shared_memory_line_is_an_error(llg, prec):
     """An open axis of 2500 cells is a 5000-point transform line: one line
-    of a shared-memory pass (two buffers and the twiddles) fits a CTA in
-    single precision but not in double."""
+    of a shared-memory pass (two buffers and the twiddles) does not fit a
+    CTA in double precision, the precision of the tensors' transforms in
+    both forms.  The refusal leaves no error behind for the next handle."""
     w = W.sc_ferromagnet(L=(4, 4, 2500), periodic=(1, 1, 0), dipole_cutoff=1.5)
     with pytest.raises(llg.LLGError, match="longer than the transform supports"):
-        llg.Solver(w, precision=llg.FP64)
-    llg.Solver(w, precision=llg.FP32C).close()
+        llg.Solver(w, precision=getattr(llg, prec))
+    ok = W.sc_ferromagnet(L=(4, 4, 2400), periodic=(1, 1, 0), dipole_cutoff=1.5)   # 4800 points
+    llg.Solver(ok, precision=getattr(llg, prec)).close()
 
 
 def test_dipole_cutoff_beyond_inradius_is_an_error(llg):
