@@ -134,6 +134,8 @@ def kernel_name(info: dict, integ: str, stage: int, precision: str, dipole: bool
             return "fused_heun<%s, %d, %d>" % (fam, info["tile_y"], minb)
         if integ == "heun":
             st = 0 if stage == 0 else (2 if info["store_rhs"] else 1)
+            if info.get("stored_noise"):
+                st = {0: 7, 2: 8}[st]   # stages 0 and 2 that store / load the thermal field
         else:
             st = 3 + stage
         rpt = info.get("rows_per_thread", 1) or 1
@@ -171,7 +173,7 @@ def parse(argv=None):
     p.add_argument("--profile-steps", type=int, default=50)
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--tuning", default="", help="planes_per_cta,flags,occupancy instead of autotuning (flags: 1 stored rhs, 2 narrow tile, "
-                        "4 two rows per thread, 8 the fused Heun step, 256 TMA plane loads)")
+                        "4 two rows per thread, 8 the fused Heun step, 256 TMA plane loads, 512 stored noise)")
     return p.parse_args(argv)
 
 
@@ -537,7 +539,8 @@ def make_solver(llg, w, prec, local, stream, tuning_arg: str = "", tune: bool = 
         sol.set_state(W.initial_state(w, r), r)
     if tuning_arg:
         tx, fl, oc = (int(v) for v in tuning_arg.split(","))
-        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2), bool(fl & 4), bool(fl & 8), bool(fl & 256))
+        sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2), bool(fl & 4), bool(fl & 8), bool(fl & 256),
+                       bool(fl & 512))
         tuning = sol.kernel_info()
     else:
         # the choice is cached per lattice shape ($JAMS_LLG_TUNE_CACHE), so a

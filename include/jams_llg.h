@@ -283,7 +283,8 @@ int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
    occupancy variant (CTAs per SM the tiled kernels were compiled for),
    info[7] rows computed per thread (1 or 2; 0 without tiled kernels),
    info[8] 1 when each Heun step is one fused kernel (predictor and
-   corrector in one sweep).  info holds 9 values. */
+   corrector in one sweep), info[9] 1 with TMA plane loads, info[10] 1 in
+   stored-noise mode.  info holds 11 values. */
 int llg_kernel_info(const llg_handle *h, int32_t *info);
 
 /* Tiling choice of the tiled FP32 kernels (no effect on other kernels):
@@ -298,8 +299,10 @@ int llg_kernel_info(const llg_handle *h, int32_t *info);
    corrector in the same sweep (sc, bcc and fcc lattices, no dipole term;
    bits 0 and 2 clear; bit 1 picks its narrow tile); flags >> 4: occupancy
    variant, 2 (<= 128 registers), 3 (<= 80) or 4 (<= 64); for the fused
-   step 2 or 4 x 256 resident threads per SM.  Every choice gives the same
-   results bit for bit. */
+   step 2 or 4 x 256 resident threads per SM; bit 8: TMA plane loads; bit
+   9: stored noise (with bit 0: the predictor also stores the step's thermal
+   field, which the corrector reads instead of drawing it again).  Every
+   choice gives the same results bit for bit. */
 int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t flags);
 
 /* Times every tiling candidate (planes per CTA 2..64, stored or recomputed

@@ -136,6 +136,7 @@ struct llg_handle {
   // device
   DevBuf<unsigned char> state[3];  // spin planes (float or double)
   DevBuf<unsigned char> aux;       // FP64 Heun ds / RK4 accumulator
+  DevBuf<float> noise;             // stored-noise mode: the step's thermal field planes
   DevBuf<ReplicaDev> d_rep;
   DevBuf<int2> d_tiles;
   DevBuf<int32_t> d_tab32;
@@ -162,6 +163,7 @@ struct llg_handle {
   // tiled FP32 path (lattice matched a stencil family)
   int family = kFamNone;
   bool tiled = false;
+  bool store_noise = false;  // Heun, stored-rhs mode: the predictor stores the thermal field for the corrector
   bool store_mode = false;   // Heun: predictor stores s0 + dt/2 rhs(s0) instead of the corrector recomputing rhs(s0)
   int occupancy = 2;         // tiled kernels compiled for >= 2, 3 or 4 CTAs per SM
   int tz = 0, ty = 0;
@@ -1210,10 +1212,14 @@ bool launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
       // TMA: the tensor map of the buffer the stage gathers from
       const CUtensorMap* m0 = h->tma ? &h->tmaps[cur] : nullptr;
       const CUtensorMap* m1 = h->tma ? &h->tmaps[1] : nullptr;
+      // stored-noise mode: stages 7 and 8 are stages 0 and 2 that write /
+      // read the thermal field planes
+      Params PN = P;
+      if (h->store_noise) PN.noise32 = h->noise.p;
       if (stage == 0)
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 0, g4, st, P, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, advance, h->dipole != nullptr, m0);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, h->store_noise ? 7 : 0, g4, st, PN, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, advance, h->dipole != nullptr, m0);
       else if (h->store_mode)
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 2, g4, st, P, h->TP, s0, sp, s0, aux, ks, advance, h->dipole != nullptr, m1);
+        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, h->store_noise ? 8 : 2, g4, st, PN, h->TP, s0, sp, s0, aux, ks, advance, h->dipole != nullptr, m1);
       else
         launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, advance, h->dipole != nullptr, m1);
     } else {
@@ -1445,7 +1451,7 @@ static int step_blocks(llg_handle* h, int32_t nsteps) {
   while (remaining > 0) {
     const int n = remaining >= K && K > 1 ? K : remaining;
     GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX + 8192 * h->ty +
-                     131072 * h->rpt + 524288 * (h->fused ? 1 : 0) + 1048576 * (h->tma ? 1 : 0),
+                     131072 * h->rpt + 524288 * (h->fused ? 1 : 0) + 1048576 * (h->tma ? 1 : 0) + 2097152 * (h->store_noise ? 1 : 0),
                  n};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end() && (n == K || h->graphs.size() < kMaxGraphs)) {
@@ -1756,6 +1762,7 @@ int llg_kernel_info(const llg_handle* h, int32_t* info) {
   info[7] = h->tiled ? h->rpt : 0;
   info[8] = h->fused ? 1 : 0;
   info[9] = h->tma ? 1 : 0;
+  info[10] = h->store_noise ? 1 : 0;
   return 0;
 }
 
@@ -1860,6 +1867,18 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
     int rc = build_tensor_maps(h);
     if (rc) return rc;
     h->tma = true;
+  }
+  // bit 9: stored noise (the Heun predictor stores the thermal field for
+  // the stored-rhs corrector)
+  h->store_noise = false;
+  if (store_rhs & 512) {
+    if (!h->store_mode || fused)
+      return h->fail(LLG_ERR_BAD_DESC, "stored noise: the two-pass Heun kernels in stored-rhs mode only");
+    if (!h->noise.p) {
+      ce = h->noise.alloc((size_t)3 * h->npad);
+      if (ce != cudaSuccess) return h->cuda_fail(ce, "alloc noise planes");
+    }
+    h->store_noise = true;
   }
   return 0;
 }
@@ -1968,6 +1987,13 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
     }
     h->ty = ty0;
   }
+  // stored noise: the stored-rhs Heun candidates again, where some replica
+  // is above 0 K (at 0 K there is no noise to store)
+  if (h->integrator == LLG_HEUN && std::any_of(h->rep_T.begin(), h->rep_T.end(), [](double T) { return T > 0.0; })) {
+    const size_t n0 = cands.size();
+    for (size_t c = 0; c < n0; ++c)
+      if (cands[c].second & 1) cands.push_back({cands[c].first, cands[c].second | 512});
+  }
   // the fused Heun step: wide or narrow tile, occupancy 2 or 4 (x 256 threads)
   if (h->integrator == LLG_HEUN && fused_supported(h->family) && !h->dipole)
     for (int t : {2, 4, 8, 16, 32, 64})
@@ -1986,7 +2012,7 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   std::pair<int, int> choice = {h->TP.TX, h->fused ? (8 | (h->fused_wide ? 0 : 2) | (h->occupancy << 4))
                                                    : ((h->store_mode ? 1 : 0) | (h->ty != wide_ty0 ? 2 : 0) |
                                                       (h->rpt == 2 ? 4 : 0) | (h->occupancy << 4) |
-                                                      (h->tma ? 256 : 0))};
+                                                      (h->tma ? 256 : 0) | (h->store_noise ? 512 : 0))};
   // each trial runs as llg_step runs steps: one CUDA graph of trial_steps
   // steps (captured and run once untimed, then timed)
   const int spg0 = h->steps_per_graph;

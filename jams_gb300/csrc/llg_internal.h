@@ -145,6 +145,10 @@ struct Params {
   const float* hdip32_s0;
   const double* hdip64;
   const double* hdip64_s0;
+  // the thermal field planes of the step (T, three planes of npad): written
+  // by the tiled Heun predictor and read by the stored-rhs corrector in
+  // stored-noise mode; null otherwise
+  float* noise32;
   // time-dependent fields (null without): kPulseVals factors per stage of
   // every step from iteration *pulse_base on, [step][stage][kPulseVals], and
   // the factors at the current solver time for fields and energies

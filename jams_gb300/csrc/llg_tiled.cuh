@@ -781,6 +781,11 @@ __device__ __forceinline__ void issue_plane(const CUtensorMap* map, const View& 
 //          partial sum s0 + dt/2 rhs(s0) into aux)
 //        1 Heun corrector recomputing rhs(s0) (rings of s0 and sp)
 //        2 Heun corrector from the stored partial sum (ring of sp; own aux)
+//        7 stage 0 that also writes the step's thermal field (P.noise32)
+//        8 stage 2 that reads the thermal field instead of drawing it again
+//          (stored-noise mode: 12 B per spin more traffic each way, no
+//          second Philox draw and Box-Muller in the corrector; the same
+//          values, so the same results)
 //        3..6 RK4 stages 1..4 (ring of sin; own s0, aux = k accumulator)
 // RPT: rows per thread.  With RPT = 2 a thread computes two neighbouring
 // rows of its column in every plane, so the per-plane work of a thread
@@ -790,12 +795,16 @@ __device__ __forceinline__ void issue_plane(const CUtensorMap* map, const View& 
 // TMA: the gathered state's planes arrive by TMA box loads (tmap: the
 // tensor map of the buffer the stage gathers from); one ring only, so STAGE 1
 // (two rings) always stages through registers.
-template <class F, int TZ, int TY, int RPT, int STAGE, int MINB, bool DIP, bool TMA>
+template <class F, int TZ, int TY, int RPT, int STG, int MINB, bool DIP, bool TMA>
 __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     tiled_stage(const __grid_constant__ Params P, const __grid_constant__ TiledParams TP, const float* s0,
                 const float* sin, float* out, float* aux, uint32_t kstep, uint32_t advance,
                 const __grid_constant__ CUtensorMap tmap) {
   using G = Geo<F, TZ, TY, RPT>;
+  // the stage computed; stages 7 and 8 are stages 0 and 2 that store / load
+  // the thermal field
+  constexpr int STAGE = STG == 7 ? 0 : (STG == 8 ? 2 : STG);
+  constexpr bool WSTORE = STG == 7, WLOAD = STG == 8;
   constexpr int NR = STAGE == 1 ? 2 : 1;
   constexpr int TYT = TY / RPT;   // thread rows per basis site
   constexpr bool USE_TMA = TMA && NR == 1;
@@ -983,6 +992,10 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
           own_r[r][1] = ay[i];
           own_r[r][2] = az[i];
         }
+        if (WLOAD && ld) {
+#pragma unroll
+          for (int m = 0; m < 3; ++m) w[r][m] = __ldg(P.noise32 + m * P.npad + V.offset + i);
+        }
         if (has_dip && ld) {
 #pragma unroll
           for (int m = 0; m < 3; ++m) dip[r][m] = __ldg(P.hdip32 + m * P.npad + V.offset + i);
@@ -992,7 +1005,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
           }
         }
       }
-      if (thermal && (x & 1) == 0) {
+      if (!WLOAD && thermal && (x & 1) == 0) {
 #pragma unroll
         for (int r = 0; r < RPT; ++r)
           noise_pair(P.philox_keys, (uint32_t)tile.x, step, (uint32_t)ir[r], amp, w[r], wn[r]);
@@ -1017,6 +1030,10 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
               ax[i] = ff(hdt, k[0], s[0]);
               ay[i] = ff(hdt, k[1], s[1]);
               az[i] = ff(hdt, k[2], s[2]);
+            }
+            if (WSTORE) {
+#pragma unroll
+              for (int m = 0; m < 3; ++m) P.noise32[m * P.npad + V.offset + i] = w[r][m];
             }
           }
         } else if (STAGE == 1 || STAGE == 2) {
@@ -1164,7 +1181,9 @@ cudaError_t launch_family(int stage, unsigned grid, cudaStream_t st, const Param
     case 3: return launch_one<F, TZ, TY, RPT, 3, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
     case 4: return launch_one<F, TZ, TY, RPT, 4, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
     case 5: return launch_one<F, TZ, TY, RPT, 5, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
-    default: return launch_one<F, TZ, TY, RPT, 6, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+    case 6: return launch_one<F, TZ, TY, RPT, 6, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+    case 7: return launch_one<F, TZ, TY, RPT, 7, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
+    default: return launch_one<F, TZ, TY, RPT, 8, MINB, DIP, TMA>(grid, st, P, TP, s0, sin, out, aux, k, adv, map);
   }
 }
 

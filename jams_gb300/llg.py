@@ -420,27 +420,28 @@ class Solver:
         return (ms[:ns], ms[ns:2 * ns]) if dipole else ms[:ns]
 
     def kernel_info(self) -> dict:
-        info = (ctypes.c_int32 * 10)()
+        info = (ctypes.c_int32 * 11)()
         self._check(self.L.llg_kernel_info(self.h, info))
         fam = {0: "generic", 1: "sc", 2: "bcc", 3: "bcc3", 4: "triangular", 5: "fcc", 6: "fcc2"}[info[0]]
         return {"family": fam, "planes_per_cta": info[1], "store_rhs": bool(info[2]), "tile_z": info[3],
                 "tile_y": info[4], "fp64": bool(info[5]), "occupancy": info[6], "rows_per_thread": info[7],
-                "fused": bool(info[8]), "tma": bool(info[9])}
+                "fused": bool(info[8]), "tma": bool(info[9]), "stored_noise": bool(info[10])}
 
     def autotune(self, trial_steps: int = 20, use_cache: bool = False) -> dict:
         self._check(self.L.llg_autotune(self.h, int(trial_steps), int(bool(use_cache))))
         return self.kernel_info()
 
     def set_tuning(self, planes_per_cta: int, store_rhs: bool, occupancy: int = 2, narrow: bool = False,
-                   pair: bool = False, fused: bool = False, tma: bool = False) -> None:
+                   pair: bool = False, fused: bool = False, tma: bool = False, noise: bool = False) -> None:
         """Tiling of the tiled FP32 kernels: planes per CTA, stored-rhs mode
         (Heun: the predictor stores the corrector's partial sum s0 + dt/2
         rhs(s0) instead of the corrector recomputing rhs(s0)), occupancy
         variant 2/3/4 (two rows per thread: 2), narrow tile (half the
         rows), two rows per thread, the fused Heun step (one kernel per
-        step), planes loaded by TMA."""
+        step), planes loaded by TMA, stored noise (stored-rhs mode: the
+        predictor also stores the thermal field for the corrector)."""
         flags = int(bool(store_rhs)) | (int(bool(narrow)) << 1) | (int(bool(pair)) << 2) | \
-            (int(bool(fused)) << 3) | (int(occupancy) << 4) | (int(bool(tma)) << 8)
+            (int(bool(fused)) << 3) | (int(occupancy) << 4) | (int(bool(tma)) << 8) | (int(bool(noise)) << 9)
         self._check(self.L.llg_set_tuning(self.h, int(planes_per_cta), flags))
 
     @property

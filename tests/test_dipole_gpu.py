@@ -160,13 +160,14 @@ def test_dipole_launches_are_counted(llg, name, per_evaluation):
 
 def test_dipole_tilings_agree(llg):
     """The tiled kernels add the FFT field like the other local terms: every
-    tiling gives the same state."""
+    tiling gives the same state, stored noise included."""
     w = W.bcc_three_shell(L=(6, 8, 10), T=300.0, start="random", dipole_cutoff=2.9)
     outs = []
-    for tx, store, occ in [(2, False, 2), (4, True, 4), (10, True, 3)]:
+    for tx, store, occ, noise in [(2, False, 2, False), (4, True, 4, False), (10, True, 3, False),
+                                  (4, True, 4, True), (6, True, 2, True)]:
         s = llg.Solver(w, precision=llg.FP32C, steps_per_graph=4)
         assert s.kernel_info()["family"] == "bcc3"
-        s.set_tuning(tx, store, occ)
+        s.set_tuning(tx, store, occ, noise=noise)
         s.set_state(start(w), 0)
         s.step(9)
         outs.append(s.get_state(0))

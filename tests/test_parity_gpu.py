@@ -321,12 +321,21 @@ def test_tiling_choices_give_identical_results(llg, name):
         choices += [(2, True, 4, False, False, False, True), (4, False, 2, False, False, False, True),
                     (6, True, 3, True, False, False, True), (4, True, 2, False, True, False, True),
                     (64, True, 2, False, False, False, True)]
-    for tx, store, occ, narrow, pair, fused, tma in choices:
+    choices = [c + (False,) for c in choices]
+    # stored noise (stored-rhs mode): one and two rows, a narrow tile, TMA
+    choices += [(2, True, 4, False, False, False, False, True), (8, True, 2, False, False, False, False, True),
+                (4, True, 3, True, False, False, False, True)]
+    if name != "tri":
+        choices += [(4, True, 2, False, True, False, False, True)]
+        if len(w.replicas) == 1:
+            choices += [(6, True, 4, False, False, False, True, True)]
+    for tx, store, occ, narrow, pair, fused, tma, noise in choices:
         s = solver(llg, w, llg.FP32C, steps_per_graph=4)
-        s.set_tuning(tx, store, occ, narrow, pair, fused, tma)
+        s.set_tuning(tx, store, occ, narrow, pair, fused, tma, noise)
         assert s.kernel_info()["rows_per_thread"] == (2 if pair else 1)
         assert s.kernel_info()["fused"] == fused
         assert s.kernel_info()["tma"] == tma
+        assert s.kernel_info()["stored_noise"] == noise
         for r in range(len(w.replicas)):
             s.set_state(W.initial_state(w, r), r)
         s.step(11)
@@ -443,6 +452,16 @@ def test_fused_step_is_refused_where_unsupported(llg):
     sc = solver(llg, W.sc_ferromagnet(L=16), llg.FP32C)
     with pytest.raises(llg.LLGError, match="fused step"):
         sc.set_tuning(4, True, 2, False, False, True)
+
+
+def test_stored_noise_needs_stored_rhs_mode(llg):
+    s = solver(llg, W.bcc_nearest_neighbour(L=8, T=300.0), llg.FP32C)
+    with pytest.raises(llg.LLGError, match="stored noise"):
+        s.set_tuning(4, False, 2, noise=True)
+    with pytest.raises(llg.LLGError, match="stored noise"):
+        s.set_tuning(4, False, 2, fused=True, noise=True)
+    s.set_tuning(4, True, 2, noise=True)
+    assert s.kernel_info()["stored_noise"]
 
 
 def test_two_rows_per_thread_is_refused_where_unsupported(llg):
