@@ -342,8 +342,10 @@ int llg_write_array_file(const char *path, const char *dataset, const double *da
 
 /* Reads an array the way the reference loads spins and per-spin parameters
    (load_array_from_file, src/jams/helpers/load.h:14-60): HDF5 dataset
-   `dataset` of a ".h5" file (contiguous or compact float64/float32; chunked
-   or compressed datasets give LLG_ERR_IO), else every number of a text file
+   `dataset` of a ".h5" file (float64/float32, contiguous, compact or
+   chunked with the shuffle and deflate filters of the HDF5 monitor's
+   "compressed" option; other filters and version-4 chunk indexes give
+   LLG_ERR_IO), else every number of a text file
    ('#' and '//' comment lines skipped) with rows = count, cols = 1.
    With data == NULL only *rows and *cols are set; LLG_ERR_BAD_DESC when
    rows x cols exceeds capacity.  Needs no device. */

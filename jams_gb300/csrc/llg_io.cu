@@ -11,9 +11,12 @@
 //    contiguous layout messages, then the raw rows.  The reader follows the
 //    HDF5 File Format Specification (superblock versions 0-3, symbol-table
 //    and compact link-message groups, object header versions 1 and 2 with
-//    continuation blocks, contiguous or compact float32/float64 datasets).
-//    Chunked datasets (the monitor's "compressed" option: chunking + shuffle
-//    + deflate) and dense link storage are rejected with an error.
+//    continuation blocks, contiguous, compact or chunked float32/float64
+//    datasets).  Chunked datasets are read through their version-1 B-tree,
+//    with the deflate and shuffle filters of the monitor's "compressed"
+//    option undone by this file's own zlib decoder.  Version-4 chunk
+//    indexes, other filters and dense link storage are rejected with an
+//    error.
 //  * anything else: whitespace-separated text, '#' or '//' comment lines,
 //    every number read in file order.
 //
@@ -512,6 +515,376 @@ bool find_link(File& F, uint64_t group_header, const std::string& name, uint64_t
   return false;
 }
 
+// --------------------------------------------------------------- inflate --
+//
+// Decoder of the zlib format (RFC 1950) around a DEFLATE stream (RFC 1951),
+// the encoding of the HDF5 deflate filter (filter 1).  Stored, fixed- and
+// dynamic-Huffman blocks; the Adler-32 trailer is checked.  Huffman codes
+// decode through one lookup table per code, indexed by the next (longest
+// code length) input bits: the codes are canonical, so each is written into
+// every slot whose low bits are its bit-reversed value.
+
+struct BitReader {
+  const uint8_t* p;
+  size_t n, pos = 0;
+  uint64_t buf = 0;
+  int cnt = 0;
+  size_t pad = 0;  // zero bytes supplied past the end of the input
+
+  BitReader(const uint8_t* p_, size_t n_) : p(p_), n(n_) {}
+  void fill(int k) {
+    while (cnt < k) {
+      uint64_t b = 0;
+      if (pos < n) b = p[pos++];
+      else ++pad;
+      buf |= b << cnt;
+      cnt += 8;
+    }
+  }
+  uint32_t peek(int k) {
+    fill(k);
+    return (uint32_t)(buf & ((1ull << k) - 1));
+  }
+  void drop(int k) {
+    buf >>= k;
+    cnt -= k;
+  }
+  uint32_t bits(int k) {
+    const uint32_t v = peek(k);
+    drop(k);
+    return v;
+  }
+  void align() { drop(cnt & 7); }
+  // true once a bit past the end of the input has been consumed
+  bool overrun() const { return pad * 8 > (size_t)cnt; }
+};
+
+struct HuffTable {
+  int maxlen = 0;
+  std::vector<uint16_t> slot;  // (symbol << 4) | code length; 0 = no code
+};
+
+// canonical code from the code lengths; false for an over-subscribed set
+bool huff_build(const uint8_t* len, int n, HuffTable& t) {
+  int count[16] = {0};
+  for (int i = 0; i < n; ++i) count[len[i]]++;
+  count[0] = 0;
+  int left = 1;
+  t.maxlen = 0;
+  for (int l = 1; l < 16; ++l) {
+    left = 2 * left - count[l];
+    if (left < 0) return false;
+    if (count[l]) t.maxlen = l;
+  }
+  if (t.maxlen == 0) t.maxlen = 1;  // no codes: every lookup fails
+  t.slot.assign((size_t)1 << t.maxlen, 0);
+  int next[16] = {0};
+  for (int l = 1, code = 0; l < 16; ++l) {
+    code = (code + count[l - 1]) << 1;
+    next[l] = code;
+  }
+  for (int sym = 0; sym < n; ++sym) {
+    const int l = len[sym];
+    if (!l) continue;
+    const int code = next[l]++;
+    int rev = 0;
+    for (int b = 0; b < l; ++b) rev |= ((code >> b) & 1) << (l - 1 - b);
+    for (int k = rev; k < (1 << t.maxlen); k += 1 << l) t.slot[k] = (uint16_t)((sym << 4) | l);
+  }
+  return true;
+}
+
+int huff_decode(BitReader& br, const HuffTable& t) {
+  const uint16_t e = t.slot[br.peek(t.maxlen)];
+  if (!e) return -1;
+  br.drop(e & 15);
+  return e >> 4;
+}
+
+bool zlib_inflate(const uint8_t* in, size_t n, std::vector<uint8_t>& out, size_t limit, std::string& err) {
+  out.clear();
+  if (n < 6) return err = "deflate chunk shorter than a zlib stream", false;
+  const int cmf = in[0], flg = in[1];
+  if ((cmf & 15) != 8 || (cmf >> 4) > 7 || ((cmf << 8) | flg) % 31 != 0)
+    return err = "deflate chunk: bad zlib header", false;
+  if (flg & 0x20) return err = "deflate chunk: preset dictionaries are not supported", false;
+  // length and distance codes: base value and extra bits
+  int lbase[29], lext[29], dbase[30], dext[30];
+  for (int i = 0, b = 3; i < 28; ++i) {
+    lext[i] = i < 8 ? 0 : (i - 4) / 4;
+    lbase[i] = b;
+    b += 1 << lext[i];
+  }
+  lbase[28] = 258;
+  lext[28] = 0;
+  for (int i = 0, b = 1; i < 30; ++i) {
+    dext[i] = i < 2 ? 0 : (i - 2) / 2;
+    dbase[i] = b;
+    b += 1 << dext[i];
+  }
+  static const int kLenOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+  BitReader br(in + 2, n - 2);
+  out.reserve(std::min<size_t>(limit, (size_t)1 << 26));
+  HuffTable lit, dist;
+  bool last = false;
+  while (!last) {
+    last = br.bits(1) != 0;
+    const int type = (int)br.bits(2);
+    if (type == 0) {
+      br.align();
+      const uint32_t len = br.bits(16), nlen = br.bits(16);
+      if (len != (~nlen & 0xffffu)) return err = "deflate chunk: bad stored block length", false;
+      if (out.size() + len > limit) return err = "deflate chunk inflates past its chunk size", false;
+      for (uint32_t i = 0; i < len; ++i) out.push_back((uint8_t)br.bits(8));
+    } else if (type == 1 || type == 2) {
+      uint8_t lens[320] = {0};
+      int nlit = 288, ndist = 30;
+      if (type == 1) {
+        for (int i = 0; i < 288; ++i) lens[i] = i < 144 ? 8 : (i < 256 ? 9 : (i < 280 ? 7 : 8));
+        for (int i = 0; i < 30; ++i) lens[288 + i] = 5;
+      } else {
+        nlit = (int)br.bits(5) + 257;
+        ndist = (int)br.bits(5) + 1;
+        const int ncl = (int)br.bits(4) + 4;
+        if (nlit > 286 || ndist > 30) return err = "deflate chunk: bad code counts", false;
+        uint8_t cl[19] = {0};
+        for (int i = 0; i < ncl; ++i) cl[kLenOrder[i]] = (uint8_t)br.bits(3);
+        HuffTable clt;
+        if (!huff_build(cl, 19, clt)) return err = "deflate chunk: bad code-length code", false;
+        for (int i = 0; i < nlit + ndist;) {
+          const int sym = huff_decode(br, clt);
+          if (sym < 0) return err = "deflate chunk: bad code length", false;
+          if (sym < 16) {
+            lens[i++] = (uint8_t)sym;
+            continue;
+          }
+          int rep = 0;
+          uint8_t v = 0;
+          if (sym == 16) {
+            if (i == 0) return err = "deflate chunk: repeat with no previous length", false;
+            v = lens[i - 1];
+            rep = 3 + (int)br.bits(2);
+          } else if (sym == 17) {
+            rep = 3 + (int)br.bits(3);
+          } else {
+            rep = 11 + (int)br.bits(7);
+          }
+          if (i + rep > nlit + ndist) return err = "deflate chunk: code lengths overrun", false;
+          while (rep--) lens[i++] = v;
+        }
+        if (lens[256] == 0) return err = "deflate chunk: no end-of-block code", false;
+        // the distance lengths follow the literal/length lengths
+        std::memmove(lens + 288, lens + nlit, (size_t)ndist);
+        std::memset(lens + nlit, 0, (size_t)(288 - nlit));
+      }
+      if (!huff_build(lens, 288, lit) || !huff_build(lens + 288, 30, dist))
+        return err = "deflate chunk: bad Huffman code", false;
+      while (true) {
+        const int sym = huff_decode(br, lit);
+        if (sym < 0 || br.overrun()) return err = "deflate chunk: bad or truncated literal/length code", false;
+        if (sym < 256) {
+          if (out.size() >= limit) return err = "deflate chunk inflates past its chunk size", false;
+          out.push_back((uint8_t)sym);
+          continue;
+        }
+        if (sym == 256) break;
+        if (sym > 285) return err = "deflate chunk: bad length code", false;
+        const size_t len = (size_t)lbase[sym - 257] + br.bits(lext[sym - 257]);
+        const int ds = huff_decode(br, dist);
+        if (ds < 0 || ds > 29) return err = "deflate chunk: bad distance code", false;
+        const size_t d = (size_t)dbase[ds] + br.bits(dext[ds]);
+        if (d > out.size()) return err = "deflate chunk: distance before the start of the output", false;
+        if (out.size() + len > limit) return err = "deflate chunk inflates past its chunk size", false;
+        const size_t from = out.size() - d;
+        if (d >= len) {
+          out.resize(out.size() + len);
+          std::memcpy(&out[out.size() - len], &out[from], len);
+        } else {
+          for (size_t k = 0; k < len; ++k) out.push_back(out[from + k]);  // overlapping: a run
+        }
+      }
+    } else {
+      return err = "deflate chunk: reserved block type", false;
+    }
+    if (br.overrun()) return err = "deflate chunk: truncated stream", false;
+  }
+  br.align();
+  uint32_t want = 0;
+  for (int i = 0; i < 4; ++i) want = (want << 8) | br.bits(8);
+  if (br.overrun()) return err = "deflate chunk: missing Adler-32 trailer", false;
+  // Adler-32, reduced modulo 65521 once per 2^20 bytes: the 64-bit sums
+  // stay below 2^49 in between
+  uint64_t a = 1, b = 0;
+  for (size_t i0 = 0; i0 < out.size(); i0 += (size_t)1 << 20) {
+    const size_t i1 = std::min(out.size(), i0 + ((size_t)1 << 20));
+    for (size_t i = i0; i < i1; ++i) {
+      a += out[i];
+      b += a;
+    }
+    a %= 65521u;
+    b %= 65521u;
+  }
+  if ((uint32_t)((b << 16) | a) != want) return err = "deflate chunk: Adler-32 mismatch", false;
+  return true;
+}
+
+// ------------------------------------------------------- chunked datasets --
+
+struct Filter {
+  int id = 0, flags = 0;
+  std::vector<uint32_t> cd;  // client data
+};
+
+// filter pipeline message (versions 1 and 2)
+bool parse_filters(File& F, const Message& m, std::vector<Filter>& fl) {
+  const int v = F.u8(m.at), nf = F.u8(m.at + 1);
+  if (v != 1 && v != 2) return F.fail("unsupported filter pipeline message version");
+  uint64_t p = m.at + (v == 1 ? 8 : 2);
+  const uint64_t end = m.at + m.size;
+  for (int i = 0; i < nf; ++i) {
+    Filter f;
+    f.id = (int)F.uint(p, 2);
+    p += 2;
+    uint64_t nlen = 0;
+    if (v == 1 || f.id >= 256) {
+      nlen = F.uint(p, 2);
+      p += 2;
+    }
+    f.flags = (int)F.uint(p, 2);
+    const uint64_t ncd = F.uint(p + 2, 2);
+    p += 4;
+    p += v == 1 ? (nlen + 7) / 8 * 8 : nlen;  // name
+    if (ncd > 64 || p + 4 * ncd > end) return F.fail("bad filter pipeline message");
+    for (uint64_t c = 0; c < ncd; ++c) f.cd.push_back((uint32_t)F.uint(p + 4 * c, 4));
+    p += 4 * ncd;
+    if (v == 1 && (ncd & 1)) p += 4;
+    if (F.oob || p > end) return F.fail("bad filter pipeline message");
+    fl.push_back(f);
+  }
+  return true;
+}
+
+struct Chunk {
+  uint64_t size = 0, at = 0;
+  uint32_t mask = 0;
+  uint64_t off[2] = {0, 0};
+};
+
+// the chunks of a version-1 B-tree of raw data chunks (node type 1); keys
+// hold the chunk's stored size, filter mask and element offsets.  At most
+// 2^16 nodes are visited, so a node that lists itself cannot blow up.
+bool chunk_btree(File& F, uint64_t at, int ndims, std::vector<Chunk>& out, int depth, int& nodes) {
+  if (depth > 32) return F.fail("chunk B-tree too deep");
+  if (++nodes > (1 << 16)) return F.fail("chunk B-tree has too many nodes");
+  at += F.base;
+  if (!F.in(at, 8 + 2 * (uint64_t)F.so) || std::memcmp(&F.d[at], "TREE", 4) != 0 || F.d[at + 4] != 1)
+    return F.fail("bad chunk B-tree node");
+  const int level = F.d[at + 5];
+  const int used = (int)F.uint(at + 6, 2);
+  const uint64_t ksz = 8 + 8 * (uint64_t)ndims;
+  uint64_t p = at + 8 + 2 * F.so;
+  if (!F.in(p, (uint64_t)used * (ksz + F.so) + ksz)) return F.fail("chunk B-tree node outside the file");
+  for (int c = 0; c < used; ++c) {
+    Chunk ch;
+    ch.size = F.uint(p, 4);
+    ch.mask = (uint32_t)F.uint(p + 4, 4);
+    for (int d = 0; d < ndims - 1 && d < 2; ++d) ch.off[d] = F.uint(p + 8 + 8 * d, 8);
+    ch.at = F.addr(p + ksz);
+    p += ksz + F.so;
+    if (F.oob || ch.at == kUndef) return F.fail("bad chunk B-tree entry");
+    if (level > 0) {
+      if (!chunk_btree(F, ch.at, ndims, out, depth + 1, nodes)) return false;
+    } else {
+      if (out.size() >= (1u << 24)) return F.fail("too many chunks");
+      out.push_back(ch);
+    }
+  }
+  return true;
+}
+
+// Reads a chunked dataset of rank 1 or 2 (layout message version 3, class
+// 2): each chunk is un-filtered (deflate, byte shuffle, in the reverse of
+// the pipeline's order, skipping the filters its mask excludes) and copied
+// into the rows x cols array; chunks never written read as 0.  This is the
+// layout of the HDF5 monitor's "compressed" option
+// (src/jams/monitors/hdf5.cc:292-323: chunks of min(4095, rows) x 1
+// values, shuffle, deflate level 6).
+bool read_chunked(File& F, uint64_t btree, const std::vector<uint64_t>& cdims, const std::vector<Filter>& filters,
+                  int tsize, uint64_t d0, uint64_t d1, int rank, std::vector<double>& out) {
+  const int ndims = rank + 1;
+  if ((int)cdims.size() != ndims || cdims[rank] != (uint64_t)tsize) return F.fail("chunk dimensions do not match the dataset");
+  uint64_t c0 = cdims[0], c1 = rank == 2 ? cdims[1] : 1;
+  if (c0 == 0 || c1 == 0 || c0 > (1ull << 31) || c1 > (1ull << 31) || c0 * c1 > (1ull << 28))
+    return F.fail("chunk dimensions out of range");
+  for (const Filter& f : filters)
+    if (f.id != 1 && f.id != 2 && !(f.flags & 1))
+      return F.fail("filter " + std::to_string(f.id) + " is not supported (deflate and shuffle are)");
+  std::vector<Chunk> chunks;
+  int nodes = 0;
+  if (btree != kUndef && !chunk_btree(F, btree, ndims, chunks, 0, nodes)) return false;
+  // the array is allocated only as large as its chunks can fill (plus up
+  // to 2^24 values of unwritten fill), so corrupt extents cannot ask for
+  // more memory than the file describes
+  if (d0 * d1 > (1ull << 24) + (uint64_t)chunks.size() * c0 * c1)
+    return F.fail("extents larger than the chunks written");
+  out.assign(d0 * d1, 0.0);
+  const size_t cbytes = (size_t)(c0 * c1) * tsize;
+  std::vector<uint8_t> a, b;
+  std::string ferr;
+  for (const Chunk& ch : chunks) {
+    const uint64_t o0 = ch.off[0], o1 = rank == 2 ? ch.off[1] : 0;
+    if (o0 >= d0 || o1 >= d1 || o0 % c0 || o1 % c1) return F.fail("chunk offset outside the dataset");
+    const uint64_t at = ch.at + F.base;
+    if (!F.in(at, ch.size)) return F.fail("chunk data outside the file");
+    // zlib expands by at most 1032:1; an unfiltered chunk is stored whole
+    bool inflates = false;
+    for (size_t i = 0; i < filters.size(); ++i)
+      if (filters[i].id == 1 && !(i < 32 && (ch.mask >> i) & 1)) inflates = true;
+    if (inflates ? cbytes > 1032 * ch.size + 64 : ch.size < cbytes)
+      return F.fail("chunk stored size does not match its extents");
+    a.assign(F.d.begin() + at, F.d.begin() + at + ch.size);
+    for (int i = (int)filters.size() - 1; i >= 0; --i) {
+      if (i < 32 && (ch.mask >> i) & 1) continue;  // skipped when written
+      const Filter& f = filters[i];
+      if (f.id == 1) {
+        if (!zlib_inflate(a.data(), a.size(), b, cbytes, ferr)) return F.fail(ferr);
+        a.swap(b);
+      } else if (f.id == 2) {
+        const size_t es = f.cd.empty() ? (size_t)tsize : f.cd[0];
+        if (es > 1 && a.size() >= es) {
+          const size_t ne = a.size() / es;
+          b.resize(a.size());
+          for (size_t j = 0; j < es; ++j)
+            for (size_t e = 0; e < ne; ++e) b[e * es + j] = a[j * ne + e];
+          std::copy(a.begin() + ne * es, a.end(), b.begin() + ne * es);
+          a.swap(b);
+        }
+      } else {
+        return F.fail("optional filter " + std::to_string(f.id) + " was applied to a chunk: not supported");
+      }
+    }
+    if (a.size() != cbytes) return F.fail("chunk decodes to " + std::to_string(a.size()) + " bytes, not " + std::to_string(cbytes));
+    for (uint64_t i = 0; i < c0 && o0 + i < d0; ++i)
+      for (uint64_t j = 0; j < c1 && o1 + j < d1; ++j) {
+        const uint8_t* q = &a[(size_t)(i * c1 + j) * tsize];
+        double v;
+        if (tsize == 8) {
+          uint64_t u = 0;
+          for (int k = 0; k < 8; ++k) u |= (uint64_t)q[k] << (8 * k);
+          std::memcpy(&v, &u, 8);
+        } else {
+          uint32_t u = 0;
+          for (int k = 0; k < 4; ++k) u |= (uint32_t)q[k] << (8 * k);
+          float f;
+          std::memcpy(&f, &u, 4);
+          v = f;
+        }
+        out[(o0 + i) * d1 + (o1 + j)] = v;
+      }
+  }
+  return true;
+}
+
 int read_h5(const std::string& path, const std::string& dataset, std::vector<double>& out, int64_t& rows,
             int64_t& cols, std::string& err) {
   File F;
@@ -589,6 +962,8 @@ int read_h5(const std::string& path, const std::string& dataset, std::vector<dou
   bool tfloat = false, tle = true;
   int layout = -1;
   uint64_t data_at = kUndef, data_size = 0;
+  std::vector<uint64_t> cdims;  // chunked: chunk extents, the element size last
+  std::vector<Filter> filters;
   for (const Message& m : msgs) {
     const uint64_t p = m.at;
     if (m.type == 0x01) {  // dataspace
@@ -609,6 +984,13 @@ int read_h5(const std::string& path, const std::string& dataset, std::vector<dou
         } else if (layout == 0) {
           data_size = F.uint(p + 2, 2);
           data_at = p + 4 - F.base;
+        } else if (layout == 2 && v == 3) {  // dimensionality, B-tree address, extents
+          const int nd = F.u8(p + 2);
+          data_at = F.addr(p + 3);
+          for (int r = 0; r < nd && r < 4; ++r) cdims.push_back(F.uint(p + 3 + F.so + 4 * (uint64_t)r, 4));
+        } else if (layout == 2) {
+          err = "dataset /" + dataset + " uses a version-4 chunk index: only version-3 (B-tree) chunked layouts are supported";
+          return 1;
         }
       } else if (v == 1 || v == 2) {
         const int rank = F.u8(p + 1);
@@ -621,16 +1003,22 @@ int read_h5(const std::string& path, const std::string& dataset, std::vector<dou
         }
       }
     } else if (m.type == 0x0B) {
-      err = "dataset /" + dataset + " uses a filter pipeline (compression): not supported";
-      return 1;
+      if (!parse_filters(F, m, filters)) {
+        err = "dataset /" + dataset + ": " + F.err;
+        return 1;
+      }
     }
   }
   if (F.oob) {
     err = "dataset /" + dataset + ": a header field lies outside the file";
     return 1;
   }
-  if (layout != 0 && layout != 1) {
-    err = "dataset /" + dataset + " is chunked or virtual: only contiguous and compact datasets are supported";
+  if (layout != 0 && layout != 1 && layout != 2) {
+    err = "dataset /" + dataset + " is virtual: only contiguous, compact and chunked datasets are supported";
+    return 1;
+  }
+  if (layout != 2 && !filters.empty()) {
+    err = "dataset /" + dataset + " has a filter pipeline but is not chunked";
     return 1;
   }
   if (!tfloat || !tle || (tsize != 8 && tsize != 4)) {
@@ -652,6 +1040,14 @@ int read_h5(const std::string& path, const std::string& dataset, std::vector<dou
   rows = (int64_t)d0;
   cols = (int64_t)d1;
   const uint64_t n = d0 * d1;
+  if (layout == 2) {
+    if (!read_chunked(F, data_at, cdims, filters, tsize, d0, d1, (int)dims.size(), out)) {
+      err = "dataset /" + dataset + ": " + F.err;
+      out.clear();
+      return 1;
+    }
+    return 0;
+  }
   if (data_at == kUndef) {  // never written: fill value 0
     if (n > (1ull << 24)) {
       err = "dataset /" + dataset + " was never written and is too large to read as zeros";

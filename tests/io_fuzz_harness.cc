@@ -5,7 +5,10 @@
 // corruptions of them (bit flips, zeroed and saturated spans, truncations,
 // repeated spans) and counts the status codes.
 //
-//   io_fuzz_harness <dir> <cases> <seed>
+//   io_fuzz_harness <dir> <cases> <seed> [more base files ...]
+//
+// The optional files (chunked, filtered HDF5 files that the library does
+// not write) join the bases; their dataset must be named "spins".
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -29,7 +32,7 @@ static std::vector<uint8_t> slurp(const std::string& p) {
 }
 
 int main(int argc, char** argv) {
-  if (argc != 4) return 2;
+  if (argc < 4) return 2;
   const std::string dir = argv[1];
   const long cases = std::atol(argv[2]);
   std::mt19937_64 rng(std::strtoull(argv[3], nullptr, 10));
@@ -57,6 +60,10 @@ int main(int argc, char** argv) {
       return 3;
     }
     bases.push_back({p, slurp(p)});
+  }
+  for (int a = 4; a < argc; ++a) {
+    bases.push_back({argv[a], slurp(argv[a])});
+    if (bases.back().bytes.empty()) return 3;
   }
   std::map<int, long> codes;
   for (long it = 0; it < cases; ++it) {

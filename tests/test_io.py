@@ -117,3 +117,88 @@ def test_text_comments_and_counting_follow_the_reference(llg, tmp_path):
     np.testing.assert_array_equal(llg.read_array_file(str(path)), [1, 2, 3, 4.5, 5.5, 6.5])
     path.write_text("1 2 3 \n")
     np.testing.assert_array_equal(llg.read_array_file(str(path)), [1, 2, 3, 0])
+
+
+def test_h5_chunked_compressed_as_the_monitor_writes(llg, tmp_path):
+    """The HDF5 monitor's "compressed" option (hdf5.cc:292-323): chunks of
+    min(4095, rows) x 1 values, shuffle, deflate level 6; a vector field
+    and a scalar field in one file, edge chunks padded."""
+    from tests import h5_chunked as H
+    rng = np.random.default_rng(11)
+    s = rng.normal(size=(10000, 3))
+    e = rng.normal(size=5000)
+    path = str(tmp_path / "compressed.h5")
+    H.write(path, {"spins": H.Dataset(s, chunks=(4095, 1)), "energy": H.Dataset(e, chunks=(4095,))})
+    np.testing.assert_array_equal(llg.read_array_file(path, "/spins"), s)
+    np.testing.assert_array_equal(llg.read_array_file(path, "/energy"), e)
+    small = rng.normal(size=(7, 3))   # fewer rows than 4095: one chunk of 7 x 1 per column
+    H.write(path, {"spins": H.Dataset(small, chunks=(7, 1))})
+    np.testing.assert_array_equal(llg.read_array_file(path, "/spins"), small)
+
+
+@pytest.mark.parametrize("filters", [
+    ((2,), (1, 0)),                      # stored deflate blocks
+    ((2,), (1, 6, 4)),                   # fixed Huffman codes (Z_FIXED)
+    ((1, 9),),                           # dynamic codes, no shuffle
+    ((2,), (1, 6, 2)),                   # Huffman only, no matches
+    ((2,), (1, 6, 3)),                   # run-length matches
+    ((2,),),                             # shuffle alone
+    (),                                  # chunked, no filters
+])
+def test_h5_chunked_filter_and_block_kinds(llg, tmp_path, filters):
+    from tests import h5_chunked as H
+    rng = np.random.default_rng(12)
+    s = np.round(rng.normal(size=(3000, 3)), 2)   # repetitive bytes: long matches
+    path = str(tmp_path / "f.h5")
+    H.write(path, {"spins": H.Dataset(s, chunks=(1000, 3), filters=filters)})
+    np.testing.assert_array_equal(llg.read_array_file(path, "/spins"), s)
+    f32 = rng.normal(size=(900, 3)).astype(np.float32)
+    H.write(path, {"spins": H.Dataset(f32, chunks=(256, 1), filters=filters)})
+    np.testing.assert_array_equal(llg.read_array_file(path, "/spins"), f32.astype(np.float64))
+
+
+def test_h5_chunked_deep_btree_unwritten_and_unfiltered_chunks(llg, tmp_path):
+    """A chunk B-tree of several levels (two entries per node); chunks never
+    written read as the fill value 0; a chunk whose filter mask skips
+    deflate is only shuffled."""
+    from tests import h5_chunked as H
+    rng = np.random.default_rng(13)
+    s = rng.normal(size=(600, 3))
+    path = str(tmp_path / "deep.h5")
+    ds = H.Dataset(s, chunks=(50, 1), fanout=2, unwritten={4, 17}, skip_deflate={0, 9, 35})
+    H.write(path, {"spins": ds})
+    want = s.copy()
+    for i, off in enumerate(H.chunk_list(ds)):
+        if i in ds.unwritten:
+            want[off[0]:off[0] + 50, off[1]] = 0.0
+    np.testing.assert_array_equal(llg.read_array_file(path, "/spins"), want)
+
+
+def test_h5_chunked_errors(llg, tmp_path):
+    from tests import h5_chunked as H
+    rng = np.random.default_rng(14)
+    s = rng.normal(size=(2000, 3))
+    path = str(tmp_path / "e.h5")
+    # an optional filter the writer never applied is passed over; a
+    # mandatory one is refused
+    H.write(path, {"spins": H.Dataset(s, chunks=(1000, 1), extra_filter=(32000, 1))})
+    np.testing.assert_array_equal(llg.read_array_file(path, "/spins"), s)
+    H.write(path, {"spins": H.Dataset(s, chunks=(1000, 1), extra_filter=(32000, 0))})
+    with pytest.raises(llg.LLGError, match="filter 32000 is not supported"):
+        llg.read_array_file(path, "/spins")
+    H.write(path, {"spins": H.Dataset(s, chunks=(1000, 1))}, layout_version=4)
+    with pytest.raises(llg.LLGError, match="version-4 chunk index"):
+        llg.read_array_file(path, "/spins")
+    # a damaged deflate stream: a flipped bit inside the first chunk
+    ds = H.Dataset(s, chunks=(1000, 1))
+    H.write(path, {"spins": ds})
+    raw, _ = H.encode_chunk(ds, (0, 0), 0)
+    b = bytearray(open(path, "rb").read())
+    at = bytes(b).index(raw)
+    for k in (len(raw) // 2, 3, len(raw) - 2):
+        bad = bytearray(b)
+        bad[at + k] ^= 0x10
+        p = str(tmp_path / "bad.h5")
+        open(p, "wb").write(bytes(bad))
+        with pytest.raises(llg.LLGError, match="dataset /spins: (deflate chunk|chunk decodes)"):
+            llg.read_array_file(p, "/spins")

@@ -30,6 +30,13 @@ CHILD = textwrap.dedent(r'''
         p = os.path.join(tmp, name)
         llg.write_array_file(p, a)
         bases.append((p, open(p, "rb").read()))
+    from tests import h5_chunked as H
+    s = np.random.default_rng(3).normal(size=(120, 3))
+    for name, ds in (("monitor.h5", H.Dataset(s, chunks=(50, 1))),
+                     ("deep.h5", H.Dataset(s, chunks=(20, 1), fanout=2, unwritten={3}, skip_deflate={5}))):
+        p = os.path.join(tmp, name)
+        H.write(p, {"spins": ds})
+        bases.append((p, open(p, "rb").read()))
 
     def corrupt(b):
         b = bytearray(b)
