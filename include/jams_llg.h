@@ -305,9 +305,11 @@ int llg_kernel_info(const llg_handle *h, int32_t *info);
    choice gives the same results bit for bit. */
 int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t flags);
 
-/* Times every tiling candidate (planes per CTA 2..64, stored or recomputed
-   rhs) for trial_steps steps on a copy of the state and keeps the fastest;
-   the state and iteration are restored.  With use_cache the choice is read
+/* Times every tiling candidate (planes per CTA 2..64; stored or recomputed
+   rhs; occupancy; narrow tile; two rows per thread; the fused Heun step;
+   TMA plane loads; stored noise above 0 K: the llg_set_tuning choices that
+   apply to the handle) for trial_steps steps on a copy of the state and
+   keeps the fastest; the state and iteration are restored.  With use_cache the choice is read
    from / appended to the file named by $JAMS_LLG_TUNE_CACHE (default
    ~/.cache/jams_llg_tuning.txt), keyed by device, lattice and terms. */
 int llg_autotune(llg_handle *h, int32_t trial_steps, int32_t use_cache);
