@@ -1067,6 +1067,20 @@ Params launch_params(llg_handle* h, const void* input, int slot) {
 }
 
 // uploads replica records (temperature- and field-dependent parts)
+// zeros in the stored-noise planes of every replica at 0 K
+cudaError_t clear_cold_noise(llg_handle* h) {
+  if (!h->noise.p) return cudaSuccess;
+  for (size_t r = 0; r < h->reps.size(); ++r) {
+    if (h->rep_T[r] > 0.0) continue;
+    for (int m = 0; m < 3; ++m) {
+      const cudaError_t ce = cudaMemsetAsync(h->noise.p + (size_t)m * h->npad + h->reps[r].offset, 0,
+                                             (size_t)h->reps[r].n * sizeof(float), h->stream);
+      if (ce != cudaSuccess) return ce;
+    }
+  }
+  return cudaSuccess;
+}
+
 int sync_replicas(llg_handle* h) {
   if (!h->params_dirty) return 0;
   for (size_t r = 0; r < h->reps.size(); ++r) {
@@ -1079,6 +1093,11 @@ int sync_replicas(llg_handle* h) {
   cudaError_t ce = cudaMemcpyAsync(h->d_rep.p, h->reps.data(), h->reps.size() * sizeof(ReplicaDev),
                                    cudaMemcpyHostToDevice, h->stream);
   if (ce != cudaSuccess) return h->cuda_fail(ce, "uploading replica records");
+  // stored noise: the predictor writes the thermal field of replicas above
+  // 0 K only, and the corrector reads every replica's, so a replica at 0 K
+  // reads zeros
+  ce = clear_cold_noise(h);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "clearing the noise planes");
   // pageable source: make sure the copy has consumed it before the vector changes
   ce = cudaStreamSynchronize(h->stream);
   if (ce != cudaSuccess) return h->cuda_fail(ce, "uploading replica records");
@@ -1877,6 +1896,8 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
     if (!h->noise.p) {
       ce = h->noise.alloc((size_t)3 * h->npad);
       if (ce != cudaSuccess) return h->cuda_fail(ce, "alloc noise planes");
+      ce = clear_cold_noise(h);
+      if (ce != cudaSuccess) return h->cuda_fail(ce, "clearing the noise planes");
     }
     h->store_noise = true;
   }

@@ -967,6 +967,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
     // guarded, so that the two rows' work interleaves
     if (RPT > 1 || active[0]) {
       int ir[RPT];
+      bool ldr[RPT];
       float w[RPT][3];
       // the spin's own start-of-step state, stored rhs / k sum and dipole
       // field (input state; s0 for the recomputed rhs): loaded before the
@@ -977,9 +978,12 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
         const int i = x * V.st[0] + yz[r];   // spin index in the replica
         const bool ld = (RPT == 1 || active[r]) && LLG_IN_RANGE(P, i, 0, (int64_t)V.L[0] * V.st[0]);
         ir[r] = i;
+        ldr[r] = ld;
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
-          w[r][m] = wn[r][m];
+          // the stored-noise predictor keeps no noise across planes: plane
+          // x + 1's comes back from its store (below)
+          w[r][m] = WSTORE ? 0.f : wn[r][m];
           own_s0[r][m] = own_r[r][m] = dip[r][m] = dip0[r][m] = 0.f;
         }
         if (STAGE >= 3 && ld) {
@@ -992,9 +996,15 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
           own_r[r][1] = ay[i];
           own_r[r][2] = az[i];
         }
-        if (WLOAD && ld) {
+        if (WLOAD && ld) {   // zeros for a replica at 0 K (the host clears its planes)
 #pragma unroll
           for (int m = 0; m < 3; ++m) w[r][m] = __ldg(P.noise32 + m * P.npad + V.offset + i);
+        }
+        if (WSTORE && ld && thermal && (x & 1)) {
+          // written by this thread one plane earlier (a plain load: the
+          // planes change within the launch)
+#pragma unroll
+          for (int m = 0; m < 3; ++m) w[r][m] = P.noise32[m * P.npad + V.offset + i];
         }
         if (has_dip && ld) {
 #pragma unroll
@@ -1009,6 +1019,23 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
 #pragma unroll
         for (int r = 0; r < RPT; ++r)
           noise_pair(P.philox_keys, (uint32_t)tile.x, step, (uint32_t)ir[r], amp, w[r], wn[r]);
+        if constexpr (WSTORE) {
+          // the thermal field of planes x and x + 1 for the corrector (and
+          // plane x + 1's for this thread's next plane)
+#pragma unroll
+          for (int r = 0; r < RPT; ++r) {
+            const int i = ir[r];
+            float* nz = P.noise32 + V.offset;
+            if (ldr[r]) {
+#pragma unroll
+              for (int m = 0; m < 3; ++m) nz[m * P.npad + i] = w[r][m];
+            }
+            if (ldr[r] && x + 1 < xe && LLG_IN_RANGE(P, i + V.st[0], 0, (int64_t)V.L[0] * V.st[0])) {
+#pragma unroll
+              for (int m = 0; m < 3; ++m) nz[m * P.npad + i + V.st[0]] = wn[r][m];
+            }
+          }
+        }
       }
 #pragma unroll
       for (int r = 0; r < RPT; ++r) {
@@ -1030,10 +1057,6 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
               ax[i] = ff(hdt, k[0], s[0]);
               ay[i] = ff(hdt, k[1], s[1]);
               az[i] = ff(hdt, k[2], s[2]);
-            }
-            if (WSTORE) {
-#pragma unroll
-              for (int m = 0; m < 3; ++m) P.noise32[m * P.npad + V.offset + i] = w[r][m];
             }
           }
         } else if (STAGE == 1 || STAGE == 2) {

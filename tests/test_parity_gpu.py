@@ -454,6 +454,32 @@ def test_fused_step_is_refused_where_unsupported(llg):
         sc.set_tuning(4, True, 2, False, False, True)
 
 
+@pytest.mark.parametrize("pair", [False, True])
+def test_stored_noise_with_replicas_at_zero_kelvin(llg, pair):
+    """Stored noise on a handle whose replicas sit above and at 0 K: the
+    predictor writes the thermal field of the warm replicas only, and the
+    host keeps the cold replicas' planes at zero, also after a replica is
+    cooled to 0 K between steps.  Both forms give the same states."""
+    w = W.bcc_three_shell(L=8, T=300.0, start="random")
+    w.replicas = [W.Replica(L=(8, 8, 8), temperature=300.0), W.Replica(L=(8, 8, 8), temperature=0.0),
+                  W.Replica(L=(6, 8, 10), temperature=150.0)]
+    outs = []
+    for noise in (False, True):
+        s = solver(llg, w, llg.FP32C, steps_per_graph=4)
+        s.set_tuning(4, True, 2, pair=pair, noise=noise)
+        assert s.kernel_info()["stored_noise"] == noise
+        for r in range(len(w.replicas)):
+            s.set_state(W.initial_state(w, r), r)
+        s.step(6)
+        s.set_temperature(0, 0.0)
+        s.step(5)
+        s.set_temperature(1, 80.0)
+        s.step(3)
+        outs.append([s.get_state(r) for r in range(len(w.replicas))])
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
 def test_stored_noise_needs_stored_rhs_mode(llg):
     s = solver(llg, W.bcc_nearest_neighbour(L=8, T=300.0), llg.FP32C)
     with pytest.raises(llg.LLGError, match="stored noise"):
