@@ -173,7 +173,8 @@ def parse(argv=None):
     p.add_argument("--profile-steps", type=int, default=50)
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--tuning", default="", help="planes_per_cta,flags,occupancy instead of autotuning (flags: 1 stored rhs, 2 narrow tile, "
-                        "4 two rows per thread, 8 the fused Heun step, 256 TMA plane loads, 512 stored noise)")
+                        "4 two rows per thread, 8 the fused Heun step, 256 TMA plane loads, 512 stored noise, "
+                        "1024 the half-width simple-cubic tile)")
     return p.parse_args(argv)
 
 
@@ -540,7 +541,7 @@ def make_solver(llg, w, prec, local, stream, tuning_arg: str = "", tune: bool = 
     if tuning_arg:
         tx, fl, oc = (int(v) for v in tuning_arg.split(","))
         sol.set_tuning(tx, bool(fl & 1), oc, bool(fl & 2), bool(fl & 4), bool(fl & 8), bool(fl & 256),
-                       bool(fl & 512))
+                       bool(fl & 512), bool(fl & 1024))
         tuning = sol.kernel_info()
     else:
         # the choice is cached per lattice shape ($JAMS_LLG_TUNE_CACHE), so a

@@ -301,13 +301,17 @@ int llg_kernel_info(const llg_handle *h, int32_t *info);
    variant, 2 (<= 128 registers), 3 (<= 80) or 4 (<= 64); for the fused
    step 2 or 4 x 256 resident threads per SM; bit 8: TMA plane loads; bit
    9: stored noise (with bit 0: the predictor also stores the step's thermal
-   field, which the corrector reads instead of drawing it again).  Every
-   choice gives the same results bit for bit. */
+   field, which the corrector reads instead of drawing it again); bit 10:
+   the half-width tile of simple-cubic lattices, 16 cells along z (fewer
+   idle lanes where z extents are not multiples of 32; wide rows, no dipole
+   term, not with TMA or the fused step).  Every choice gives the same
+   results bit for bit. */
 int llg_set_tuning(llg_handle *h, int32_t planes_per_cta, int32_t flags);
 
 /* Times every tiling candidate (planes per CTA 2..64; stored or recomputed
    rhs; occupancy; narrow tile; two rows per thread; the fused Heun step;
-   TMA plane loads; stored noise above 0 K: the llg_set_tuning choices that
+   TMA plane loads; stored noise above 0 K; the half-width simple-cubic
+   tile: the llg_set_tuning choices that
    apply to the handle) for trial_steps steps on a copy of the state and
    keeps the fastest; the state and iteration are restored.  With use_cache the choice is read
    from / appended to the file named by $JAMS_LLG_TUNE_CACHE (default

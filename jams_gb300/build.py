@@ -23,7 +23,7 @@ LIB = os.path.join(OUT, "libjams_llg.so")
 OUT_CHECKED = os.path.join(HERE, "_build_checked")
 LIB_CHECKED = os.path.join(OUT_CHECKED, "libjams_llg.so")
 SOURCES = ["llg_kernels.cu", "llg_tiled.cu", "llg_tiled_dipole.cu", "llg_tiled_pair.cu", "llg_tiled_tma.cu",
-           "llg_tiled_tma_pair.cu", "llg_fused_a.cu",
+           "llg_tiled_tma_pair.cu", "llg_tiled_z16.cu", "llg_fused_a.cu",
            "llg_fused_b.cu", "llg_observe.cu", "llg_host.cu", "llg_noalloc.cu", "llg_config.cu", "llg_io.cu",
            "llg_dipole.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1236,11 +1236,11 @@ bool launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
       Params PN = P;
       if (h->store_noise) PN.noise32 = h->noise.p;
       if (stage == 0)
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, h->store_noise ? 7 : 0, g4, st, PN, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, advance, h->dipole != nullptr, m0);
+        launch_tiled(h->family, h->tz, h->ty, h->rpt, h->occupancy, h->store_noise ? 7 : 0, g4, st, PN, h->TP, s0, nullptr, sp, h->store_mode ? aux : nullptr, ks, advance, h->dipole != nullptr, m0);
       else if (h->store_mode)
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, h->store_noise ? 8 : 2, g4, st, PN, h->TP, s0, sp, s0, aux, ks, advance, h->dipole != nullptr, m1);
+        launch_tiled(h->family, h->tz, h->ty, h->rpt, h->occupancy, h->store_noise ? 8 : 2, g4, st, PN, h->TP, s0, sp, s0, aux, ks, advance, h->dipole != nullptr, m1);
       else
-        launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, advance, h->dipole != nullptr, m1);
+        launch_tiled(h->family, h->tz, h->ty, h->rpt, h->occupancy, 1, g4, st, P, h->TP, s0, sp, buf<float>(h, 2 - cur), nullptr, ks, advance, h->dipole != nullptr, m1);
     } else {
       float* s0 = buf<float>(h, 0);
       float* a = buf<float>(h, 1);
@@ -1248,7 +1248,7 @@ bool launch_stage(llg_handle* h, int stage, uint32_t ks, int cur, cudaEvent_t af
       float* in = stage == 0 ? s0 : (stage == 2 ? b : a);
       float* out = stage == 0 ? a : (stage == 1 ? b : (stage == 2 ? a : s0));
       const CUtensorMap* m = h->tma ? &h->tmaps[stage == 0 ? 0 : (stage == 2 ? 2 : 1)] : nullptr;
-      launch_tiled(h->family, h->ty, h->rpt, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, advance, h->dipole != nullptr, m);
+      launch_tiled(h->family, h->tz, h->ty, h->rpt, h->occupancy, 3 + stage, g4, st, P, h->TP, s0, in, out, aux, ks, advance, h->dipole != nullptr, m);
     }
     return true;
   }
@@ -1470,7 +1470,8 @@ static int step_blocks(llg_handle* h, int32_t nsteps) {
   while (remaining > 0) {
     const int n = remaining >= K && K > 1 ? K : remaining;
     GraphKey key{h->cur + 4 * (h->store_mode ? 1 : 0) + 8 * h->occupancy + 64 * h->TP.TX + 8192 * h->ty +
-                     131072 * h->rpt + 524288 * (h->fused ? 1 : 0) + 1048576 * (h->tma ? 1 : 0) + 2097152 * (h->store_noise ? 1 : 0),
+                     131072 * h->rpt + 524288 * (h->fused ? 1 : 0) + 1048576 * (h->tma ? 1 : 0) + 2097152 * (h->store_noise ? 1 : 0) +
+                     4194304 * (h->tz == 16 ? 1 : 0),
                  n};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end() && (n == K || h->graphs.size() < kMaxGraphs)) {
@@ -1872,8 +1873,15 @@ int llg_set_tuning(llg_handle* h, int32_t planes_per_cta, int32_t store_rhs) {
   tiled_geometry(h->family, &wide_tz, &wide_ty);
   const int ty = fused ? fused_rows(h->family, h->fused_wide)
                        : ((store_rhs & 2) ? narrow_tile_rows(h->family) : wide_ty);
-  const bool retile = ty != h->ty;
+  // bit 10: the half-width simple-cubic tile (16 cells along z, wide rows)
+  const bool half = (store_rhs & 1024) != 0;
+  if (half && (h->family != kFamSC || fused || tma || h->dipole || (store_rhs & 2)))
+    return h->fail(LLG_ERR_BAD_DESC, "half-width tile: simple-cubic lattices without a dipole term, the wide rows, "
+                                     "not with the fused step or TMA");
+  const int tz = half ? 16 : wide_tz;
+  const bool retile = ty != h->ty || tz != h->tz;
   h->ty = ty;
+  h->tz = tz;
   if (planes_per_cta != h->TP.TX || retile) {
     h->TP.TX = planes_per_cta;
     int rc = build_tiles4(h);
@@ -2015,6 +2023,13 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
     for (size_t c = 0; c < n0; ++c)
       if (cands[c].second & 1) cands.push_back({cands[c].first, cands[c].second | 512});
   }
+  // the half-width simple-cubic tile: the wide-row candidates again, without
+  // TMA
+  if (h->family == kFamSC && !h->dipole) {
+    const size_t n0 = cands.size();
+    for (size_t c = 0; c < n0; ++c)
+      if (!(cands[c].second & (2 | 256))) cands.push_back({cands[c].first, cands[c].second | 1024});
+  }
   // the fused Heun step: wide or narrow tile, occupancy 2 or 4 (x 256 threads)
   if (h->integrator == LLG_HEUN && fused_supported(h->family) && !h->dipole)
     for (int t : {2, 4, 8, 16, 32, 64})
@@ -2033,7 +2048,8 @@ int llg_autotune(llg_handle* h, int32_t trial_steps, int32_t use_cache) {
   std::pair<int, int> choice = {h->TP.TX, h->fused ? (8 | (h->fused_wide ? 0 : 2) | (h->occupancy << 4))
                                                    : ((h->store_mode ? 1 : 0) | (h->ty != wide_ty0 ? 2 : 0) |
                                                       (h->rpt == 2 ? 4 : 0) | (h->occupancy << 4) |
-                                                      (h->tma ? 256 : 0) | (h->store_noise ? 512 : 0))};
+                                                      (h->tma ? 256 : 0) | (h->store_noise ? 512 : 0) |
+                                                      (h->tz == 16 ? 1024 : 0))};
   // each trial runs as llg_step runs steps: one CUDA graph of trial_steps
   // steps (captured and run once untimed, then timed)
   const int spg0 = h->steps_per_graph;

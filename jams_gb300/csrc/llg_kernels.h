@@ -57,9 +57,11 @@ int narrow_tile_rows(int family);
 bool pair_rows_supported(int family);
 // map: the tensor map of the gathered buffer for TMA plane loads (null:
 // planes staged through registers); tma_box gives its box geometry
-cudaError_t launch_tiled(int family, int ty, int rpt, int occupancy, int stage, unsigned grid, cudaStream_t st,
-                         const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
-                         float* aux, uint32_t k, uint32_t advance, bool dipole, const CUtensorMap* map);
+// tz: cells along z of the tile, 32 or (simple cubic, wide rows, no dipole
+// term, no TMA) the half-width 16
+cudaError_t launch_tiled(int family, int tz, int ty, int rpt, int occupancy, int stage, unsigned grid,
+                         cudaStream_t st, const Params& P, const TiledParams& TP, const float* s0, const float* sin,
+                         float* out, float* aux, uint32_t k, uint32_t advance, bool dipole, const CUtensorMap* map);
 bool tma_box(int family, int ty, int* lo, int* width, int* rows);
 // fused Heun step (llg_fused.cuh, instantiated by llg_fused_a.cu and
 // llg_fused_b.cu): one launch per step, s0 -> s1; tile rows fused_rows()

@@ -44,9 +44,17 @@ bool pair_rows_supported(int family) {
   return family == kFamSC || family == kFamBCC || family == kFamBCC3 || family == kFamFCC || family == kFamFCC2;
 }
 
-cudaError_t launch_tiled(int family, int ty, int rpt, int occupancy, int stage, unsigned grid, cudaStream_t st,
-                         const Params& P, const TiledParams& TP, const float* s0, const float* sin, float* out,
-                         float* aux, uint32_t k, uint32_t advance, bool dipole, const CUtensorMap* map) {
+cudaError_t launch_tiled_sc16(int rpt, int occupancy, int stage, unsigned grid, cudaStream_t st, const Params& P,
+                              const TiledParams& TP, const float* s0, const float* sin, float* out, float* aux,
+                              uint32_t k, uint32_t adv);
+
+cudaError_t launch_tiled(int family, int tz, int ty, int rpt, int occupancy, int stage, unsigned grid,
+                         cudaStream_t st, const Params& P, const TiledParams& TP, const float* s0, const float* sin,
+                         float* out, float* aux, uint32_t k, uint32_t advance, bool dipole, const CUtensorMap* map) {
+  if (tz == 16) {   // the half-width simple-cubic tile (llg_tiled_z16.cu)
+    if (family != kFamSC || ty != 8 || dipole || map) return cudaErrorInvalidValue;
+    return launch_tiled_sc16(rpt, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, advance);
+  }
   if (dipole) {
     if (rpt != 1 || map) return cudaErrorInvalidValue;
     return launch_tiled_t<true, 1, false>(family, ty, occupancy, stage, grid, st, P, TP, s0, sin, out, aux, k, advance,

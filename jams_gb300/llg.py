@@ -432,16 +432,19 @@ class Solver:
         return self.kernel_info()
 
     def set_tuning(self, planes_per_cta: int, store_rhs: bool, occupancy: int = 2, narrow: bool = False,
-                   pair: bool = False, fused: bool = False, tma: bool = False, noise: bool = False) -> None:
+                   pair: bool = False, fused: bool = False, tma: bool = False, noise: bool = False,
+                   half_z: bool = False) -> None:
         """Tiling of the tiled FP32 kernels: planes per CTA, stored-rhs mode
         (Heun: the predictor stores the corrector's partial sum s0 + dt/2
         rhs(s0) instead of the corrector recomputing rhs(s0)), occupancy
         variant 2/3/4 (two rows per thread: 2), narrow tile (half the
         rows), two rows per thread, the fused Heun step (one kernel per
         step), planes loaded by TMA, stored noise (stored-rhs mode: the
-        predictor also stores the thermal field for the corrector)."""
+        predictor also stores the thermal field for the corrector), the
+        half-width simple-cubic tile (16 cells along z)."""
         flags = int(bool(store_rhs)) | (int(bool(narrow)) << 1) | (int(bool(pair)) << 2) | \
-            (int(bool(fused)) << 3) | (int(occupancy) << 4) | (int(bool(tma)) << 8) | (int(bool(noise)) << 9)
+            (int(bool(fused)) << 3) | (int(occupancy) << 4) | (int(bool(tma)) << 8) | (int(bool(noise)) << 9) | \
+            (int(bool(half_z)) << 10)
         self._check(self.L.llg_set_tuning(self.h, int(planes_per_cta), flags))
 
     @property

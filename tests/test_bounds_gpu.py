@@ -61,6 +61,11 @@ CASES = {
                       (4, True, 2, False, True, False, True)),
     "sc_open_tma": (lambda: W.sc_ferromagnet(L=(7, 5, 12), T=50.0, periodic=(0, 1, 0)), "FP32C",
                     (2, True, 4, True, False, False, True)),
+    # the half-width simple-cubic tile: ragged z and y edges, open z, two rows
+    "sc_half_open": (lambda: W.sc_ferromagnet(L=(6, 11, 21), T=50.0, periodic=(1, 1, 0)), "FP32C",
+                     (4, True, 2, False, True, False, False, True, True)),
+    "sc_half": (lambda: W.sc_ferromagnet(L=(5, 9, 35), T=50.0), "FP32C",
+                (2, False, 3, False, False, False, False, False, True)),
 }
 
 

@@ -329,13 +329,23 @@ def test_tiling_choices_give_identical_results(llg, name):
         choices += [(4, True, 2, False, True, False, False, True)]
         if len(w.replicas) == 1:
             choices += [(6, True, 4, False, False, False, True, True)]
-    for tx, store, occ, narrow, pair, fused, tma, noise in choices:
+    choices = [c + (False,) for c in choices]
+    if name == "sc":
+        # the half-width tile (16 cells along z): one and two rows, stored
+        # or recomputed rhs, stored noise, every occupancy
+        choices += [(2, False, 2, False, False, False, False, False, True),
+                    (4, True, 3, False, False, False, False, False, True),
+                    (6, True, 4, False, False, False, False, True, True),
+                    (4, False, 2, False, True, False, False, False, True),
+                    (64, True, 2, False, True, False, False, True, True)]
+    for tx, store, occ, narrow, pair, fused, tma, noise, half in choices:
         s = solver(llg, w, llg.FP32C, steps_per_graph=4)
-        s.set_tuning(tx, store, occ, narrow, pair, fused, tma, noise)
+        s.set_tuning(tx, store, occ, narrow, pair, fused, tma, noise, half)
         assert s.kernel_info()["rows_per_thread"] == (2 if pair else 1)
         assert s.kernel_info()["fused"] == fused
         assert s.kernel_info()["tma"] == tma
         assert s.kernel_info()["stored_noise"] == noise
+        assert (s.kernel_info()["tile_z"] == 16) == half
         for r in range(len(w.replicas)):
             s.set_state(W.initial_state(w, r), r)
         s.step(11)
@@ -478,6 +488,48 @@ def test_stored_noise_with_replicas_at_zero_kelvin(llg, pair):
         outs.append([s.get_state(r) for r in range(len(w.replicas))])
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
+
+
+def test_half_width_tile_on_replicas_of_uneven_sizes(llg):
+    """The half-width simple-cubic tile on a batch of replicas whose z
+    extents are not multiples of 16 or 32, open and periodic: the same
+    states as the 32-cell tile."""
+    w = W.sc_ferromagnet(L=16, T=200.0)
+    w.replicas = [W.Replica(L=(17, 19, 23), temperature=200.0), W.Replica(L=(16, 16, 16), temperature=0.0),
+                  W.Replica(L=(9, 40, 41), temperature=600.0)]
+    outs = []
+    for half in (False, True):
+        for pair in (False, True):
+            s = solver(llg, w, llg.FP32C, steps_per_graph=4)
+            s.set_tuning(4, True, 2, pair=pair, half_z=half)
+            for r in range(len(w.replicas)):
+                s.set_state(W.initial_state(w, r), r)
+            s.step(9)
+            outs.append(s.get_state(-1))
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    w.model.periodic = (1, 0, 0)
+    outs = []
+    for half in (False, True):
+        s = solver(llg, w, llg.FP32C, steps_per_graph=4)
+        s.set_tuning(2, False, 4, half_z=half)
+        for r in range(len(w.replicas)):
+            s.set_state(W.initial_state(w, r), r)
+        s.step(7)
+        outs.append(s.get_state(-1))
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_half_width_tile_is_refused_where_unsupported(llg):
+    s = solver(llg, W.bcc_nearest_neighbour(L=8, T=300.0), llg.FP32C)
+    with pytest.raises(llg.LLGError, match="half-width tile"):
+        s.set_tuning(4, True, 2, half_z=True)
+    s = solver(llg, W.sc_ferromagnet(L=(8, 8, 40), T=10.0), llg.FP32C)
+    for kw in ({"narrow": True}, {"fused": True, "store_rhs": False}, {"tma": True}):
+        with pytest.raises(llg.LLGError, match="half-width tile"):
+            args = dict(store_rhs=True, occupancy=2)
+            args.update(kw)
+            s.set_tuning(4, half_z=True, **args)
 
 
 def test_stored_noise_needs_stored_rhs_mode(llg):
