@@ -277,8 +277,8 @@ int llg_profile_stages(llg_handle *h, int32_t nsteps, double *ms);
    kernels (0: generic gather kernels; 1 simple cubic, 2 bcc nearest
    neighbours, 3 bcc three shells, 4 triangular monolayer, 5 fcc nearest
    neighbours, 6 fcc two shells), info[1] planes
-   streamed per CTA, info[2] 1 when the Heun predictor stores rhs(s0) for
-   the corrector (else the corrector recomputes it), info[3..4] CTA tile
+   streamed per CTA, info[2] 1 when the Heun predictor stores the corrector's
+   partial sum s0 + dt/2 rhs(s0) (else the corrector recomputes rhs(s0)), info[3..4] CTA tile
    (cells along the contiguous axis, rows), info[5] 1 for FP64, info[6] the
    occupancy variant (CTAs per SM the tiled kernels were compiled for),
    info[7] rows computed per thread (1 or 2; 0 without tiled kernels),
