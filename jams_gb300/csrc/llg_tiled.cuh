@@ -19,16 +19,12 @@
 #include <cuda.h>
 
 #include <cstdint>
+#include <type_traits>
 #include <utility>
 
 #include "llg_families.h"
 #include "llg_kernels.h"
 
-// neighbour sums with packed f32x2 adds for x and y (1) or scalar adds (0);
-// both give the same sums bit for bit
-#ifndef JAMS_TILED_PACKED_GATHER
-#define JAMS_TILED_PACKED_GATHER 0
-#endif
 #include "llg_noise.cuh"
 
 namespace jams_llg {
@@ -283,8 +279,11 @@ __host__ __device__ constexpr int shell_of(int b, int k) {
   return g;
 }
 
-// one neighbour slot: every offset is a compile-time constant
-template <class F, int TZ, int TY, int B, int K>
+// one neighbour slot: every offset is a compile-time constant.  PK: the
+// x and y sums as one packed f32x2 add (the same sums bit for bit as two
+// scalar adds; fewer instructions, but in the one-row and fcc kernels the
+// packed operands cost registers and spills, so those add scalars)
+template <class F, int TZ, int TY, int B, int K, bool PK = false>
 __device__ __forceinline__ void gather_slot(const float4* bm, const float4* b0, const float4* bp,
                                             float2 (&axy)[F::NSHELL], float (&az)[F::NSHELL], float (&r)[3],
                                             const TiledParams& TP) {
@@ -294,12 +293,12 @@ __device__ __forceinline__ void gather_slot(const float4* bm, const float4* b0, 
   constexpr int g = shell_of<F>(B, K);
   const float4* p = sl.dx < 0 ? bm : (sl.dx == 0 ? b0 : bp);
   const float4 v = p[off];
-#if JAMS_TILED_PACKED_GATHER
-  axy[g] = add2(axy[g], make_float2(v.x, v.y));
-#else
-  axy[g].x = fa(axy[g].x, v.x);
-  axy[g].y = fa(axy[g].y, v.y);
-#endif
+  if constexpr (PK) {
+    axy[g] = add2(axy[g], make_float2(v.x, v.y));
+  } else {
+    axy[g].x = fa(axy[g].x, v.x);
+    axy[g].y = fa(axy[g].y, v.y);
+  }
   az[g] = fa(az[g], v.z);
   if constexpr (F::REST != 0) {
     const float* J = TP.rest[B][K];
@@ -309,11 +308,11 @@ __device__ __forceinline__ void gather_slot(const float4* bm, const float4* b0, 
   }
 }
 
-template <class F, int TZ, int TY, int B, int... K>
+template <class F, int TZ, int TY, int B, bool PK = false, int... K>
 __device__ __forceinline__ void gather_all(std::integer_sequence<int, K...>, const float4* bm, const float4* b0,
                                            const float4* bp, float2 (&axy)[F::NSHELL], float (&az)[F::NSHELL],
                                            float (&r)[3], const TiledParams& TP) {
-  (gather_slot<F, TZ, TY, B, K>(bm, b0, bp, axy, az, r, TP), ...);
+  (gather_slot<F, TZ, TY, B, K, PK>(bm, b0, bp, axy, az, r, TP), ...);
 }
 
 // Separable bcc stencils.  Shell 1 of basis site 0 is the 2x2 block
@@ -402,7 +401,7 @@ __device__ __forceinline__ void shell_combine(const TiledParams& TP, const float
 // FP32 sum of the neighbour spins of each shell (x and y packed), then
 // h += J_shell * sum with TwoProd/TwoSum compensation; 3x3 remainders (REST
 // families) per slot
-template <class F, int TZ, int TY, int B>
+template <class F, int TZ, int TY, int B, bool PK = false>
 __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const float4* ring, int xs, int own,
                                                Carry& cy, float hi[3], float lo[3]) {
   using G = Geo<F, TZ, TY>;
@@ -442,7 +441,7 @@ __device__ __forceinline__ void exchange_tiled(const TiledParams& TP, const floa
       }
     }
   } else {
-    gather_all<F, TZ, TY, B>(std::make_integer_sequence<int, F::Z>{}, bm, b0, bp, axy, az, r, TP);
+    gather_all<F, TZ, TY, B, PK>(std::make_integer_sequence<int, F::Z>{}, bm, b0, bp, axy, az, r, TP);
   }
   shell_combine<F, B>(TP, axy, az, r, hi, lo);
 }
@@ -483,24 +482,24 @@ __device__ __forceinline__ void shell_combine(const TiledParams& TP, const float
   }
 }
 
-template <class F, int TZ, int TY>
+template <class F, int TZ, int TY, bool PK = false>
 __device__ __forceinline__ void exchange_dispatch(int b, const TiledParams& TP, const float4* ring, int xs, int own,
                                                   Carry& cy, float hi[3], float lo[3]) {
   // the basis site is uniform per warp; one compile-time stencil per site
   if (F::NB == 1 || b == 0) {
-    exchange_tiled<F, TZ, TY, 0>(TP, ring, xs, own, cy, hi, lo);
+    exchange_tiled<F, TZ, TY, 0, PK>(TP, ring, xs, own, cy, hi, lo);
   } else if (b == 1) {
-    exchange_tiled<F, TZ, TY, (F::NB > 1 ? 1 : 0)>(TP, ring, xs, own, cy, hi, lo);
+    exchange_tiled<F, TZ, TY, (F::NB > 1 ? 1 : 0), PK>(TP, ring, xs, own, cy, hi, lo);
   } else if (b == 2) {
-    exchange_tiled<F, TZ, TY, (F::NB > 2 ? 2 : 0)>(TP, ring, xs, own, cy, hi, lo);
+    exchange_tiled<F, TZ, TY, (F::NB > 2 ? 2 : 0), PK>(TP, ring, xs, own, cy, hi, lo);
   } else {
-    exchange_tiled<F, TZ, TY, (F::NB > 3 ? 3 : 0)>(TP, ring, xs, own, cy, hi, lo);
+    exchange_tiled<F, TZ, TY, (F::NB > 3 ? 3 : 0), PK>(TP, ring, xs, own, cy, hi, lo);
   }
   static_assert(F::NB <= 4, "at most four basis sites per family");
 }
 
 // total field (meV) of the thread's spin from ring `ring`
-template <class F, int TZ, int TY>
+template <class F, int TZ, int TY, bool PK = false>
 __device__ __forceinline__ void field_tiled(const LocalField& L, const TiledParams& TP, int b, const float4* ring,
                                            int xs, int own, Carry& cy, float h[3], float s[3], bool has_dip,
                                            const float dip[3]) {
@@ -510,7 +509,7 @@ __device__ __forceinline__ void field_tiled(const LocalField& L, const TiledPara
   s[1] = c.y;
   s[2] = c.z;
   float hi[3], lo[3];
-  exchange_dispatch<F, TZ, TY>(b, TP, ring, xs, own, cy, hi, lo);
+  exchange_dispatch<F, TZ, TY, PK>(b, TP, ring, xs, own, cy, hi, lo);
   local_terms(L, s, hi, lo);
   if (has_dip) {   // the dipole field of this spin, precomputed by FFT convolution
 #pragma unroll
@@ -808,6 +807,9 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
   constexpr int NR = STAGE == 1 ? 2 : 1;
   constexpr int TYT = TY / RPT;   // thread rows per basis site
   constexpr bool USE_TMA = TMA && NR == 1;
+  // packed x / y neighbour sums: the two-row kernels outside the fcc
+  // families (where they measured faster without costing spills)
+  constexpr bool PACK = RPT == 2 && !std::is_same<F, FamFCC>::value && !std::is_same<F, FamFCC2>::value;
   static_assert(TY % RPT == 0, "rows per thread must divide the tile rows");
   static_assert(!USE_TMA || TmaGeo<F, TZ, TY>::FITS, "TMA box dimensions are at most 256");
   extern __shared__ __align__(128) float4 smem[];
@@ -1042,7 +1044,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
         const int i = ir[r];
         const bool st = (RPT == 1 || active[r]) && LLG_IN_RANGE(P, i, 0, (int64_t)V.L[0] * V.st[0]);
         float h[3], s[3], k[3];
-        field_tiled<F, TZ, TY>(L, TP, b, ring0, x, own[r], cy0[r], h, s, has_dip, dip[r]);
+        field_tiled<F, TZ, TY, PACK>(L, TP, b, ring0, x, own[r], cy0[r], h, s, has_dip, dip[r]);
         llg_rhs_t(L, s, h, w[r], k);
         if (STAGE == 0) {
           float v[3] = {ff(dt, k[0], s[0]), ff(dt, k[1], s[1]), ff(dt, k[2], s[2])};
@@ -1070,7 +1072,7 @@ __global__ void __launch_bounds__(Geo<F, TZ, TY, RPT>::NT, MINB)
             L0.hb[0] = hb0[0];
             L0.hb[1] = hb0[1];
             L0.hb[2] = hb0[2];
-            field_tiled<F, TZ, TY>(L0, TP, b, ring1, x, own[r], cy1[r], h0, s0v, has_dip, dip0[r]);
+            field_tiled<F, TZ, TY, PACK>(L0, TP, b, ring1, x, own[r], cy1[r], h0, s0v, has_dip, dip0[r]);
             llg_rhs_t(L, s0v, h0, w[r], r0);
 #pragma unroll
             for (int m = 0; m < 3; ++m) a[m] = ff(hdt, r0[m], s0v[m]);
