@@ -107,3 +107,25 @@ def test_reference_arm_runs_on_rank_zero_only():
     bench = _bench()
     args = bench.parse(["--impl", "reference"])
     assert bench.run_reference(args, rank=1, world=2) == 0
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` on the CPU: one JSON line with the arm's
+    metric, a cpu_baseline describing the run and an e2e object with no
+    host-device traffic (a small workload, so the test takes a second)."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--workload", "sc32",
+                          "--steps", "3", "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "spin-steps/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 3 and d["warmup"] == 3 and d["n_gpus"] == 1
+    assert d["config"]["workload"] == "sc32" and d["config"]["spins"] == 32768
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "spin-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
